@@ -1,0 +1,214 @@
+"""GB300 (sm_103a) implementation of 3DThesis's hot path, driven through its C ABI.
+
+The package is a thin ctypes layer over ``libthesis_gb300.so`` (declared in
+``include/thesis_gb300.h``).  Its ``Simulation`` class mirrors the reference's
+operator interface for the path:
+
+=======================  ==================================================================
+``Simulation(deck)``     Init::GetFileNames + Init::ReadSimParams + Grid(sim)
+``integrate(t, is_sol)`` Calc::Integrate_Serial -> the node fields xb ... expmod
+``calc_T(t, pts)``       Grid::Calc_T (set = false) at many points
+``snapshot(i)``          one snapshot of Run::Snapshots_NoTracking
+``solidify()``           Run::Solidify (Tracking None / Volume / Surface)
+``field(name)``          Grid getters (T, tSol, G, V, Gx, Gy, Gz, dTdt, eqFrac, ...)
+``simulate()``           Run::Simulate plus the CSV outputs of the reference CLI
+=======================  ==================================================================
+
+There is no CPU fallback: if the library is missing or no GPU is present the calls
+raise ``ThesisError``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Dict, Optional
+
+import numpy as np
+
+from . import decks  # noqa: F401  (re-exported workload definitions)
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libthesis_gb300.so")
+CLI_PATH = os.path.join(_HERE, "thesis_gb300")
+
+FP64 = 0
+FP32_KAHAN = 1
+_PRECISIONS = {"fp64": FP64, "fp32": FP32_KAHAN, "fp32_kahan": FP32_KAHAN, FP64: FP64, FP32_KAHAN: FP32_KAHAN}
+
+NODE_FIELDS = ("xb", "yb", "zb", "phix", "phiy", "phiz", "dtau", "expmod")
+FIELDS = ("T", "tSol", "G", "V", "Gx", "Gy", "Gz", "dTdt", "eqFrac", "numMelt", "depth", "output_flag")
+EXPORTED = ("th_ctx_create_from_deck", "th_ctx_destroy", "th_last_error", "th_get_info", "th_snapshot_time",
+            "th_nodes", "th_calc_T", "th_calc_T_device", "th_snapshot", "th_solidify", "th_field",
+            "th_simulate", "th_pairs", "th_set_tile_shape", "th_last_kernel_ms", "th_sync")
+
+
+class ThesisError(RuntimeError):
+    """A th_* call returned a non-zero status."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"[status {status}] {message}")
+        self.status = status
+
+
+class Info(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("nz", ctypes.c_int32),
+                ("pnum", ctypes.c_int64), ("n_beams", ctypes.c_int32), ("n_snapshots", ctypes.c_int32),
+                ("mode", ctypes.c_int32), ("tracking", ctypes.c_int32), ("dt", ctypes.c_double),
+                ("end_time", ctypes.c_double), ("T0", ctypes.c_double), ("TL", ctypes.c_double),
+                ("xmin", ctypes.c_double), ("xmax", ctypes.c_double), ("ymin", ctypes.c_double),
+                ("ymax", ctypes.c_double), ("zmin", ctypes.c_double), ("zmax", ctypes.c_double),
+                ("precision", ctypes.c_int32), ("out_flags", ctypes.c_int32)]
+
+
+_lib: Optional[ctypes.CDLL] = None
+
+
+def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
+    """Loads the C-ABI library (built in-tree by ``__graft_entry__.build()``)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ThesisError(-1, f"{path} is missing: build it with __graft_entry__.build()")
+    L = ctypes.CDLL(path)
+    vp, c_int, c_i64, c_d = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_double
+    L.th_ctx_create_from_deck.argtypes = [ctypes.c_char_p, c_int, ctypes.POINTER(vp)]
+    L.th_ctx_destroy.argtypes = [vp]
+    L.th_ctx_destroy.restype = None
+    L.th_last_error.argtypes = [vp]
+    L.th_last_error.restype = ctypes.c_char_p
+    L.th_get_info.argtypes = [vp, ctypes.POINTER(Info)]
+    L.th_snapshot_time.argtypes = [vp, c_int]
+    L.th_snapshot_time.restype = c_d
+    L.th_nodes.argtypes = [vp, c_d, c_int, vp, c_int, ctypes.POINTER(c_int)]
+    L.th_calc_T.argtypes = [vp, c_d, vp, c_i64, vp]
+    L.th_calc_T_device.argtypes = [vp, c_d, vp, c_i64, vp, vp]
+    L.th_sync.argtypes = [vp, vp]
+    L.th_snapshot.argtypes = [vp, c_int, vp]
+    L.th_solidify.argtypes = [vp, c_i64, ctypes.POINTER(c_i64)]
+    L.th_field.argtypes = [vp, ctypes.c_char_p, vp]
+    L.th_simulate.argtypes = [vp]
+    L.th_pairs.argtypes = [vp, ctypes.POINTER(c_i64)]
+    L.th_set_tile_shape.argtypes = [vp, c_int, c_int]
+    L.th_last_kernel_ms.argtypes = [vp, ctypes.POINTER(ctypes.c_float)]
+    _lib = L
+    return L
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Simulation:
+    """One deck on one GPU (the context is bound to the current CUDA device)."""
+
+    def __init__(self, param_input: str, precision="fp32"):
+        self._lib = load_library()
+        self._ctx = ctypes.c_void_p()
+        prec = _PRECISIONS[precision]
+        st = self._lib.th_ctx_create_from_deck(os.fspath(param_input).encode(), prec, ctypes.byref(self._ctx))
+        if st != 0:
+            raise ThesisError(st, self._lib.th_last_error(None).decode())
+        self.precision = prec
+        inf = Info()
+        self._check(self._lib.th_get_info(self._ctx, ctypes.byref(inf)))
+        self.info: Dict[str, object] = {f: getattr(inf, f) for f, _ in Info._fields_}
+
+    # ------------------------------------------------------------------ plumbing
+    def _check(self, st: int):
+        if st != 0:
+            raise ThesisError(st, self._lib.th_last_error(self._ctx).decode())
+
+    def close(self):
+        if self._ctx:
+            self._lib.th_ctx_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self) -> int:
+        return self._ctx.value
+
+    @property
+    def pnum(self) -> int:
+        return int(self.info["pnum"])
+
+    @property
+    def snapshot_times(self):
+        return [self._lib.th_snapshot_time(self._ctx, i) for i in range(int(self.info["n_snapshots"]))]
+
+    # ------------------------------------------------------------------ hot path
+    def integrate(self, t: float, is_sol: bool = False) -> Dict[str, np.ndarray]:
+        """Quadrature nodes at t, as the reference's Nodes fields."""
+        cap = 4096
+        while True:
+            buf = np.zeros((8, cap))
+            n = ctypes.c_int32()
+            self._check(self._lib.th_nodes(self._ctx, float(t), int(bool(is_sol)), _ptr(buf), cap, ctypes.byref(n)))
+            if n.value <= cap:
+                return {f: buf[i, :n.value].copy() for i, f in enumerate(NODE_FIELDS)}
+            cap = n.value
+
+    def calc_T(self, t: float, pts: Optional[np.ndarray] = None) -> np.ndarray:
+        """T at flat point ids (k fastest); all points when pts is None."""
+        if pts is None:
+            out = np.empty(self.pnum)
+            self._check(self._lib.th_calc_T(self._ctx, float(t), None, self.pnum, _ptr(out)))
+            return out
+        p = np.ascontiguousarray(pts, dtype=np.int64)
+        out = np.empty(p.size)
+        self._check(self._lib.th_calc_T(self._ctx, float(t), _ptr(p), p.size, _ptr(out)))
+        return out
+
+    def calc_T_device(self, t: float, d_pts: int, n: int, d_T: int, stream: int = 0):
+        """Device-pointer form (integers are raw CUDA addresses, e.g. tensor.data_ptr())."""
+        self._check(self._lib.th_calc_T_device(self._ctx, float(t), ctypes.c_void_p(d_pts or None), int(n),
+                                               ctypes.c_void_p(d_T), ctypes.c_void_p(stream or None)))
+
+    def sync(self, stream: int = 0):
+        self._check(self._lib.th_sync(self._ctx, ctypes.c_void_p(stream or None)))
+
+    def snapshot(self, idx: int, out: Optional[np.ndarray] = None, copy: bool = True) -> Optional[np.ndarray]:
+        if copy and out is None:
+            out = np.empty(self.pnum)
+        self._check(self._lib.th_snapshot(self._ctx, int(idx), _ptr(out) if copy else None))
+        return out
+
+    def solidify(self, max_steps: int = 0) -> int:
+        steps = ctypes.c_int64()
+        self._check(self._lib.th_solidify(self._ctx, int(max_steps), ctypes.byref(steps)))
+        return steps.value
+
+    def field(self, name: str) -> np.ndarray:
+        out = np.empty(self.pnum)
+        self._check(self._lib.th_field(self._ctx, name.encode(), _ptr(out)))
+        return out
+
+    def simulate(self):
+        self._check(self._lib.th_simulate(self._ctx))
+
+    @property
+    def pairs(self) -> int:
+        v = ctypes.c_int64()
+        self._check(self._lib.th_pairs(self._ctx, ctypes.byref(v)))
+        return v.value
+
+    def set_tile_shape(self, kp: int, kch: int):
+        self._check(self._lib.th_set_tile_shape(self._ctx, int(kp), int(kch)))
+
+    @property
+    def last_kernel_ms(self) -> float:
+        v = ctypes.c_float()
+        self._check(self._lib.th_last_kernel_ms(self._ctx, ctypes.byref(v)))
+        return v.value

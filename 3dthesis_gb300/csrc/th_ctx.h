@@ -1,0 +1,43 @@
+// The context behind the C ABI's opaque th_ctx handle.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "../../include/thesis_gb300.h"
+#include "th_kernels.h"
+#include "th_problem.h"
+
+struct RunState;   // solidification state (th_run.cu)
+
+struct th_ctx {
+  HostProblem hp;
+  DevProblem dp;
+  int precision = TH_FP32_KAHAN;
+  int device = -1;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  float last_ms = 0.f;
+  std::string err;
+
+  DevSeg* d_segs = nullptr;
+  void* node_mem = nullptr;
+  NodeBufView nb{};
+  int* d_small = nullptr;                 // [0] node count, [1] error bits, [2..] scratch
+  unsigned long long* d_pairs = nullptr;  // point x node pairs evaluated
+  int last_count = 0;
+  TileShape shape{4, 2};
+
+  double* d_T = nullptr;       size_t T_bytes = 0;   bool T_valid = false;
+  int64_t* d_pts = nullptr;    size_t pts_bytes = 0;
+  double* d_Tlist = nullptr;   size_t Tlist_bytes = 0;
+  double* d_export = nullptr;  size_t export_bytes = 0;
+
+  RunState* run = nullptr;
+};
+
+th_status th_fail(th_ctx* ctx, th_status code, const std::string& msg);
+th_status th_cuda_check(th_ctx* ctx, cudaError_t e, const char* what);
+th_status th_gen_nodes_checked(th_ctx* ctx, double t, bool is_sol);
+th_status th_ensure(th_ctx* ctx, void** ptr, size_t* cap_bytes, size_t need);
+void th_release_run_state(th_ctx* ctx);

@@ -1,0 +1,36 @@
+// Launch wrappers for the device kernels (host side).
+#pragma once
+#include <cuda_runtime.h>
+#include "th_problem.h"
+
+// Device node list: structure-of-arrays, capacity `cap`.
+//  doubles: x y z ipx ipy ipz dtau amp   (amp = q beta / sqrt(phix phiy phiz))
+//  floats : kx ky kz w                   (k = -3 log2(e) / phi, w = dtau * amp)
+//           xh xl yh yl zh zl            (coordinates split into two floats)
+struct NodeBufView {
+  double *x, *y, *z, *ipx, *ipy, *ipz, *dtau, *amp;
+  float *kx, *ky, *kz, *w, *xh, *xl, *yh, *yl, *zh, *zl;
+  int cap;
+};
+
+// Tile shape of the whole-grid point x node kernels: 256 threads, each owning KP
+// consecutive k-points of one (i, j) column; KCH k-chunks per tile.
+struct TileShape { int kp, kch; };
+
+// Generates the node list at time t into nb with one warp; *d_count receives the
+// total, *d_err the error bits (capacity / walk limit).
+void th_launch_nodes(const DevProblem& P, double t, bool is_sol, const NodeBufView& nb, int* d_count, int* d_err,
+                     cudaStream_t s);
+
+// T at every grid point (p = i*ny*nz + j*nz + k) from the node list.
+void th_launch_grid_sum(const DevProblem& P, const NodeBufView& nb, const int* d_count, double* d_T, int precision,
+                        TileShape shape, unsigned long long* d_pairs, cudaStream_t s);
+
+// T at n listed points.
+void th_launch_list_sum(const DevProblem& P, const NodeBufView& nb, const int* d_count, const int64_t* d_pts,
+                        int64_t n, double* d_T, int precision, unsigned long long* d_pairs, cudaStream_t s);
+
+// Converts the node list into the reference's 8 fields (expmod = log(amp)) in out[8][cap].
+void th_launch_nodes_export(const NodeBufView& nb, const int* d_count, double* d_out, int cap, cudaStream_t s);
+
+bool th_tile_shape_supported(TileShape shape);

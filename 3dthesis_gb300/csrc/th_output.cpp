@@ -1,0 +1,61 @@
+// CSV output in the reference's layout (src/Grid.cpp:72-99, column order from the Grid
+// constructor, src/Grid.h:138-254): a header of the enabled field names, then one row
+// per output point in point order, every value printed as an ostream would print a double
+// with the default precision of 6 significant digits.
+#include "th_output.h"
+
+#include <sys/stat.h>
+#include <sys/types.h>
+
+#include <cstdio>
+#include <string>
+
+std::string th_data_dir(const HostProblem& hp) { return hp.dir + "/Data"; }
+
+bool th_write_csv(const HostProblem& hp, const std::string& tag, const std::vector<std::string>& names,
+                  const std::vector<const double*>& cols, const unsigned char* flag, std::string& err) {
+  if (names.empty()) return true;
+  const std::string dir = th_data_dir(hp);
+  mkdir(dir.c_str(), 0777);
+  const std::string path = dir + "/" + hp.name + "." + tag + ".csv";
+  FILE* f = std::fopen(path.c_str(), "w");
+  if (!f) { err = "cannot write " + path; return false; }
+  std::vector<char> buf(1 << 20);
+  std::setvbuf(f, buf.data(), _IOFBF, buf.size());
+  for (size_t c = 0; c < names.size(); ++c) std::fprintf(f, c ? ",%s" : "%s", names[c].c_str());
+  std::fputc('\n', f);
+  const int64_t n = hp.pnum;
+  for (int64_t p = 0; p < n; ++p) {
+    if (flag && !flag[p]) continue;
+    for (size_t c = 0; c < cols.size(); ++c) std::fprintf(f, c ? ",%g" : "%g", cols[c][p]);
+    std::fputc('\n', f);
+  }
+  const bool ok = std::fclose(f) == 0;
+  if (!ok) err = "error writing " + path;
+  return ok;
+}
+
+void th_grid_coords(const HostProblem& hp, std::vector<double>& x, std::vector<double>& y, std::vector<double>& z) {
+  const int gx = (uint16_t)hp.nx, gy = (uint16_t)hp.ny, gz = (uint16_t)hp.nz;
+  const double hx = gx > 1 ? (hp.xmax - hp.xmin) / (gx - 1) : 0.0;
+  const double hy = gy > 1 ? (hp.ymax - hp.ymin) / (gy - 1) : 0.0;
+  const double hz = gz > 1 ? (hp.zmax - hp.zmin) / (gz - 1) : 0.0;
+  x.resize(hp.pnum); y.resize(hp.pnum); z.resize(hp.pnum);
+  int64_t p = 0;
+  for (int i = 0; i < hp.nx; ++i) {
+    const double xv = (gx - 1) ? hp.xmin + (double(i) * hx) : hp.xmax;
+    for (int j = 0; j < hp.ny; ++j) {
+      const double yv = (gy - 1) ? hp.ymin + (double(j) * hy) : hp.ymax;
+      for (int k = 0; k < hp.nz; ++k, ++p) {
+        x[p] = xv; y[p] = yv;
+        z[p] = (gz - 1) ? hp.zmin + (double(k) * hz) : hp.zmax;
+      }
+    }
+  }
+}
+
+std::string th_zero_pad(int v, int width) {
+  char b[32];
+  std::snprintf(b, sizeof(b), "%0*d", width, v);
+  return b;
+}

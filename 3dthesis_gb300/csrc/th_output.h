@@ -1,0 +1,13 @@
+#pragma once
+#include <string>
+#include <vector>
+
+#include "th_problem.h"
+
+std::string th_data_dir(const HostProblem& hp);
+// Writes <deck dir>/Data/<name>.<tag>.csv; rows only where flag[p] (all rows if flag is null).
+bool th_write_csv(const HostProblem& hp, const std::string& tag, const std::vector<std::string>& names,
+                  const std::vector<const double*>& cols, const unsigned char* flag, std::string& err);
+// Point coordinates exactly as the reference's Grid getters compute them.
+void th_grid_coords(const HostProblem& hp, std::vector<double>& x, std::vector<double>& y, std::vector<double>& z);
+std::string th_zero_pad(int v, int width);

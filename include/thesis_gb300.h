@@ -1,0 +1,135 @@
+/*
+ * thesis_gb300 - C ABI of the GB300 (sm_103a) implementation of the 3DThesis hot path:
+ * the time integral of the moving 3D-Gaussian heat source, summed over adaptive Gauss
+ * quadrature nodes on the scan path, at every tracked grid point.
+ *
+ * Plain C types only (no CUDA or torch types).  Every call returns a th_status; on an
+ * error th_last_error(ctx) (or th_last_error(NULL) for failed creation) describes it.
+ * A context owns every device buffer it uses and is bound to the CUDA device that was
+ * current when it was created.  Contexts are independent; one context must not be used
+ * from two host threads at once.
+ *
+ * Reference interfaces each entry point replaces (paths inside the 3DThesis tree):
+ *   th_ctx_create_from_deck  Init::GetFileNames + Init::ReadSimParams + Grid(sim)
+ *                            (src/Init.cpp:233-303, src/Grid.h:120-280, bin/Main.cpp:62-74)
+ *   th_nodes                 Calc::Integrate_Serial (src/Calc.h:23, src/Calc.cpp:48-65)
+ *   th_calc_T                Grid::Calc_T with set = false over many points
+ *                            (src/Grid.h:290, src/Grid.cpp:275-314)
+ *   th_snapshot              one iteration of Run::Snapshots_NoTracking (src/Run.cpp:80-124)
+ *   th_solidify              Run::Solidify (src/Run.cpp:390-709): NoTracking, Volume, Surface
+ *   th_simulate              Run::Simulate + the final outputs of bin/Main.cpp:88-118
+ *   th_field                 the Grid getters (src/Grid.h:299-370)
+ */
+#ifndef THESIS_GB300_H
+#define THESIS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int th_status;
+enum {
+  TH_OK = 0,
+  TH_ERR_INVALID = 1,      /* bad argument or input deck */
+  TH_ERR_IO = 2,           /* file could not be read or written */
+  TH_ERR_CUDA = 3,         /* a CUDA call failed */
+  TH_ERR_CAPACITY = 4,     /* a fixed-size buffer or limit was exceeded */
+  TH_ERR_UNSUPPORTED = 5,  /* a reference feature this build does not implement */
+  TH_ERR_TIMEOUT = 6       /* a bounded device loop gave up */
+};
+
+/* Arithmetic of the point x node sums. */
+enum {
+  TH_FP64 = 0,        /* plain double precision, the reference's arithmetic */
+  TH_FP32_KAHAN = 1   /* FP32 pair terms, Kahan-compensated FP32 sums, FP64 node
+                         generation and FP64 node-to-tile offsets */
+};
+
+typedef struct th_ctx th_ctx;
+
+typedef struct th_info {
+  int32_t nx, ny, nz;          /* grid points per axis (k fastest: p = i*ny*nz + j*nz + k) */
+  int64_t pnum;                /* nx*ny*nz */
+  int32_t n_beams;
+  int32_t n_snapshots;
+  int32_t mode;                /* 0 Snapshots, 1 Solidification */
+  int32_t tracking;            /* 0 None, 1 Volume, 2 Surface */
+  double dt;                   /* solidification timestep (s) */
+  double end_time;             /* end of the last scan path (s) */
+  double T0, TL;               /* initial and liquidus temperature (K) */
+  double xmin, xmax, ymin, ymax, zmin, zmax;
+  int32_t precision;
+  int32_t out_flags;           /* bit mask of requested output fields, TH_OUT_* */
+} th_info;
+
+/* Output field bits (the reference's Output.txt keywords). */
+enum {
+  TH_OUT_T = 1 << 0, TH_OUT_TSOL = 1 << 1, TH_OUT_G = 1 << 2, TH_OUT_GX = 1 << 3,
+  TH_OUT_GY = 1 << 4, TH_OUT_GZ = 1 << 5, TH_OUT_V = 1 << 6, TH_OUT_DTDT = 1 << 7,
+  TH_OUT_EQFRAC = 1 << 8, TH_OUT_DEPTH = 1 << 9, TH_OUT_NUMMELT = 1 << 10
+};
+
+/* Creates a context from a deck's ParamInput.txt.  File names inside the deck are
+ * resolved relative to the directory of param_input (the reference opens them relative
+ * to its working directory, which is that directory when run as `3DThesis ParamInput.txt`). */
+th_status th_ctx_create_from_deck(const char* param_input, int32_t precision, th_ctx** out);
+void th_ctx_destroy(th_ctx* ctx);
+const char* th_last_error(const th_ctx* ctx);
+th_status th_get_info(th_ctx* ctx, th_info* out);
+double th_snapshot_time(th_ctx* ctx, int32_t idx);
+
+/* Quadrature nodes at time t (is_sol != 0: the refined solidification schedule).
+ * Writes 8 arrays of length cap, in this order: xb, yb, zb, 1/phix, 1/phiy, 1/phiz, dtau,
+ * expmod (the reference's Nodes fields).  *n_out receives the node count; when it exceeds
+ * cap only the first cap nodes are written. */
+th_status th_nodes(th_ctx* ctx, double t, int32_t is_sol, double* out, int32_t cap, int32_t* n_out);
+
+/* T at n grid points (flat ids) from the nodes at t; host buffers.  pts == NULL means
+ * every grid point (n must then equal pnum). */
+th_status th_calc_T(th_ctx* ctx, double t, const int64_t* pts, int64_t n, double* T_out);
+
+/* The same with device buffers, enqueued on `stream` (a cudaStream_t; NULL = the
+ * context's own stream).  Returns after enqueueing, without synchronising: a device-side
+ * failure (node list larger than its buffer, walk step limit) is reported by th_sync or by
+ * the next synchronous call on the context. */
+th_status th_calc_T_device(th_ctx* ctx, double t, const int64_t* d_pts, int64_t n, double* d_T,
+                           void* stream);
+
+/* Waits for `stream` (NULL: only the context's own stream) and reports any device-side
+ * error latched since the last check. */
+th_status th_sync(th_ctx* ctx, void* stream);
+
+/* Snapshot idx of a Snapshots deck over the whole grid: T for every point (host buffer,
+ * pnum doubles).  T_out == NULL leaves the result in the context's device buffer. */
+th_status th_snapshot(th_ctx* ctx, int32_t idx, double* T_out);
+
+/* Runs the Solidification loop of the deck on the device.  max_steps <= 0 runs to the
+ * reference's finish test (t past the end of every path and no liquid point left).
+ * *steps_out (may be NULL) receives the number of timesteps taken. */
+th_status th_solidify(th_ctx* ctx, int64_t max_steps, int64_t* steps_out);
+
+/* Copies a per-point field (pnum doubles) to host memory after th_snapshot/th_solidify:
+ * "T", "tSol", "G", "V", "Gx", "Gy", "Gz", "dTdt", "eqFrac", "numMelt", "depth",
+ * "output_flag". */
+th_status th_field(th_ctx* ctx, const char* name, double* out);
+
+/* Whole run as the reference CLI does it: the mode loop, then the CSV files under
+ * <deck dir>/Data (same names, columns and number format). */
+th_status th_simulate(th_ctx* ctx);
+
+/* Point x node pairs evaluated by this context so far (temperature and gradient sums). */
+th_status th_pairs(th_ctx* ctx, int64_t* out);
+
+/* Tile shape of the whole-grid kernels: kp k-points per thread, kch k-chunks per tile
+ * (supported: kp 4 with kch 1/2/4, kp 2 with kch 2/4, kp 8 with kch 1/2). */
+th_status th_set_tile_shape(th_ctx* ctx, int32_t kp, int32_t kch);
+
+/* Device time (ms) of the most recent th_snapshot's point x node kernel. */
+th_status th_last_kernel_ms(th_ctx* ctx, float* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* THESIS_GB300_H */

@@ -1,0 +1,103 @@
+/*
+ * TEST INFRASTRUCTURE ONLY.  A thin C entry layer over the UNMODIFIED 3DThesis
+ * library, compiled from the reference's own sources by oracle/Makefile (target
+ * "ref") into oracle/_ref/.  It exists to pin the oracle and to generate the golden
+ * fixtures under tests/golden/; nothing in the product or in the GPU-box tests loads it.
+ *
+ * Entry points call the reference's public interface:
+ *   Init::GetFileNames / Init::ReadSimParams (src/Init.h), Grid (src/Grid.h),
+ *   Calc::Integrate_Serial (src/Calc.h:23), Grid::Calc_T (src/Grid.h:290),
+ *   Run::Simulate (src/Run.h), and the Grid getters (src/Grid.h:299-370).
+ */
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <unistd.h>
+
+#include "DataStructs.h"
+#include "Grid.h"
+#include "Init.h"
+#include "Run.h"
+#include "Calc.h"
+#include "Util.h"
+
+struct RefRun {
+  Simdat sim;
+  Grid* grid = nullptr;
+};
+
+extern "C" {
+
+// Loads a deck the way bin/Main.cpp:44-77 does; the working directory becomes the
+// deck's directory because the reference opens the files named in ParamInput.txt
+// relative to the working directory.
+void* ref_load(const char* deck_dir) {
+  if (chdir(deck_dir) != 0) return nullptr;
+  RefRun* r = new RefRun();
+  r->sim.print = false;
+  Init::GetFileNames(r->sim.files, "ParamInput.txt", r->sim.print);
+  Init::ReadSimParams(r->sim);
+  r->grid = new Grid(r->sim);
+  r->sim.util.approxEndTime = r->sim.util.allScansEndTime;
+  return r;
+}
+
+void ref_info(void* h, double* info) {
+  RefRun* r = (RefRun*)h;
+  info[0] = r->sim.domain.xnum; info[1] = r->sim.domain.ynum; info[2] = r->sim.domain.znum;
+  info[3] = r->sim.domain.pnum; info[4] = (double)r->sim.beams.size();
+  info[5] = (double)r->sim.param.SnapshotTimes.size(); info[6] = r->sim.util.allScansEndTime;
+  info[7] = r->sim.settings.r_max;
+}
+
+double ref_snapshot_time(void* h, int i) { return ((RefRun*)h)->sim.param.SnapshotTimes.at(i); }
+
+int ref_nodes(void* h, double t, int is_sol, double* out, int cap) {
+  RefRun* r = (RefRun*)h;
+  Nodes nodes;
+  Calc::Integrate_Serial(nodes, r->sim, t, is_sol != 0);
+  const int n = (int)nodes.size;
+  const int m = n < cap ? n : cap;
+  const vector<double>* f[8] = {&nodes.xb, &nodes.yb, &nodes.zb, &nodes.phix, &nodes.phiy, &nodes.phiz, &nodes.dtau, &nodes.expmod};
+  for (int c = 0; c < 8; ++c) for (int i = 0; i < m; ++i) out[(size_t)c * cap + i] = (*f[c])[i];
+  return n;
+}
+
+void ref_calc_T(void* h, double t, const int64_t* pts, int64_t n, double* T) {
+  RefRun* r = (RefRun*)h;
+  Nodes nodes;
+  Calc::Integrate_Serial(nodes, r->sim, t, false);
+  for (int64_t i = 0; i < n; ++i) T[i] = r->grid->Calc_T(t, nodes, r->sim, false, (int)pts[i]);
+}
+
+void ref_simulate(void* h) {
+  RefRun* r = (RefRun*)h;
+  Run::Simulate(*r->grid, r->sim);
+}
+
+int ref_field(void* h, const char* name, double* out) {
+  RefRun* r = (RefRun*)h;
+  Grid& g = *r->grid;
+  const std::string f(name);
+  const int n = r->sim.domain.pnum;
+  for (int p = 0; p < n; ++p) {
+    double v;
+    if (f == "T") v = g.get_T(p);
+    else if (f == "tSol") v = g.get_tSol(p);
+    else if (f == "G") v = g.get_G(p);
+    else if (f == "V") v = g.get_V(p);
+    else if (f == "Gx") v = g.get_Gx(p);
+    else if (f == "Gy") v = g.get_Gy(p);
+    else if (f == "Gz") v = g.get_Gz(p);
+    else if (f == "dTdt") v = g.get_dTdt(p);
+    else if (f == "eqFrac") v = g.get_eqFrac(p);
+    else if (f == "numMelt") v = g.get_numMelt(p);
+    else if (f == "depth") v = g.get_depth(p);
+    else if (f == "output_flag") v = g.get_output_flag(p) ? 1.0 : 0.0;
+    else return 2;
+    out[p] = v;
+  }
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,57 @@
+/*
+ * TEST INFRASTRUCTURE ONLY.  CPU restatement of the 3DThesis hot path, used as the
+ * parity oracle and as the timed CPU baseline.  Nothing in the product links it.
+ *
+ * It restates, in double precision and in the reference's own operation order:
+ *   - the keyword-file input layer            (src/Init.cpp:33-908)
+ *   - quadrature-node generation              (src/Calc.cpp:48-211, src/Util.cpp:40-50,145-237)
+ *   - method-of-images boundary nodes         (src/Calc.cpp:503-608)
+ *   - the point x node temperature sum        (src/Grid.cpp:275-314)
+ *   - solidification time / G / V / dT/dt     (src/Grid.cpp:316-453, 522-548)
+ *   - beam trace, frontier expansion, depth   (src/Melt.cpp:20-357)
+ *   - the snapshot and solidification drivers (src/Run.cpp:80-124, 409-709)
+ *
+ * Pinned against the reference itself: tests/golden/ holds vectors produced by the
+ * reference compiled from its own sources (oracle/Makefile, target "ref").
+ */
+#pragma once
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Parse a deck (ParamInput.txt).  Returns an opaque handle or NULL (message in err). */
+void* or_load(const char* param_input, char* err, int errlen);
+void  or_free(void* h);
+
+/* info[0..15]: nx, ny, nz, pnum, n_beams, n_snapshots, mode(0 snap,1 sol),
+ * tracking(0 None,1 Volume,2 Surface), dt, end_time, T0, TL, r_max, a, threads, use_bcs */
+void  or_info(void* h, double* info);
+double or_snapshot_time(void* h, int idx);
+
+/* Quadrature nodes at t (reference field order: xb yb zb 1/phix 1/phiy 1/phiz dtau expmod),
+ * written as 8 consecutive arrays of length cap.  Returns the node count (may exceed cap:
+ * then only cap are written). */
+int   or_nodes(void* h, double t, int is_sol, double* out, int cap);
+
+/* T at the given points (flat ids, k fastest) from the nodes at t.  threads<=0: all. */
+void  or_calc_T(void* h, double t, const int64_t* pts, int64_t n, double* T, int threads);
+
+/* Snapshot idx over the whole grid (Snapshots_NoTracking). */
+void  or_snapshot(void* h, int idx, double* T, int threads);
+
+/* Full solidification run (Solidify_NoTracking / _Volume / _Surface).  max_steps<=0: until
+ * the reference's finish test.  Returns the number of steps taken. */
+int64_t or_solidify(void* h, int threads, int64_t max_steps);
+
+/* Per-point field after or_solidify: "T", "tSol", "G", "V", "Gx", "Gy", "Gz", "dTdt",
+ * "eqFrac", "numMelt", "depth", "output_flag".  Returns 0 on success. */
+int   or_field(void* h, const char* name, double* out);
+
+/* Point x node pairs evaluated since load (temperature sums + gradient sums). */
+int64_t or_pairs(void* h);
+
+#ifdef __cplusplus
+}
+#endif

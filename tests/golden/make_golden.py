@@ -1,0 +1,148 @@
+"""Generate the golden fixtures in this directory from the UNMODIFIED reference.
+
+Run from the repository root, on a machine holding the 3DThesis sources:
+
+    make -C oracle ref REF=/path/to/3DThesis     # builds oracle/_ref/libthesis_ref.so
+    python tests/golden/make_golden.py
+
+Each deck is written to a scratch directory and loaded by the reference library in its
+own process (the reference keeps function-static state).  The fixtures hold:
+
+* ``nodes_<deck>.npz``  - quadrature node lists (8 fields) at the deck's snapshot times,
+  plus ``is_sol`` lists at the same times (Calc::Integrate_Serial).
+* ``temp_snapshot_raster.npz`` - T at 4096 seeded points of the 200x100x40 raster grid at
+  its three snapshot times (Grid::Calc_T with set = false).
+* ``run_<deck>.npz`` - a full Run::Simulate on a small solidification deck: the packed
+  molten-point mask, per-field checksums over all output points, and every output
+  field at a seeded subset of 1500 output points.
+"""
+from __future__ import annotations
+
+import importlib
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+decks = importlib.import_module("3dthesis_gb300.decks")
+REF_LIB = os.path.join(ROOT, "oracle", "_ref", "libthesis_ref.so")
+
+_CHILD = r"""
+import ctypes, sys, numpy as np
+L = ctypes.CDLL(sys.argv[1]); L.ref_load.restype = ctypes.c_void_p
+L.ref_snapshot_time.restype = ctypes.c_double
+job = dict(np.load(sys.argv[3], allow_pickle=True))
+h = ctypes.c_void_p(L.ref_load(sys.argv[2].encode()))
+info = np.zeros(8); L.ref_info(h, info.ctypes.data_as(ctypes.c_void_p))
+out = {"info": info}
+cap = 60000
+def nodes(t, sol):
+    buf = np.zeros(8 * cap)
+    n = L.ref_nodes(h, ctypes.c_double(t), sol, buf.ctypes.data_as(ctypes.c_void_p), cap)
+    return buf.reshape(8, cap)[:, :n].copy()
+if "times" in job:
+    for i, t in enumerate(job["times"]):
+        out[f"t{i}"] = np.float64(t)
+        out[f"nodes{i}"] = nodes(float(t), 0)
+        out[f"sol_nodes{i}"] = nodes(float(t), 1)
+if "pts" in job:
+    pts = job["pts"].astype(np.int64)
+    for i in range(int(info[5])):
+        t = L.ref_snapshot_time(h, i); T = np.zeros(len(pts))
+        L.ref_calc_T(h, ctypes.c_double(t), pts.ctypes.data_as(ctypes.c_void_p), ctypes.c_int64(len(pts)),
+                     T.ctypes.data_as(ctypes.c_void_p))
+        out[f"t{i}"] = np.float64(t); out[f"T{i}"] = T
+if "fields" in job:
+    L.ref_simulate(h)
+    for f in job["fields"]:
+        a = np.zeros(int(info[3])); L.ref_field(h, str(f).encode(), a.ctypes.data_as(ctypes.c_void_p)); out[str(f)] = a
+np.savez(sys.argv[4], **out)
+"""
+
+
+def run_ref(deck, job: dict, scratch: str) -> dict:
+    d = os.path.join(scratch, deck.name)
+    deck.write(d)
+    jf, of = os.path.join(scratch, "job.npz"), os.path.join(scratch, "out.npz")
+    np.savez(jf, **job)
+    subprocess.run([sys.executable, "-c", _CHILD, REF_LIB, d, jf, of], check=True,
+                   stdout=subprocess.DEVNULL)
+    return dict(np.load(of))
+
+
+def node_fixture(deck, times, scratch):
+    r = run_ref(deck, {"times": np.asarray(times, dtype=np.float64)}, scratch)
+    np.savez_compressed(os.path.join(HERE, f"nodes_{deck.name}.npz"), **r)
+    return r
+
+
+def run_fixture(deck, scratch, tag):
+    fields = ["T", "output_flag"] + [f for f in ("tSol", "G", "V", "Gx", "Gy", "Gz", "dTdt", "eqFrac",
+                                                 "numMelt", "depth") if deck.outputs.get(f)]
+    r = run_ref(deck, {"fields": np.asarray(fields)}, scratch)
+    flag = r["output_flag"] > 0
+    idx = np.flatnonzero(flag)
+    rng = np.random.default_rng(1234)
+    sub = np.sort(rng.choice(idx, min(1500, idx.size), replace=False)) if idx.size else idx
+    out = {"info": r["info"], "mask": np.packbits(flag), "n_points": np.int64(flag.size), "sample": sub}
+    for f in fields:
+        if f == "output_flag":
+            continue
+        v = r[f][flag]
+        out[f"{f}_sum"] = np.float64(np.sum(v))
+        out[f"{f}_abssum"] = np.float64(np.sum(np.abs(v)))
+        out[f"{f}_max"] = np.float64(np.max(v)) if v.size else np.float64(0)
+        out[f"{f}_sample"] = r[f][sub]
+    np.savez_compressed(os.path.join(HERE, f"run_{tag}.npz"), **out)
+    return out
+
+
+RASTER_END = 0.0380224859550507   # end of the 10 x 2 mm raster (s)
+NODE_TIMES = {
+    "snapshot_raster": [0.25 * RASTER_END, 0.5 * RASTER_END, RASTER_END, 0.012345678, 0.03, RASTER_END + 2e-3],
+    "small_spots": [0.3e-3, 0.9e-3, 1.7e-3, 2.52e-3, 3.1e-3],
+    "small_multibeam": [1e-4, 5e-4, 1.5e-3, 2.5e-3],
+    "small_bcs": [0.4e-3, 1.2e-3, 3.0e-3],
+}
+RUNS = {"small_surface": ("small_surface", "Surface"), "small_volume": ("small_surface", "Volume"),
+        "small_none": ("small_surface", "None"), "small_multibeam": ("small_multibeam",)}
+
+
+def node_deck(name):
+    """The deck each nodes_<name>.npz fixture was made from."""
+    if name == "small_bcs":
+        d = decks.small_snapshot()
+        d.name = "small_bcs"
+        d.bcs = {"X_min": -0.02e-3, "X_max": 0.6e-3, "Y_min": -0.05e-3, "Z_min": -0.2e-3, "Reflections": 2}
+        return d
+    return getattr(decks, name)()
+
+
+def run_deck(tag):
+    """The deck each run_<tag>.npz fixture was made from."""
+    fn, *args = RUNS[tag]
+    return getattr(decks, fn)(*args)
+
+
+def main():
+    if not os.path.exists(REF_LIB):
+        sys.exit(f"missing {REF_LIB}: build it with `make -C oracle ref`")
+    with tempfile.TemporaryDirectory() as scratch:
+        for name, times in NODE_TIMES.items():
+            node_fixture(node_deck(name), times, scratch)
+        rng = np.random.default_rng(7)
+        pts = np.sort(rng.choice(800000, 4096, replace=False)).astype(np.int64)
+        r = run_ref(decks.snapshot_raster(), {"pts": pts}, scratch)
+        np.savez_compressed(os.path.join(HERE, "temp_snapshot_raster.npz"), pts=pts, **r)
+        for tag in RUNS:
+            run_fixture(run_deck(tag), scratch, tag)
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

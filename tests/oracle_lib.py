@@ -1,0 +1,95 @@
+"""ctypes wrapper of the CPU oracle (oracle/liboracle.so) - test infrastructure."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB = os.path.join(ROOT, "oracle", "liboracle.so")
+NODE_FIELDS = ("xb", "yb", "zb", "phix", "phiy", "phiz", "dtau", "expmod")
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        src = os.path.join(ROOT, "oracle", "thesis_oracle.cpp")
+        if not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
+            subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+        L = ctypes.CDLL(LIB)
+        vp = ctypes.c_void_p
+        L.or_load.restype = vp
+        L.or_load.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int]
+        L.or_free.argtypes = [vp]
+        L.or_info.argtypes = [vp, vp]
+        L.or_snapshot_time.argtypes = [vp, ctypes.c_int]
+        L.or_snapshot_time.restype = ctypes.c_double
+        L.or_nodes.argtypes = [vp, ctypes.c_double, ctypes.c_int, vp, ctypes.c_int]
+        L.or_calc_T.argtypes = [vp, ctypes.c_double, vp, ctypes.c_int64, vp, ctypes.c_int]
+        L.or_snapshot.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int]
+        L.or_solidify.argtypes = [vp, ctypes.c_int, ctypes.c_int64]
+        L.or_solidify.restype = ctypes.c_int64
+        L.or_field.argtypes = [vp, ctypes.c_char_p, vp]
+        L.or_pairs.argtypes = [vp]
+        L.or_pairs.restype = ctypes.c_int64
+        _lib = L
+    return Oracle
+
+
+class Oracle:
+    def __init__(self, param_input):
+        load()
+        err = ctypes.create_string_buffer(512)
+        self.h = _lib.or_load(os.fspath(param_input).encode(), err, 512)
+        if not self.h:
+            raise RuntimeError(err.value.decode())
+        info = np.zeros(16)
+        _lib.or_info(self.h, info.ctypes.data_as(ctypes.c_void_p))
+        self.nx, self.ny, self.nz, self.pnum = (int(v) for v in info[:4])
+        self.n_snapshots = int(info[5])
+        self.end_time = info[9]
+        self.T0, self.TL = info[10], info[11]
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            _lib.or_free(self.h)
+            self.h = None
+
+    def snapshot_time(self, i):
+        return _lib.or_snapshot_time(self.h, i)
+
+    def nodes(self, t, is_sol=False):
+        cap = 4096
+        while True:
+            buf = np.zeros((8, cap))
+            n = _lib.or_nodes(self.h, float(t), int(is_sol), buf.ctypes.data_as(ctypes.c_void_p), cap)
+            if n <= cap:
+                return {f: buf[i, :n].copy() for i, f in enumerate(NODE_FIELDS)}
+            cap = n
+
+    def calc_T(self, t, pts, threads=0):
+        p = np.ascontiguousarray(pts, dtype=np.int64)
+        out = np.empty(p.size)
+        _lib.or_calc_T(self.h, float(t), p.ctypes.data_as(ctypes.c_void_p), p.size,
+                       out.ctypes.data_as(ctypes.c_void_p), threads)
+        return out
+
+    def snapshot(self, i, threads=0):
+        out = np.empty(self.pnum)
+        _lib.or_snapshot(self.h, i, out.ctypes.data_as(ctypes.c_void_p), threads)
+        return out
+
+    def solidify(self, threads=0, max_steps=0):
+        return _lib.or_solidify(self.h, threads, max_steps)
+
+    def field(self, name):
+        out = np.empty(self.pnum)
+        rc = _lib.or_field(self.h, name.encode(), out.ctypes.data_as(ctypes.c_void_p))
+        if rc:
+            raise KeyError(name)
+        return out
+
+    @property
+    def pairs(self):
+        return _lib.or_pairs(self.h)

@@ -1,0 +1,58 @@
+"""C-ABI library: loads, exports every declared symbol, and rejects bad decks on the host."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = []
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if h.endswith(".h"):
+            text = open(os.path.join(ROOT, "include", h)).read()
+            names += re.findall(r"^\w[\w\s\*]*?\b(th_\w+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol(built_library):
+    lib = ctypes.CDLL(built_library)
+    names = declared_symbols()
+    assert len(names) >= 15
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_layer_binds_every_symbol(thesis, built_library):
+    assert set(declared_symbols()) <= set(thesis.EXPORTED)
+
+
+def _create(thesis, path):
+    L = thesis.load_library()
+    ctx = ctypes.c_void_p()
+    st = L.th_ctx_create_from_deck(path.encode(), 1, ctypes.byref(ctx))
+    return st, L.th_last_error(None).decode(), ctx
+
+
+def test_missing_deck_is_an_error(thesis, built_library, tmp_path):
+    st, msg, ctx = _create(thesis, str(tmp_path / "nope" / "ParamInput.txt"))
+    assert st == 1 and "cannot open" in msg and not ctx.value
+
+
+@pytest.mark.parametrize("edit,needle", [
+    (lambda d: setattr(d, "mode", "Bogus"), "exactly one"),
+    (lambda d: setattr(d, "tracking", "Geometry"), "tracking"),
+    (lambda d: d.settings_extra.update({"Path": {"Compression": "1"}}), "compression"),
+    (lambda d: setattr(d.beams[0], "width_x", 0.0), "widths"),
+])
+def test_bad_decks_are_rejected_before_any_launch(thesis, built_library, decks, tmp_path, edit, needle):
+    d = decks.small_surface("Surface")
+    edit(d)
+    path = d.write(str(tmp_path / "deck"))
+    if d.mode == "Bogus":
+        with open(os.path.join(os.path.dirname(path), "Mode.txt"), "w") as f:
+            f.write("Bogus\n{\n}\n")
+    st, msg, ctx = _create(thesis, path)
+    assert st != 0 and needle.lower() in msg.lower() and not ctx.value

@@ -1,0 +1,57 @@
+"""The CPU oracle against vectors produced by the unmodified reference (tests/golden)."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "golden"))
+import make_golden  # noqa: E402
+
+GOLDEN = os.path.join(HERE, "golden")
+
+
+def _load(name):
+    return dict(np.load(os.path.join(GOLDEN, name)))
+
+
+@pytest.mark.parametrize("deck", sorted(make_golden.NODE_TIMES))
+def test_oracle_nodes_match_reference(deck, oracle, tmp_path):
+    g = _load(f"nodes_{deck}.npz")
+    path = make_golden.node_deck(deck).write(str(tmp_path / deck))
+    o = oracle(path)
+    for i, t in enumerate(make_golden.NODE_TIMES[deck]):
+        for sol in (False, True):
+            ref = g[f"{'sol_' if sol else ''}nodes{i}"]
+            got = o.nodes(float(g[f"t{i}"]), sol)
+            assert got["xb"].size == ref.shape[1], (deck, t, sol)
+            for c, f in enumerate(("xb", "yb", "zb", "phix", "phiy", "phiz", "dtau", "expmod")):
+                np.testing.assert_allclose(got[f], ref[c], rtol=1e-13, atol=0, err_msg=f"{deck} t={t} {f}")
+
+
+def test_oracle_temperature_matches_reference(oracle, tmp_path, decks):
+    g = _load("temp_snapshot_raster.npz")
+    o = oracle(decks.snapshot_raster().write(str(tmp_path / "raster")))
+    for i in range(3):
+        assert o.snapshot_time(i) == float(g[f"t{i}"])
+        T = o.calc_T(o.snapshot_time(i), g["pts"])
+        np.testing.assert_allclose(T, g[f"T{i}"], rtol=1e-13, atol=1e-10)
+
+
+@pytest.mark.parametrize("tag", sorted(make_golden.RUNS))
+def test_oracle_solidification_matches_reference(tag, oracle, tmp_path):
+    g = _load(f"run_{tag}.npz")
+    deck = make_golden.run_deck(tag)
+    o = oracle(deck.write(str(tmp_path / tag)))
+    o.solidify(threads=4)
+    flag = o.field("output_flag") > 0
+    assert np.array_equal(np.packbits(flag), g["mask"]), "molten-point set differs"
+    sub = g["sample"]
+    for key in g:
+        if not key.endswith("_sample"):
+            continue
+        f = key[:-len("_sample")]
+        v = o.field(f)
+        np.testing.assert_allclose(v[sub], g[key], rtol=1e-12, atol=1e-12, err_msg=f)
+        np.testing.assert_allclose(np.sum(v[flag]), g[f + "_sum"], rtol=1e-11, err_msg=f)
