@@ -39,7 +39,8 @@ NODE_FIELDS = ("xb", "yb", "zb", "phix", "phiy", "phiz", "dtau", "expmod")
 FIELDS = ("T", "tSol", "G", "V", "Gx", "Gy", "Gz", "dTdt", "eqFrac", "numMelt", "depth", "output_flag")
 EXPORTED = ("th_ctx_create_from_deck", "th_ctx_destroy", "th_last_error", "th_get_info", "th_snapshot_time",
             "th_nodes", "th_calc_T", "th_calc_T_device", "th_snapshot", "th_solidify", "th_field",
-            "th_simulate", "th_pairs", "th_set_tile_shape", "th_last_kernel_ms", "th_sync")
+            "th_simulate", "th_pairs", "th_set_tile_shape", "th_last_kernel_ms", "th_sync",
+            "th_calc_T_noalloc")
 
 
 class ThesisError(RuntimeError):
@@ -84,6 +85,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.th_calc_T.argtypes = [vp, c_d, vp, c_i64, vp]
     L.th_calc_T_device.argtypes = [vp, c_d, vp, c_i64, vp, vp]
     L.th_sync.argtypes = [vp, vp]
+    L.th_calc_T_noalloc.argtypes = [vp, c_d, vp, c_i64, vp, vp]
     L.th_snapshot.argtypes = [vp, c_int, vp]
     L.th_solidify.argtypes = [vp, c_i64, ctypes.POINTER(c_i64)]
     L.th_field.argtypes = [vp, ctypes.c_char_p, vp]
@@ -175,6 +177,12 @@ class Simulation:
         """Device-pointer form (integers are raw CUDA addresses, e.g. tensor.data_ptr())."""
         self._check(self._lib.th_calc_T_device(self._ctx, float(t), ctypes.c_void_p(d_pts or None), int(n),
                                                ctypes.c_void_p(d_T), ctypes.c_void_p(stream or None)))
+
+    def calc_T_noalloc(self, t: float, d_pts: int, n: int, d_T: int, stream: int = 0):
+        """Like calc_T_device, but the node list uses the library's static device array
+        instead of memory the context allocates; never allocates device memory."""
+        self._check(self._lib.th_calc_T_noalloc(self._ctx, float(t), ctypes.c_void_p(d_pts or None), int(n),
+                                                ctypes.c_void_p(d_T), ctypes.c_void_p(stream or None)))
 
     def sync(self, stream: int = 0):
         self._check(self._lib.th_sync(self._ctx, ctypes.c_void_p(stream or None)))

@@ -97,6 +97,21 @@ th_status th_calc_T(th_ctx* ctx, double t, const int64_t* pts, int64_t n, double
 th_status th_calc_T_device(th_ctx* ctx, double t, const int64_t* d_pts, int64_t n, double* d_T,
                            void* stream);
 
+/* Allocation-free form of th_calc_T_device, for callers that cannot allocate device
+ * memory or let the library allocate it (their device memory is owned by their own pool
+ * or a budget fixed at start-up, or the call sits in a time loop where cudaMalloc /
+ * cudaFree would synchronise the device and could fail).  No counterpart in the reference.
+ * It calls no cudaMalloc, cudaFree or other allocating routine: the node list lives in a
+ * static device array of the library holding at most 16384 nodes (about 1.7 MB, kept by
+ * every GPU that loads the library until the process exits); a longer list returns
+ * TH_ERR_CAPACITY and leaves d_T invalid.  The first call on a device looks the array's
+ * address up once for that device.  It synchronises `stream` before returning (to report
+ * that error).  Every call, from every context on the device, shares the one array, so
+ * calls that overlap on the GPU (other streams or host threads) race and must be
+ * serialised by the caller. */
+th_status th_calc_T_noalloc(th_ctx* ctx, double t, const int64_t* d_pts, int64_t n, double* d_T,
+                            void* stream);
+
 /* Waits for `stream` (NULL: only the context's own stream) and reports any device-side
  * error latched since the last check. */
 th_status th_sync(th_ctx* ctx, void* stream);
