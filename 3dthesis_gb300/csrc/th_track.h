@@ -1,0 +1,95 @@
+// Solidification-mode device state and kernels (NoTracking, Volume, Surface).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "th_kernels.h"
+#include "th_problem.h"
+
+// One liquid -> solid transition seen by the tracking loop; the solidification time and
+// the gradients are computed later, in bulk, from these four numbers
+// (the inputs of Grid::Solidify, src/Grid.cpp:316-338).
+struct SolRec {
+  int32_t p;       // point id
+  int32_t step;    // timestep index
+  double t;        // time of the step
+  double T;        // temperature at t
+  double Tl;       // temperature at the previous step (T_last)
+};
+
+// Per-step counters; one struct in device memory.
+struct TrackCounters {
+  int liq_n[2];     // liquid list length (ping-pong by step parity)
+  int reset_n[2];   // reset list length
+  int col_n;        // column solidification work items
+  int seed_n;       // beam-trace seeds
+  int rec_n;        // solidification records queued
+  int step;         // next step to run
+  int done;         // finish test passed
+  int stop;         // the loop stopped early (record queue high-water mark)
+  int rounds;       // frontier rounds of the last step
+  int max_rounds;   // largest number of rounds in one step
+  int front_n[4096];// frontier length per round of the current step
+};
+
+constexpr int kMaxFrontRounds = 4095;
+
+// Device pointers of the solidification state.
+struct TrackState {
+  double* T;
+  double* T_last;
+  unsigned* flag;          // T_calc_flag
+  unsigned char* outflag;  // output_flag
+  int* last_liq;           // last step at which the point was liquid (-1: never)
+  int* num_melt;
+  int* sol_step;           // step of the record whose results are stored (-1: none)
+  double* tSol; double* G; double* V; double* Gx; double* Gy; double* Gz; double* dTdt; double* eqFrac;
+  double* depth;           // per point (Surface with depth output), may be null
+  int* depths;             // per (i, j) column: deepest liquid layer
+  double* depth_max;       // per column
+  int* liq[2];
+  int* reset[2];
+  int* front[2];
+  int2* colwork;           // (point, recompute T_last?)
+  int* seeds;
+  int list_cap;
+  SolRec* rec;
+  int rec_cap;
+  TrackCounters* C;
+  unsigned* bar;           // grid barrier: [0] arrivals, [1] generation
+  int* err;
+  unsigned long long* pairs;
+};
+
+// A window of precomputed node lists: slot s holds the list of step (base - 1 + s).
+struct NodeWindow {
+  NodeBufView nb;          // slot-major: slot s starts at s * slot_cap
+  int slot_cap;
+  int nslots;
+  int* count;              // per slot
+  const double* t;         // per slot
+  int base;                // step of slot 1
+};
+
+// Error bits written by the solidification kernels (besides the node bits).
+enum { ERR_BARRIER = 16, ERR_RECORDS = 32, ERR_LISTS = 64, ERR_ROUNDS = 128 };
+
+void th_launch_nodes_window(const DevProblem& P, const NodeWindow& w, int first_slot, int nslots, bool is_sol,
+                            int* d_err, cudaStream_t s);
+
+// Runs steps [k_begin, k_end) of a Volume/Surface loop inside one cooperative launch.
+cudaError_t th_launch_track(const DevProblem& P, const TrackState& S, const NodeWindow& w, int k_begin, int k_end,
+                            int precision, int rec_high_water, cudaStream_t s);
+
+// One NoTracking step over the whole grid (src/Run.cpp:423-444).
+void th_launch_notrack_step(const DevProblem& P, const TrackState& S, const NodeWindow& w, int k, int precision,
+                            cudaStream_t s);
+
+// Solidification time, gradients and derived fields for the queued records.
+void th_launch_solidify(const DevProblem& P, const TrackState& S, int nrec, int precision, bool do_sol, cudaStream_t s);
+
+// Final per-point field with the reference's liquid markers applied.
+void th_launch_final_field(const DevProblem& P, const TrackState& S, int field, double* out, cudaStream_t s);
+
+int th_track_blocks(int precision);

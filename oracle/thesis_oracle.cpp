@@ -569,6 +569,8 @@ inline double int_abs(double x) {
   return (double)(i < 0 ? -i : i);
 }
 
+void solid_fields(Problem& P, long p, double tsol, double* out);
+
 void solidify(Problem& P, double t, long p) {                                 // src/Grid.cpp:316-338
   P.numMelt[p] += 1;
   if (!P.do_sol) return;
@@ -587,8 +589,18 @@ void solidify(Problem& P, double t, long p) {                                 //
     if (Tt > T0) { t1 = tsol; T1 = Tt; } else { t2 = tsol; T2 = Tt; }
   }
   P.tSol[p] = tsol;
+  double out[8];
+  solid_fields(P, p, tsol, out);
+  P.G[p] = out[0]; P.Gx[p] = out[1]; P.Gy[p] = out[2]; P.Gz[p] = out[3];
+  P.dTdt[p] = out[4]; P.V[p] = out[5]; P.eqFrac[p] = out[6];
+}
+
+// Nodes at tsol with the refined schedule, then the gradient / Laplacian / source sums
+// (src/Grid.cpp:406-453) and the derived fields (src/Grid.cpp:522-548):
+// out = {G, Gx/G, Gy/G, Gz/G, dTdt, V, eqFrac}.
+void solid_fields(Problem& P, long p, double tsol, double* out) {
+  Nodes N;
   make_nodes(P, tsol, true, N);
-  // gradient / Laplacian / source sums (src/Grid.cpp:406-453)
   const double xp = px_(P, p), yp = py_(P, p), zp = pz_(P, p);
   double gx = 0, gy = 0, gz = 0, lap = 0, dTt = 0;
   for (size_t n = 0; n < N.size(); ++n) {
@@ -607,8 +619,7 @@ void solidify(Problem& P, double t, long p) {                                 //
   const double dTdt = int_abs(P.a * lap + dTt);
   const double V = dTdt / G;
   const double eq = (1.0 - std::exp((-4 * kPi * P.cetN0 / 3) * std::pow(G * (P.cetn + 1) / (std::pow(P.ceta * V, 1 / P.cetn)), -3)));
-  P.G[p] = G; P.Gx[p] = gx / G; P.Gy[p] = gy / G; P.Gz[p] = gz / G;
-  P.dTdt[p] = dTdt; P.V[p] = V; P.eqFrac[p] = eq;
+  out[0] = G; out[1] = gx / G; out[2] = gy / G; out[3] = gz / G; out[4] = dTdt; out[5] = V; out[6] = eq;
 }
 
 // ------------------------------------------------------------------ melt tracking
@@ -945,5 +956,7 @@ int or_field(void* h, const char* name, double* out) {
 }
 
 int64_t or_pairs(void* h) { return ((Problem*)h)->pairs.load(); }
+
+void or_solid_fields(void* h, int64_t p, double tsol, double* out) { solid_fields(*(Problem*)h, (long)p, tsol, out); }
 
 }  // extern "C"

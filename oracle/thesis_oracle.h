@@ -49,6 +49,10 @@ int64_t or_solidify(void* h, int threads, int64_t max_steps);
  * "eqFrac", "numMelt", "depth", "output_flag".  Returns 0 on success. */
 int   or_field(void* h, const char* name, double* out);
 
+/* G, Gx/G, Gy/G, Gz/G, dT/dt, V, eqFrac of point p for a solidification time tsol
+ * (the second half of Grid::Solidify), into out[0..6]. */
+void  or_solid_fields(void* h, int64_t p, double tsol, double* out);
+
 /* Point x node pairs evaluated since load (temperature sums + gradient sums). */
 int64_t or_pairs(void* h);
 

@@ -31,6 +31,7 @@ def load():
         L.or_solidify.argtypes = [vp, ctypes.c_int, ctypes.c_int64]
         L.or_solidify.restype = ctypes.c_int64
         L.or_field.argtypes = [vp, ctypes.c_char_p, vp]
+        L.or_solid_fields.argtypes = [vp, ctypes.c_int64, ctypes.c_double, vp]
         L.or_pairs.argtypes = [vp]
         L.or_pairs.restype = ctypes.c_int64
         _lib = L
@@ -89,6 +90,11 @@ class Oracle:
         if rc:
             raise KeyError(name)
         return out
+
+    def solid_fields(self, p, tsol):
+        out = np.zeros(8)
+        _lib.or_solid_fields(self.h, int(p), float(tsol), out.ctypes.data_as(ctypes.c_void_p))
+        return dict(zip(("G", "Gx", "Gy", "Gz", "dTdt", "V", "eqFrac"), out[:7]))
 
     @property
     def pairs(self):
