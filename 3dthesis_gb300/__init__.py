@@ -40,7 +40,7 @@ FIELDS = ("T", "tSol", "G", "V", "Gx", "Gy", "Gz", "dTdt", "eqFrac", "numMelt", 
 EXPORTED = ("th_ctx_create_from_deck", "th_ctx_destroy", "th_last_error", "th_get_info", "th_snapshot_time",
             "th_nodes", "th_calc_T", "th_calc_T_device", "th_snapshot", "th_solidify", "th_field",
             "th_simulate", "th_pairs", "th_set_tile_shape", "th_last_kernel_ms", "th_sync",
-            "th_calc_T_noalloc")
+            "th_calc_T_noalloc", "th_run_stats", "th_run_reset")
 
 
 class ThesisError(RuntimeError):
@@ -86,6 +86,8 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.th_calc_T_device.argtypes = [vp, c_d, vp, c_i64, vp, vp]
     L.th_sync.argtypes = [vp, vp]
     L.th_calc_T_noalloc.argtypes = [vp, c_d, vp, c_i64, vp, vp]
+    L.th_run_stats.argtypes = [vp, vp, c_int]
+    L.th_run_reset.argtypes = [vp]
     L.th_snapshot.argtypes = [vp, c_int, vp]
     L.th_solidify.argtypes = [vp, c_i64, ctypes.POINTER(c_i64)]
     L.th_field.argtypes = [vp, ctypes.c_char_p, vp]
@@ -197,6 +199,18 @@ class Simulation:
         steps = ctypes.c_int64()
         self._check(self._lib.th_solidify(self._ctx, int(max_steps), ctypes.byref(steps)))
         return steps.value
+
+    def reset(self):
+        """Discards the solidification state; the next solidify() starts at t = 0."""
+        self._check(self._lib.th_run_reset(self._ctx))
+
+    def run_stats(self) -> Dict[str, float]:
+        """Device time (ms) and counters of the solidification loop so far."""
+        out = np.zeros(11)
+        self._check(self._lib.th_run_stats(self._ctx, _ptr(out), 11))
+        keys = ("ms_nodes", "ms_track", "ms_solidify", "windows", "records", "max_rounds", "steps", "slot_cap",
+                "ms_device", "pairs_solidify", "pairs_total")
+        return dict(zip(keys, out.tolist()))
 
     def field(self, name: str) -> np.ndarray:
         out = np.empty(self.pnum)

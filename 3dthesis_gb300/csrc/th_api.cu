@@ -130,8 +130,8 @@ th_status th_ctx_create_from_deck(const char* param_input, int32_t precision, th
   }
   if (th_cuda_check(ctx, cudaMalloc(&ctx->d_small, 16 * sizeof(int)), "cudaMalloc") != TH_OK) return fail(TH_ERR_CUDA);
   if (th_cuda_check(ctx, cudaMemset(ctx->d_small, 0, 16 * sizeof(int)), "cudaMemset") != TH_OK) return fail(TH_ERR_CUDA);
-  if (th_cuda_check(ctx, cudaMalloc(&ctx->d_pairs, sizeof(unsigned long long)), "cudaMalloc") != TH_OK) return fail(TH_ERR_CUDA);
-  if (th_cuda_check(ctx, cudaMemset(ctx->d_pairs, 0, sizeof(unsigned long long)), "cudaMemset") != TH_OK) return fail(TH_ERR_CUDA);
+  if (th_cuda_check(ctx, cudaMalloc(&ctx->d_pairs, 2 * sizeof(unsigned long long)), "cudaMalloc") != TH_OK) return fail(TH_ERR_CUDA);
+  if (th_cuda_check(ctx, cudaMemset(ctx->d_pairs, 0, 2 * sizeof(unsigned long long)), "cudaMemset") != TH_OK) return fail(TH_ERR_CUDA);
   // capacity: 64 nodes per segment per beam and a margin, times the image count; grown on demand
   size_t segs_total = segs.size();
   int cap = (int)std::min<size_t>((size_t)(64 * segs_total + 4096) * (size_t)ctx->dp.n_images, 1 << 24);

@@ -30,6 +30,7 @@ constexpr int kRecCap = 1 << 22;      // queued solidification records
 struct RunState {
   TrackState S{};
   std::vector<void*> allocs;
+  std::vector<std::pair<size_t, int>> alloc_fill;   // bytes and fill byte of each allocation
   void* win_mem = nullptr;
   NodeWindow W{};
   double* d_t = nullptr;
@@ -43,6 +44,11 @@ struct RunState {
   bool initialised = false;
   int max_rounds = 0;
   double* d_field = nullptr;
+  // device time per phase (ms) and counts, for th_run_stats
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  cudaEvent_t ev_run[2] = {nullptr, nullptr};
+  double ms_nodes = 0, ms_track = 0, ms_solid = 0, ms_device = 0;
+  long long windows = 0, records = 0;
 };
 
 void th_release_run_state(th_ctx* ctx) {
@@ -53,6 +59,10 @@ void th_release_run_state(th_ctx* ctx) {
   cudaFree(r->d_t);
   cudaFree(r->d_count);
   cudaFree(r->d_field);
+  if (r->ev[0]) cudaEventDestroy(r->ev[0]);
+  if (r->ev[1]) cudaEventDestroy(r->ev[1]);
+  if (r->ev_run[0]) cudaEventDestroy(r->ev_run[0]);
+  if (r->ev_run[1]) cudaEventDestroy(r->ev_run[1]);
   delete r;
   ctx->run = nullptr;
 }
@@ -65,6 +75,7 @@ th_status dalloc(th_ctx* ctx, RunState* r, T** p, size_t n, int fill_byte = 0) {
   th_status st = th_cuda_check(ctx, cudaMalloc(&v, std::max<size_t>(n, 1) * sizeof(T)), "cudaMalloc");
   if (st != TH_OK) return st;
   r->allocs.push_back(v);
+  r->alloc_fill.push_back({std::max<size_t>(n, 1) * sizeof(T), fill_byte});
   st = th_cuda_check(ctx, cudaMemsetAsync(v, fill_byte, std::max<size_t>(n, 1) * sizeof(T), ctx->stream), "cudaMemset");
   *p = (T*)v;
   return st;
@@ -126,6 +137,10 @@ th_status init_run(th_ctx* ctx) {
   r->t_prev = 0.0;
   r->t_next = 0.0;
   r->initialised = true;
+  cudaEventCreate(&r->ev[0]);
+  cudaEventCreate(&r->ev[1]);
+  cudaEventCreate(&r->ev_run[0]);
+  cudaEventCreate(&r->ev_run[1]);
   return th_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "init");
 }
 
@@ -176,7 +191,9 @@ th_status build_window(th_ctx* ctx, RunState* r, int n, std::vector<double>& ts)
     st = th_cuda_check(ctx, cudaMemsetAsync(ctx->d_small + 1, 0, sizeof(int), ctx->stream), "cudaMemsetAsync");
     if (st != TH_OK) return st;
     const int first = r->k == 0 ? 1 : 0;
+    cudaEventRecord(r->ev[0], ctx->stream);
     th_launch_nodes_window(ctx->dp, r->W, first, n + 1 - first, false, ctx->d_small + 1, ctx->stream);
+    cudaEventRecord(r->ev[1], ctx->stream);
     st = th_cuda_check(ctx, cudaGetLastError(), "node window");
     if (st != TH_OK) return st;
     int err = 0;
@@ -188,6 +205,10 @@ th_status build_window(th_ctx* ctx, RunState* r, int n, std::vector<double>& ts)
     if (st != TH_OK) return st;
     st = th_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "node window");
     if (st != TH_OK) return st;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, r->ev[0], r->ev[1]);
+    r->ms_nodes += ms;
+    r->windows++;
     if (err & 2) return th_fail(ctx, TH_ERR_TIMEOUT, "quadrature walk exceeded its step limit");
     if (!(err & 1)) return TH_OK;
     int mx = 0;
@@ -237,6 +258,7 @@ th_status advance(th_ctx* ctx, int64_t stop_at) {
     th_status st = build_window(ctx, r, n, ts);
     if (st != TH_OK) return st;
     TrackCounters h;
+    cudaEventRecord(r->ev[0], ctx->stream);
     if (track) {
       st = th_cuda_check(ctx, cudaMemsetAsync(r->S.bar, 0, 2 * sizeof(unsigned), ctx->stream), "cudaMemsetAsync");
       if (st != TH_OK) return st;
@@ -248,10 +270,17 @@ th_status advance(th_ctx* ctx, int64_t stop_at) {
       st = th_cuda_check(ctx, cudaGetLastError(), "notrack step");
       if (st != TH_OK) return st;
     }
+    cudaEventRecord(r->ev[1], ctx->stream);
     st = read_counters(ctx, r, &h);
     if (st != TH_OK) return st;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, r->ev[0], r->ev[1]);
+    r->ms_track += ms;
+    cudaEventRecord(r->ev[0], ctx->stream);
     st = drain_records(ctx, r, h.rec_n);
     if (st != TH_OK) return st;
+    cudaEventRecord(r->ev[1], ctx->stream);
+    r->records += h.rec_n;
     const int k_new = h.step;
     if (k_new <= r->k && !h.done) return th_fail(ctx, TH_ERR_INVALID, "solidification loop made no progress");
     // times of the steps actually run (slots are 1-based from r->k)
@@ -260,6 +289,9 @@ th_status advance(th_ctx* ctx, int64_t stop_at) {
     r->t_next = ran + 1 <= n ? ts[ran + 1] : ts[n] + hp.dt;
     r->k = k_new;
     r->done = h.done != 0;
+    cudaEventSynchronize(r->ev[1]);
+    cudaEventElapsedTime(&ms, r->ev[0], r->ev[1]);
+    r->ms_solid += ms;
     r->max_rounds = std::max(r->max_rounds, h.max_rounds);
   }
   return th_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "solidification");
@@ -343,9 +375,52 @@ th_status th_solidify(th_ctx* ctx, int64_t max_steps, int64_t* steps_out) {
     if (st != TH_OK) return st;
   }
   const int64_t stop = max_steps > 0 ? std::min<int64_t>(max_steps, INT_MAX - 1) : (int64_t)INT_MAX - 1;
+  RunState* r = ctx->run;
+  cudaEventRecord(r->ev_run[0], ctx->stream);
   st = advance(ctx, stop);
+  cudaEventRecord(r->ev_run[1], ctx->stream);
+  if (cudaEventSynchronize(r->ev_run[1]) == cudaSuccess) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, r->ev_run[0], r->ev_run[1]);
+    r->ms_device += ms;
+  }
   if (steps_out) *steps_out = ctx->run->k;
   return st;
+}
+
+th_status th_run_reset(th_ctx* ctx) {
+  if (!ctx) return th_fail(ctx, TH_ERR_INVALID, "null context");
+  th_status st = th_cuda_check(ctx, cudaSetDevice(ctx->device), "cudaSetDevice");
+  if (st != TH_OK) return st;
+  RunState* r = ctx->run;
+  if (!r) return TH_OK;
+  // the buffers stay allocated; every one is refilled with its initial contents
+  for (size_t i = 0; i < r->allocs.size(); ++i) {
+    st = th_cuda_check(ctx, cudaMemsetAsync(r->allocs[i], r->alloc_fill[i].second, r->alloc_fill[i].first, ctx->stream),
+                       "cudaMemsetAsync");
+    if (st != TH_OK) return st;
+  }
+  if (ctx->hp.tracking == TH_TRACK_NONE) k_fill_d<<<1024, 256, 0, ctx->stream>>>(r->S.T, (int64_t)ctx->hp.pnum, ctx->hp.T0);
+  r->k = 0; r->t_prev = 0.0; r->t_next = 0.0; r->done = false; r->max_rounds = 0;
+  r->ms_nodes = r->ms_track = r->ms_solid = r->ms_device = 0;
+  r->windows = r->records = 0;
+  st = th_cuda_check(ctx, cudaMemsetAsync(ctx->d_pairs, 0, 2 * sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
+  if (st != TH_OK) return st;
+  return th_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "reset");
+}
+
+th_status th_run_stats(th_ctx* ctx, double* out, int32_t n) {
+  if (!ctx || !out) return th_fail(ctx, TH_ERR_INVALID, "null argument");
+  const RunState* r = ctx->run;
+  unsigned long long pairs[2] = {0, 0};
+  th_status st = th_cuda_check(ctx, cudaMemcpy(pairs, ctx->d_pairs, sizeof(pairs), cudaMemcpyDeviceToHost), "cudaMemcpy");
+  if (st != TH_OK) return st;
+  const double v[11] = {r ? r->ms_nodes : 0, r ? r->ms_track : 0, r ? r->ms_solid : 0, r ? (double)r->windows : 0,
+                        r ? (double)r->records : 0, r ? (double)r->max_rounds : 0, r ? (double)r->k : 0,
+                        r ? (double)r->slot_cap : 0, r ? r->ms_device : 0, (double)pairs[1],
+                        (double)pairs[0]};
+  for (int i = 0; i < n && i < 11; ++i) out[i] = v[i];
+  return TH_OK;
 }
 
 th_status th_field(th_ctx* ctx, const char* name, double* out) {

@@ -635,6 +635,7 @@ __global__ void __launch_bounds__(128) k_solidify(DevProblem P, TrackState S, in
   if (S.V) S.V[p] = V;
   if (S.eqFrac) S.eqFrac[p] = eq;
   atomicAdd(S.pairs, pairs);
+  atomicAdd(S.pairs + 1, pairs);
   if (err) atomicOr(S.err, err);
 }
 

@@ -130,6 +130,16 @@ th_status th_solidify(th_ctx* ctx, int64_t max_steps, int64_t* steps_out);
  * "output_flag". */
 th_status th_field(th_ctx* ctx, const char* name, double* out);
 
+/* Discards the solidification state (the next th_solidify starts again at t = 0). */
+th_status th_run_reset(th_ctx* ctx);
+
+/* Device time and counters of the solidification loop so far, out[0..n): ms building
+ * node windows, ms in the tracking / NoTracking steps, ms solidifying records, windows,
+ * records, largest number of frontier rounds in one step, steps, node slots per step,
+ * device-elapsed ms of th_solidify calls (host gaps included), point x node pairs of the
+ * bulk solidification, all point x node pairs of the context. */
+th_status th_run_stats(th_ctx* ctx, double* out, int32_t n);
+
 /* Whole run as the reference CLI does it: the mode loop, then the CSV files under
  * <deck dir>/Data (same names, columns and number format). */
 th_status th_simulate(th_ctx* ctx);
