@@ -208,7 +208,7 @@ class Simulation:
         """Device time (ms) and counters of the solidification loop so far."""
         out = np.zeros(11)
         self._check(self._lib.th_run_stats(self._ctx, _ptr(out), 11))
-        keys = ("ms_nodes", "ms_track", "ms_solidify", "windows", "records", "max_rounds", "steps", "slot_cap",
+        keys = ("ms_nodes", "ms_track", "ms_solidify", "windows", "records", "max_items", "steps", "slot_cap",
                 "ms_device", "pairs_solidify", "pairs_total")
         return dict(zip(keys, out.tolist()))
 

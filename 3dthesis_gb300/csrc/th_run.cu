@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -97,7 +98,7 @@ th_status init_run(th_ctx* ctx) {
 #define ALLOC(ptr, cnt, fill) if ((st = dalloc(ctx, r, &(ptr), (cnt), (fill))) != TH_OK) return st
   ALLOC(S.T, n, 0);
   ALLOC(S.T_last, n, 0);
-  ALLOC(S.flag, n, 0);
+  ALLOC(S.stamp, n, 0);
   ALLOC(S.outflag, n, 0);
   ALLOC(S.last_liq, n, 0xff);   // -1
   ALLOC(S.num_melt, n, 0);
@@ -117,9 +118,11 @@ th_status init_run(th_ctx* ctx) {
   }
   if (hp.tracking != TH_TRACK_NONE) {
     S.list_cap = (int)n;
-    for (int i = 0; i < 2; ++i) { ALLOC(S.liq[i], n, 0); ALLOC(S.reset[i], n, 0); ALLOC(S.front[i], n, 0); }
-    ALLOC(S.colwork, n, 0);
-    ALLOC(S.seeds, n, 0);
+    for (int i = 0; i < 3; ++i) ALLOC(S.liq[i], n, 0);
+    // work items of one step: every claimed point, column layer and depth walk at most
+    // once, which in practice stays far below 2 * pnum
+    S.queue_cap = (int)std::min<size_t>(2 * n + 4096, (size_t)1 << 24);
+    ALLOC(S.queue, (size_t)S.queue_cap, 0);
   }
   S.rec_cap = kRecCap;
   ALLOC(S.rec, (size_t)kRecCap, 0);
@@ -221,7 +224,7 @@ th_status build_window(th_ctx* ctx, RunState* r, int n, std::vector<double>& ts)
 }
 
 th_status read_counters(th_ctx* ctx, RunState* r, TrackCounters* h) {
-  th_status st = th_cuda_check(ctx, cudaMemcpyAsync(h, r->S.C, offsetof(TrackCounters, front_n), cudaMemcpyDeviceToHost,
+  th_status st = th_cuda_check(ctx, cudaMemcpyAsync(h, r->S.C, sizeof(TrackCounters), cudaMemcpyDeviceToHost,
                                                     ctx->stream), "copy");
   if (st != TH_OK) return st;
   int err = 0;
@@ -229,10 +232,16 @@ th_status read_counters(th_ctx* ctx, RunState* r, TrackCounters* h) {
   if (st != TH_OK) return st;
   st = th_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "solidification step");
   if (st != TH_OK) return st;
-  if (err & 16) return th_fail(ctx, TH_ERR_TIMEOUT, "grid barrier wait exceeded its limit");
+  if (err & 16) {
+    char b[256];
+    std::snprintf(b, sizeof(b), "a %s wait exceeded its limit (step %d, ticket %d, initial items %d, tickets %d, "
+                  "published %d, published %d, completed %d, errors 0x%x)", h->diag[0] == 2 ? "grid barrier" : "work-queue",
+                  h->diag[1], h->diag[2], h->diag[3], h->diag[4], h->diag[5], h->diag[6], h->diag[7], err);
+    return th_fail(ctx, TH_ERR_TIMEOUT, b);
+  }
   if (err & 32) return th_fail(ctx, TH_ERR_CAPACITY, "solidification record queue overflowed");
   if (err & 64) return th_fail(ctx, TH_ERR_CAPACITY, "a tracking list overflowed");
-  if (err & 128) return th_fail(ctx, TH_ERR_TIMEOUT, "frontier expansion exceeded its round limit");
+  if (err & 128) return th_fail(ctx, TH_ERR_CAPACITY, "the per-step work queue overflowed");
   if (err & 2) return th_fail(ctx, TH_ERR_TIMEOUT, "quadrature walk exceeded its step limit");
   return TH_OK;
 }
@@ -292,7 +301,7 @@ th_status advance(th_ctx* ctx, int64_t stop_at) {
     cudaEventSynchronize(r->ev[1]);
     cudaEventElapsedTime(&ms, r->ev[0], r->ev[1]);
     r->ms_solid += ms;
-    r->max_rounds = std::max(r->max_rounds, h.max_rounds);
+    r->max_rounds = std::max(r->max_rounds, h.max_items);
   }
   return th_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "solidification");
 }

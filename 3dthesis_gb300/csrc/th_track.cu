@@ -91,11 +91,6 @@ __device__ __forceinline__ double warp_T(const DevProblem& P, const NodeBufView&
 __device__ __forceinline__ int ldcg_i(const int* p) { return __ldcg(p); }
 __device__ __forceinline__ double ldcg_d(const double* p) { return __ldcg(p); }
 
-__device__ __forceinline__ void push(int* list, int* cnt, int cap, int v, int* err) {
-  const int i = atomicAdd(cnt, 1);
-  if (i < cap) list[i] = v; else atomicOr(err, ERR_LISTS);
-}
-
 __device__ __forceinline__ void push_record(const TrackState& S, int p, int step, double t, double T, double Tl) {
   const int i = atomicAdd(&S.C->rec_n, 1);
   if (i < S.rec_cap) { SolRec r; r.p = p; r.step = step; r.t = t; r.T = T; r.Tl = Tl; S.rec[i] = r; }
@@ -107,7 +102,6 @@ __device__ __forceinline__ void push_record(const TrackState& S, int p, int step
 // eqFrac = -1) are applied when fields are read, from last_liq.
 __device__ __forceinline__ void set_T(const TrackState& S, const DevProblem& P, int p, double T, int step) {
   S.T[p] = T;
-  S.flag[p] = 1u;
   if (T >= P.TL) { S.outflag[p] = 1; S.last_liq[p] = step; }
 }
 
@@ -128,7 +122,10 @@ __device__ __forceinline__ bool grid_sync(const TrackState& S) {
     } else {
       long long spins = 0;
       while (*gen == g) {
-        if (++spins > kSpinLimit) { atomicOr(S.err, ERR_BARRIER); break; }
+        if (++spins > kSpinLimit) {
+          if (atomicOr(S.err, ERR_BARRIER) == 0) { S.C->diag[0] = 2; S.C->diag[2] = (int)blockIdx.x; S.C->diag[4] = (int)*S.bar; }
+          break;
+        }
         __nanosleep(32);
       }
     }
@@ -147,17 +144,102 @@ __device__ __forceinline__ int first_ge(const DevSeg* path, int ns, double t) {
   return lo;
 }
 
-__device__ __forceinline__ void claim_seed(const TrackState& S, int64_t q) {
-  if (atomicCAS(&S.flag[q], 0u, 1u) == 0u) push(S.seeds, &S.C->seed_n, S.list_cap, (int)q, S.err);
-}
-
 __device__ __forceinline__ int64_t pid(const DevProblem& P, int i, int j, int k) {
   return (int64_t)i * ((int64_t)P.ny * P.nz) + (int64_t)j * P.nz + k;
 }
 
+// Claim for this step (the reference's T_calc_flag test-and-set, src/Melt.cpp:213-218):
+// a point counts as claimed in step k when its stamp is >= k + 1.
+__device__ __forceinline__ bool claim(const TrackState& S, int q, unsigned stamp) {
+  if (__ldcg(S.stamp + q) >= stamp) return false;
+  return atomicMax(S.stamp + q, stamp) < stamp;
+}
+
+// ------------------------------------------------------------------ step work queue
+enum { IT_RETEST = 0, IT_SEEDS = 1, IT_VISIT = 2, IT_COLUMN = 3, IT_DEPTH = 4 };
+
+struct StepCtx {
+  int k;                   // step
+  unsigned stamp;          // k + 1
+  double t;
+  NodeBufView nb, nbl;
+  int nn, nnl;
+  int nL, n_init;
+  const int* L;
+  int* Lo;
+  int* lo_n;
+  QueueCounters* qc;
+};
+
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ int ld_acquire_s32(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_s32(int* p, int v) {
+  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Publishes one child item per lane that has one (warp-uniform call).  The children are
+// counted as published in the same atomic that hands out their slots, before any of them
+// can be taken, so "completed == initial + published" can only hold once the step has no
+// work left; each slot's tag is released after its payload.
+__device__ __forceinline__ void emit(const TrackState& S, const StepCtx& X, bool has, int type, int p, int aux,
+                                     int& nchild) {
+  const int lane = threadIdx.x & 31;
+  const unsigned m = __ballot_sync(0xffffffffu, has);
+  if (!m) return;
+  unsigned base = 0;
+  if (lane == 0) base = (unsigned)(atomicAdd(&X.qc->state, (unsigned long long)__popc(m) << 32) >> 32);
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (has) {
+    const unsigned j = base + __popc(m & ((1u << lane) - 1u));
+    if (j < (unsigned)S.queue_cap) {
+      int4* slot = S.queue + j;
+      slot->y = type; slot->z = p; slot->w = aux;
+      st_release_s32(&slot->x, (int)X.stamp);
+    } else {
+      atomicOr(S.err, ERR_QUEUE);
+    }
+  }
+  nchild += __popc(m);
+}
+
+// Claims the unvisited neighbours of p (3x3 in the same layer for Surface, 3x3x{k-1, k}
+// for Volume; src/Melt.cpp:202-257) and queues them for evaluation.
+template <bool SURF>
+__device__ __forceinline__ void expand(const DevProblem& P, const TrackState& S, const StepCtx& X, int p, int& nchild) {
+  const int lane = threadIdx.x & 31;
+  const int nyz = P.ny * P.nz;
+  const int pi = p / nyz, pj = (p / P.nz) % P.ny, pk = p % P.nz;
+  bool got = false;
+  int q = 0;
+  if (lane < (SURF ? 9 : 18)) {
+    const int di = (lane % 9) / 3 - 1, dj = lane % 3 - 1, dk = SURF ? 0 : (lane / 9) - 1;
+    const int ni = pi + di, nj = pj + dj, nk = pk + dk;
+    if (!(ni < 0 || ni > P.nx - 1 || nj < 0 || nj > P.ny - 1 || nk < 0)) {
+      q = (int)pid(P, ni, nj, nk);
+      got = claim(S, q, X.stamp);
+    }
+  }
+  emit(S, X, got, IT_VISIT, q, 0, nchild);
+}
+
+__device__ __forceinline__ void push_liquid(const TrackState& S, const StepCtx& X, int p) {
+  const int i = atomicAdd(X.lo_n, 1);
+  if (i < S.list_cap) X.Lo[i] = p; else atomicOr(S.err, ERR_LISTS);
+  atomicMax(S.stamp + p, X.stamp + 1u);   // already claimed for the next step's re-test
+}
+
 // Perimeter seeds of one anchor point (src/Melt.cpp:36-55, 69-77): when the anchor lies
 // outside the grid, surface points along that edge within CheckRadius * ax are tested.
-__device__ void perimeter(const DevProblem& P, const TrackState& S, double x, double y, double r2) {
+__device__ void perimeter(const DevProblem& P, const TrackState& S, const StepCtx& X, double x, double y, double r2,
+                          int& nchild) {
   const int lane = threadIdx.x & 31;
   const int xg = (int)floor(rn_div(rn_sub(x, P.xmin), P.xres));
   const int yg = (int)floor(rn_div(rn_sub(y, P.ymin), P.yres));
@@ -169,29 +251,45 @@ __device__ void perimeter(const DevProblem& P, const TrackState& S, double x, do
     else if (edge == 2) { if (!(yg < 0)) continue; fixed = 0; xfixed = false; }
     else { if (!(yg > P.ny - 1)) continue; fixed = P.ny - 1; xfixed = false; }
     const int hi = xfixed ? P.ny : P.nx;
-    for (int v = lane; v < hi; v += 32) {
-      const int i = xfixed ? fixed : v, j = xfixed ? v : fixed;
-      const double dx = rn_sub(rn_add(P.xmin, rn_mul((double)i, P.xres)), x);
-      const double dy = rn_sub(rn_add(P.ymin, rn_mul((double)j, P.yres)), y);
-      if (rn_add(rn_mul(dx, dx), rn_mul(dy, dy)) < r2) claim_seed(S, pid(P, i, j, P.nz - 1));
+    for (int v0 = 0; v0 < hi; v0 += 32) {
+      const int v = v0 + lane;
+      bool got = false;
+      int q = 0;
+      if (v < hi) {
+        const int i = xfixed ? fixed : v, j = xfixed ? v : fixed;
+        const double dx = rn_sub(rn_add(P.xmin, rn_mul((double)i, P.xres)), x);
+        const double dy = rn_sub(rn_add(P.ymin, rn_mul((double)j, P.yres)), y);
+        if (rn_add(rn_mul(dx, dx), rn_mul(dy, dy)) < r2) {
+          q = (int)pid(P, i, j, P.nz - 1);
+          got = claim(S, q, X.stamp);
+        }
+      }
+      emit(S, X, got, IT_VISIT, q, 0, nchild);
     }
   }
 }
 
 // The 2 x 2 surface cells at and after an anchor inside the grid (src/Melt.cpp:122-146).
-__device__ void cell(const DevProblem& P, const TrackState& S, double x, double y) {
+__device__ void cell(const DevProblem& P, const TrackState& S, const StepCtx& X, double x, double y, int& nchild) {
   const int lane = threadIdx.x & 31;
   const int xg = (int)floor(rn_div(rn_sub(x, P.xmin), P.xres));
   const int yg = (int)floor(rn_div(rn_sub(y, P.ymin), P.yres));
   if (xg < 0 || xg > P.nx - 1 || yg < 0 || yg > P.ny - 1) return;
+  bool got = false;
+  int q = 0;
   if (lane < 4) {
     const int i = xg + (lane >> 1), j = yg + (lane & 1);
-    if (!(i < 0 || i > P.nx - 1 || j < 0 || j > P.ny - 1)) claim_seed(S, pid(P, i, j, P.nz - 1));
+    if (!(i < 0 || i > P.nx - 1 || j < 0 || j > P.ny - 1)) {
+      q = (int)pid(P, i, j, P.nz - 1);
+      got = claim(S, q, X.stamp);
+    }
   }
+  emit(S, X, got, IT_VISIT, q, 0, nchild);
 }
 
-// Melt::beam_trace for (t_start, t_end], run by one warp (src/Melt.cpp:20-183).
-__device__ void beam_trace(const DevProblem& P, const TrackState& S, double t_start, double t_end) {
+// Melt::beam_trace for (t - dt, t] (src/Melt.cpp:20-183), claims queued as visits.
+__device__ void beam_trace(const DevProblem& P, const TrackState& S, const StepCtx& X, int& nchild) {
+  const double t_end = X.t, t_start = rn_sub(X.t, P.dt);
   for (int b = 0; b < P.nbeams; ++b) {
     const DevBeam& B = P.beam[b];
     const DevSeg* path = P.segs + B.seg_off;
@@ -200,253 +298,217 @@ __device__ void beam_trace(const DevProblem& P, const TrackState& S, double t_st
     const double ts = (rn_sub(t_end, tsub) < 0.0) ? 0.0 : rn_sub(t_end, tsub);
     const double r2 = rn_mul(rn_mul(rc2, B.ax), B.ax);
     const int s0 = first_ge(path, B.nseg, ts), s1 = first_ge(path, B.nseg, t_end);
-    for (int s = max(s0 - 1, 0); s <= s1; ++s) perimeter(P, S, path[s].x, path[s].y, r2);
+    for (int s = max(s0 - 1, 0); s <= s1; ++s) perimeter(P, S, X, path[s].x, path[s].y, r2, nchild);
     if (path[s1].mode == 0 && t_end < B.tlast) {
       const BeamLoc L = beam_loc(P, path, t_end, s1);
-      perimeter(P, S, L.x, L.y, r2);
+      perimeter(P, S, X, L.x, L.y, r2, nchild);
     }
   }
   for (int b = 0; b < P.nbeams; ++b) {
     const DevBeam& B = P.beam[b];
     const DevSeg* path = P.segs + B.seg_off;
     const int s0 = first_ge(path, B.nseg, t_start), s1 = first_ge(path, B.nseg, t_end);
-    for (int s = max(s0 - 1, 0); s <= s1; ++s) cell(P, S, path[s].x, path[s].y);
+    for (int s = max(s0 - 1, 0); s <= s1; ++s) cell(P, S, X, path[s].x, path[s].y, nchild);
     if (path[s1].mode == 0 && t_end < B.tlast) {
       const BeamLoc L = beam_loc(P, path, t_end, s1);
-      cell(P, S, L.x, L.y);
+      cell(P, S, X, L.x, L.y, nchild);
     }
   }
-  __syncwarp();
+}
+
+// Depth walk under a liquid surface point and the running depth maximum
+// (src/Melt.cpp:271-357): walk down while liquid, else walk up solidifying.
+template <int PREC>
+__device__ void depth_walk(const DevProblem& P, const TrackState& S, const StepCtx& X, int p,
+                           unsigned long long& pairs) {
+  const int lane = threadIdx.x & 31;
+  const int col = p / P.nz;
+  const int D = ldcg_i(S.depths + col);
+  int d = D;
+  bool none_deeper = true;
+  while (true) {
+    ++d;
+    if (d == P.nz) break;
+    const int q = col * P.nz + (P.nz - 1 - d);
+    const double T = warp_T<PREC>(P, X.nb, X.nn, q);
+    pairs += X.nn;
+    if (lane == 0) set_T(S, P, q, T, X.k);
+    if (!(T >= P.TL)) break;
+    none_deeper = false;
+  }
+  while (true) {
+    --d;
+    if (d == 0 || !none_deeper) break;
+    const int q = col * P.nz + (P.nz - 1 - d);
+    const double Told = ldcg_d(S.T + q);
+    const double T = warp_T<PREC>(P, X.nb, X.nn, q);
+    pairs += X.nn;
+    if (lane == 0) set_T(S, P, q, T, X.k);
+    if (!(T >= P.TL)) {
+      double Tl = Told;                                   // T of the previous step
+      if (d != D) { Tl = warp_T<PREC>(P, X.nbl, X.nnl, q); pairs += X.nnl; }
+      if (lane == 0) push_record(S, q, X.k, X.t, T, Tl);
+    } else {
+      break;
+    }
+  }
+  if (d == P.nz) --d;
+  if (lane == 0) {
+    S.depths[col] = d;
+    if (S.depth) {
+      double dep;
+      if (d == P.nz - 1) dep = d;
+      else {
+        const double Tl = ldcg_d(S.T + col * P.nz + (P.nz - 1 - d));
+        const double Ts = ldcg_d(S.T + col * P.nz + (P.nz - 1 - (d + 1)));
+        dep = rn_add((double)d, rn_div(rn_sub(P.TL, Tl), rn_sub(Ts, Tl)));
+      }
+      if (dep > S.depth_max[col]) {
+        S.depth_max[col] = dep;
+        for (int dd = d; dd >= 0; --dd) S.depth[col * P.nz + (P.nz - 1 - dd)] = dep;
+      }
+    }
+  }
+}
+
+// One work item; returns the number of child items it published (already counted).
+template <int PREC, bool SURF>
+__device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx& X, int type, int p, int aux,
+                        unsigned long long& pairs) {
+  const int lane = threadIdx.x & 31;
+  int nchild = 0;
+  if (type == IT_SEEDS) {
+    beam_trace(P, S, X, nchild);
+    return nchild;
+  }
+  if (type == IT_DEPTH) {
+    depth_walk<PREC>(P, S, X, p, pairs);
+    return 0;
+  }
+  const double Told = ldcg_d(S.T + p);
+  const double T = warp_T<PREC>(P, X.nb, X.nn, p);
+  pairs += X.nn;
+  if (lane == 0) set_T(S, P, p, T, X.k);
+  const bool liquid = T >= P.TL;
+  if (type == IT_COLUMN) {                 // a layer under a surface point that solidified
+    double Tl = Told;
+    if (aux) { Tl = warp_T<PREC>(P, X.nbl, X.nnl, p); pairs += X.nnl; }
+    if (lane == 0) push_record(S, p, X.k, X.t, T, Tl);
+    return 0;
+  }
+  if (type == IT_RETEST && !liquid) {      // cooled below T_L since the last step
+    if (lane == 0) push_record(S, p, X.k, X.t, T, Told);
+    if (SURF) {
+      const int col = p / P.nz;
+      const int D = ldcg_i(S.depths + col);
+      for (int d0 = 1; d0 <= D; d0 += 32) {
+        const int d = d0 + lane;
+        emit(S, X, d <= D, IT_COLUMN, col * P.nz + (P.nz - 1 - d), d != D, nchild);
+      }
+      if (lane == 0) S.depths[col] = 0;
+    }
+  }
+  if (liquid && lane == 0) push_liquid(S, X, p);
+  if (SURF) emit(S, X, liquid && lane == 0, IT_DEPTH, p, 0, nchild);
+  // Surface expands every re-tested point, Volume only the liquid ones (src/Run.cpp:655, 531)
+  if (liquid || (SURF && type == IT_RETEST)) expand<SURF>(P, S, X, p, nchild);
+  return nchild;
 }
 
 // ------------------------------------------------------------------ the tracking loop
+// One launch runs steps [k_begin, k_end) of a Volume or Surface loop (src/Run.cpp:469-709).
+// Each step is a single phase: the previous step's liquid points are re-tested, the beam
+// trace seeds the new ones, and every claimed point, column and depth walk becomes a work
+// item that any warp may take; a packed (published << 32 | completed) counter tells the
+// warps when the step has no work left, and one grid barrier ends the step.
 template <int PREC, bool SURF>
 __global__ void __launch_bounds__(256) k_track(DevProblem P, TrackState S, NodeWindow W, int k_begin, int k_end,
                                                int high_water) {
   const int lane = threadIdx.x & 31;
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
-  const int warp = tid >> 5, nwarps = nthreads >> 5;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   TrackCounters* C = S.C;
   unsigned long long pairs = 0;
-  const int nyz = P.ny * P.nz;
   for (int k = k_begin; k < k_end; ++k) {
+    StepCtx X;
     const int slot = k - W.base + 1;
-    const NodeBufView nb = slot_view(W, slot), nbl = slot_view(W, slot - 1);
-    const int nn = W.count[slot], nnl = (k == 0) ? 0 : W.count[slot - 1];
-    const double t = W.t[slot];
-    const int cur = k & 1, nxt = cur ^ 1;
-    const int nL = ldcg_i(&C->liq_n[cur]), nR = ldcg_i(&C->reset_n[cur]);
-    const int* L = S.liq[cur];
-    const int* R = S.reset[cur];
-    int* Lo = S.liq[nxt];
-    int* Ro = S.reset[nxt];
-    int* liq_out = &C->liq_n[nxt];
-    int* reset_out = &C->reset_n[nxt];
-
-    // A. reset the points evaluated last step; the new reset list starts as last step's
-    //    liquid list (src/Run.cpp:603-616)
-    for (int i = tid; i < nR; i += nthreads) {
-      const int p = __ldcg(R + i);
-      S.T_last[p] = ldcg_d(S.T + p);
-      S.flag[p] = 0u;
+    X.k = k;
+    X.stamp = (unsigned)k + 1u;
+    X.nb = slot_view(W, slot);
+    X.nbl = slot_view(W, slot - 1);
+    X.nn = W.count[slot];
+    X.nnl = (k == 0) ? 0 : W.count[slot - 1];
+    X.t = W.t[slot];
+    const int b0 = k % 3, b1 = (k + 1) % 3, b2 = (k + 2) % 3;
+    X.nL = ldcg_i(&C->liq_n[b0]);
+    X.L = S.liq[b0];
+    X.Lo = S.liq[b1];
+    X.lo_n = &C->liq_n[b1];
+    X.qc = &C->q[b0];
+    const bool seeds = k > 0 && X.t < P.end_time + P.dt;
+    X.n_init = X.nL + (seeds ? 1 : 0);
+    if (tid == 0) {                       // buffers of the step after next
+      C->liq_n[b2] = 0;
+      C->q[b1].head = 0; C->q[b1].state = 0ull;
     }
-    for (int i = tid; i < nL; i += nthreads) Ro[i] = __ldcg(L + i);
-    if (tid == 0) {
-      const int prev_rounds = C->rounds;
-      for (int r = 0; r <= prev_rounds + 1 && r <= kMaxFrontRounds; ++r) C->front_n[r] = 0;
-      *liq_out = 0;
-      *reset_out = nL;
-      C->col_n = 0;
-      C->seed_n = 0;
-    }
-    if (!grid_sync(S)) return;
-
-    // B. re-test last step's liquid points; queue the ones that cooled below T_L
-    for (int i = warp; i < nL; i += nwarps) {
-      const int p = __ldcg(L + i);
-      const double T = warp_T<PREC>(P, nb, nn, p);
-      pairs += nn;
-      if (lane == 0) set_T(S, P, p, T, k);
-      if (!(T >= P.TL)) {
-        if (lane == 0) push_record(S, p, k, t, T, ldcg_d(S.T_last + p));
-        if (SURF) {                                  // the column below solidifies too
-          const int col = p / P.nz;
-          const int D = ldcg_i(S.depths + col);
-          for (int d = D - lane; d > 0; d -= 32) {
-            const int q = col * P.nz + (P.nz - 1 - d);
-            const int w = atomicAdd(&C->col_n, 1);
-            if (w < S.list_cap) S.colwork[w] = make_int2(q, d != D); else atomicOr(S.err, ERR_LISTS);
-          }
-          if (lane == 0) S.depths[col] = 0;
-        }
-      } else if (lane == 0) {
-        push(Lo, liq_out, S.list_cap, p, S.err);
-      }
-    }
-    if (!grid_sync(S)) return;
-
-    // C. column solidification, beam-trace seeds, first frontier
-    {
-      const int ncol = ldcg_i(&C->col_n);
-      for (int i = warp; i < ncol; i += nwarps) {
-        const int2 it = __ldcg(S.colwork + i);
-        const int q = it.x;
-        const double T = warp_T<PREC>(P, nb, nn, q);
-        pairs += nn;
-        double Tl;
-        if (it.y) { Tl = warp_T<PREC>(P, nbl, nnl, q); pairs += nnl; }
-        else Tl = ldcg_d(S.T_last + q);
-        if (lane == 0) {
-          set_T(S, P, q, T, k);
-          if (it.y) S.T_last[q] = Tl;
-          push_record(S, q, k, t, T, Tl);
-          push(Ro, reset_out, S.list_cap, q, S.err);
-        }
-      }
-      if (SURF) {
-        for (int i = tid; i < nL; i += nthreads) S.front[0][i] = __ldcg(L + i);
-        if (tid == 0) C->front_n[0] = nL;
-      } else {
-        const int nLo = ldcg_i(liq_out);
-        for (int i = tid; i < nLo; i += nthreads) S.front[0][i] = __ldcg(Lo + i);
-        if (tid == 0) C->front_n[0] = nLo;
-      }
-      if (warp == nwarps - 1 && k > 0 && t < P.end_time + P.dt) beam_trace(P, S, rn_sub(t, P.dt), t);
-    }
-    if (!grid_sync(S)) return;
-
-    // D. evaluate the seeds (src/Run.cpp:662-669)
-    {
-      const int ns = ldcg_i(&C->seed_n);
-      for (int i = warp; i < ns; i += nwarps) {
-        const int p = __ldcg(S.seeds + i);
-        const double T = warp_T<PREC>(P, nb, nn, p);
-        pairs += nn;
-        if (lane == 0) {
-          set_T(S, P, p, T, k);
-          push(Ro, reset_out, S.list_cap, p, S.err);
-          if (T >= P.TL) {
-            push(S.front[0], &C->front_n[0], S.list_cap, p, S.err);
-            push(Lo, liq_out, S.list_cap, p, S.err);
-          }
-        }
-      }
-    }
-    if (!grid_sync(S)) return;
-
-    // E. frontier rounds: claim unvisited neighbours, evaluate, keep the liquid ones
-    //    (src/Melt.cpp:185-269; 3x3 at the same layer for Surface, 3x3x{k-1,k} for Volume)
-    int r = 0;
+    // the work loop
+    long long idle = 0;
     while (true) {
-      const int n_in = ldcg_i(&C->front_n[r]);
-      if (n_in == 0) break;
-      if (r >= kMaxFrontRounds) { if (tid == 0) atomicOr(S.err, ERR_ROUNDS); break; }
-      const int* Fin = S.front[r & 1];
-      int* Fout = S.front[(r + 1) & 1];
-      int* fout_n = &C->front_n[r + 1];
-      for (int i = warp; i < n_in; i += nwarps) {
-        const int p = __ldcg(Fin + i);
-        const int pi = p / nyz, pj = (p / P.nz) % P.ny, pk = p % P.nz;
-        bool claimed = false;
-        int q = 0;
-        const int nnb = SURF ? 9 : 18;
-        if (lane < nnb) {
-          const int di = (lane % 9) / 3 - 1, dj = lane % 3 - 1, dk = SURF ? 0 : (lane / 9) - 1;
-          const int ni = pi + di, nj = pj + dj, nk = pk + dk;
-          if (!(ni < 0 || ni > P.nx - 1 || nj < 0 || nj > P.ny - 1 || nk < 0)) {
-            q = (int)pid(P, ni, nj, nk);
-            if (__ldcg((const unsigned*)S.flag + q) == 0u) claimed = atomicCAS(&S.flag[q], 0u, 1u) == 0u;
-          }
-        }
-        unsigned m = __ballot_sync(0xffffffffu, claimed);
-        while (m) {
-          const int src = __ffs(m) - 1;
-          m &= m - 1;
-          const int qq = __shfl_sync(0xffffffffu, q, src);
-          const double T = warp_T<PREC>(P, nb, nn, qq);
-          pairs += nn;
+      unsigned ticket = 0;
+      if (lane == 0) ticket = atomicAdd(&X.qc->head, 1u);
+      ticket = __shfl_sync(0xffffffffu, ticket, 0);
+      int type, p = 0, aux = 0;
+      if (ticket < (unsigned)X.nL) {
+        type = IT_RETEST;
+        p = __ldcg(X.L + ticket);
+      } else if (ticket < (unsigned)X.n_init) {
+        type = IT_SEEDS;
+      } else {
+        const unsigned j = ticket - (unsigned)X.n_init;
+        bool ready = false, finished = false;
+        while (true) {
           if (lane == 0) {
-            set_T(S, P, qq, T, k);
-            push(Ro, reset_out, S.list_cap, qq, S.err);
-            if (T >= P.TL) {
-              push(Fout, fout_n, S.list_cap, qq, S.err);
-              push(Lo, liq_out, S.list_cap, qq, S.err);
+            const int tag = (j < (unsigned)S.queue_cap) ? ld_acquire_s32(&S.queue[j].x) : 0;
+            ready = tag == (int)X.stamp;
+            if (!ready) {
+              const unsigned long long st = ld_relaxed_u64(&X.qc->state);
+              finished = (unsigned)(st & 0xffffffffu) == (unsigned)X.n_init + (unsigned)(st >> 32);
             }
           }
-        }
-      }
-      if (!grid_sync(S)) return;
-      ++r;
-    }
-    if (tid == 0) { C->rounds = r; if (r > C->max_rounds) C->max_rounds = r; }
-
-    if (SURF && P.nz != 1) {
-      // F. depth walk under every liquid surface point (src/Melt.cpp:271-317)
-      const int nLo = ldcg_i(liq_out);
-      for (int i = warp; i < nLo; i += nwarps) {
-        const int p = __ldcg(Lo + i);
-        const int col = p / P.nz;
-        const int D = ldcg_i(S.depths + col);
-        int d = D;
-        bool none_deeper = true;
-        while (true) {
-          ++d;
-          if (d == P.nz) break;
-          const int q = col * P.nz + (P.nz - 1 - d);
-          const double T = warp_T<PREC>(P, nb, nn, q);
-          pairs += nn;
-          if (lane == 0) { set_T(S, P, q, T, k); push(Ro, reset_out, S.list_cap, q, S.err); }
-          if (!(T >= P.TL)) break;
-          none_deeper = false;
-        }
-        while (true) {
-          --d;
-          if (d == 0 || !none_deeper) break;
-          const int q = col * P.nz + (P.nz - 1 - d);
-          const double T = warp_T<PREC>(P, nb, nn, q);
-          pairs += nn;
-          if (lane == 0) { set_T(S, P, q, T, k); push(Ro, reset_out, S.list_cap, q, S.err); }
-          if (!(T >= P.TL)) {
-            double Tl;
-            if (d != D) { Tl = warp_T<PREC>(P, nbl, nnl, q); pairs += nnl; }
-            else Tl = ldcg_d(S.T_last + q);
+          ready = __shfl_sync(0xffffffffu, ready, 0);
+          finished = __shfl_sync(0xffffffffu, finished, 0);
+          if (ready || finished) break;
+          if (++idle > kSpinLimit) {
             if (lane == 0) {
-              if (d != D) S.T_last[q] = Tl;
-              push_record(S, q, k, t, T, Tl);
+              if (atomicOr(S.err, ERR_BARRIER) == 0) {        // first waiter to give up records its view
+                const unsigned long long st = ld_relaxed_u64(&X.qc->state);
+                int* g = S.C->diag;
+                g[0] = 1; g[1] = k; g[2] = (int)ticket; g[3] = X.n_init;
+                g[4] = (int)*(volatile unsigned*)&X.qc->head; g[5] = (int)(st >> 32);
+                g[6] = (int)(st >> 32); g[7] = (int)(st & 0xffffffffu);
+              }
             }
-          } else {
+            finished = true;
             break;
           }
+          __nanosleep(20);
         }
-        if (d == P.nz) --d;
-        if (lane == 0) S.depths[col] = d;
+        if (!ready) break;
+        const int4 it = __ldcg(S.queue + j);
+        type = it.y; p = it.z; aux = it.w;
       }
-      if (!grid_sync(S)) return;
-      // G. deepest liquid position per column, kept as a running maximum (src/Melt.cpp:319-357)
-      if (S.depth) {
-        for (int i = tid; i < nLo; i += nthreads) {
-          const int p = __ldcg(Lo + i);
-          const int col = p / P.nz;
-          const int dl = ldcg_i(S.depths + col);
-          double dep;
-          if (dl == P.nz - 1) dep = dl;
-          else {
-            const double Tl = ldcg_d(S.T + col * P.nz + (P.nz - 1 - dl));
-            const double Ts = ldcg_d(S.T + col * P.nz + (P.nz - 1 - (dl + 1)));
-            dep = rn_add((double)dl, rn_div(rn_sub(P.TL, Tl), rn_sub(Ts, Tl)));
-          }
-          if (dep > S.depth_max[col]) {
-            S.depth_max[col] = dep;
-            for (int d = dl; d >= 0; --d) S.depth[col * P.nz + (P.nz - 1 - d)] = dep;
-          }
-        }
-        if (!grid_sync(S)) return;
-      }
+      run_item<PREC, SURF>(P, S, X, type, p, aux, pairs);
+      __threadfence();
+      if (lane == 0) atomicAdd(&X.qc->state, 1ull);             // completed
     }
+    if (!grid_sync(S)) return;
     // finish test (src/Util.cpp:239-243) and the record queue's high-water mark
-    const int nLo = ldcg_i(liq_out);
-    if (tid == 0) C->step = k + 1;
-    if (t > P.end_time && nLo == 0) { if (tid == 0) C->done = 1; break; }
+    const int nLo = ldcg_i(X.lo_n);
+    if (tid == 0) {
+      C->step = k + 1;
+      const unsigned items = (unsigned)(__ldcg(&X.qc->state) >> 32) + (unsigned)X.n_init;
+      if ((int)items > C->max_items) C->max_items = (int)items;
+    }
+    if (X.t > P.end_time && nLo == 0) { if (tid == 0) C->done = 1; break; }
     if (ldcg_i(&C->rec_n) > high_water) { if (tid == 0) C->stop = 1; break; }
   }
   if (lane == 0 && pairs) atomicAdd(S.pairs, pairs);
@@ -680,7 +742,7 @@ static cudaError_t launch_track_t(const DevProblem& P, const TrackState& S, cons
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_track<PREC, SURF>, 256, 0);
-  const int blocks = sms * (occ < 2 ? occ : 2);
+  const int blocks = sms * (occ < 1 ? occ : 1);
   if (blocks <= 0) return cudaErrorInvalidConfiguration;
   DevProblem Pc = P;
   TrackState Sc = S;

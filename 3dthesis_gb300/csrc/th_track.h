@@ -18,28 +18,33 @@ struct SolRec {
   double Tl;       // temperature at the previous step (T_last)
 };
 
-// Per-step counters; one struct in device memory.
+// Per-step counters; one struct in device memory.  Lists rotate over three buffers by
+// step (k % 3: this step's liquid list, (k + 1) % 3: the next one, (k + 2) % 3: being
+// cleared), so no buffer is reset while another block may still read it.
+struct QueueCounters {
+  unsigned head;                 // tickets taken
+  unsigned unused;
+  unsigned long long state;      // (dynamic items published << 32) | items completed; the
+                                 // published count also hands out the items' queue slots
+  unsigned pad[4];
+};
+
 struct TrackCounters {
-  int liq_n[2];     // liquid list length (ping-pong by step parity)
-  int reset_n[2];   // reset list length
-  int col_n;        // column solidification work items
-  int seed_n;       // beam-trace seeds
+  int liq_n[3];     // liquid list lengths
   int rec_n;        // solidification records queued
   int step;         // next step to run
   int done;         // finish test passed
   int stop;         // the loop stopped early (record queue high-water mark)
-  int rounds;       // frontier rounds of the last step
-  int max_rounds;   // largest number of rounds in one step
-  int front_n[4096];// frontier length per round of the current step
+  int max_items;    // most work items in one step
+  int diag[8];      // where a bounded wait gave up: kind, step, ticket, n_init, head, tail, published, completed
+  QueueCounters q[3];
 };
-
-constexpr int kMaxFrontRounds = 4095;
 
 // Device pointers of the solidification state.
 struct TrackState {
   double* T;
-  double* T_last;
-  unsigned* flag;          // T_calc_flag
+  double* T_last;          // NoTracking only
+  unsigned* stamp;         // claim stamp: claimed in step k <=> stamp >= k + 1
   unsigned char* outflag;  // output_flag
   int* last_liq;           // last step at which the point was liquid (-1: never)
   int* num_melt;
@@ -48,12 +53,10 @@ struct TrackState {
   double* depth;           // per point (Surface with depth output), may be null
   int* depths;             // per (i, j) column: deepest liquid layer
   double* depth_max;       // per column
-  int* liq[2];
-  int* reset[2];
-  int* front[2];
-  int2* colwork;           // (point, recompute T_last?)
-  int* seeds;
+  int* liq[3];
   int list_cap;
+  int4* queue;             // work items {tag, type, point, aux}
+  int queue_cap;
   SolRec* rec;
   int rec_cap;
   TrackCounters* C;
@@ -73,7 +76,7 @@ struct NodeWindow {
 };
 
 // Error bits written by the solidification kernels (besides the node bits).
-enum { ERR_BARRIER = 16, ERR_RECORDS = 32, ERR_LISTS = 64, ERR_ROUNDS = 128 };
+enum { ERR_BARRIER = 16, ERR_RECORDS = 32, ERR_LISTS = 64, ERR_QUEUE = 128 };
 
 void th_launch_nodes_window(const DevProblem& P, const NodeWindow& w, int first_slot, int nslots, bool is_sol,
                             int* d_err, cudaStream_t s);

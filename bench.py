@@ -192,13 +192,13 @@ def run_solidification(args, th, torch, dev, path, deck, world):
             "achieved": achieved / 1e9, "peak": peak_pairs / 1e9, "unit": "Gpairs/s", "frac": achieved / peak_pairs,
             "peak_basis": f"{SM_COUNT} SMs x {clk_mhz:.0f} MHz x min({FP32_LANES}/{FP32_OPS_KAHAN} FP32 issue, "
                           f"{MUFU_LANES} MUFU) pairs/clk",
-            "note": "each timestep evaluates ~1e3 points x ~300 nodes between grid-wide barriers; the loop is bound "
-                    "by per-step latency, not by FP32/MUFU issue or HBM",
+            "note": "each timestep evaluates ~1e3 points x ~300 nodes in a work queue closed by one grid barrier; "
+                    "the loop is bound by per-step latency, not by FP32/MUFU issue or HBM",
             "traffic": None, "peak_source": src}
     sim.close()
     detail = {"steps": int(st["steps"]), "pairs_per_step": pairs, "ms_node_windows": st["ms_nodes"],
               "ms_tracking": st["ms_track"], "ms_solidify": st["ms_solidify"], "records": int(st["records"]),
-              "max_frontier_rounds": int(st["max_rounds"]), "wall_s_per_step": statistics.median(wall),
+              "max_items_per_step": int(st["max_items"]), "wall_s_per_step": statistics.median(wall),
               "device_s_per_step": statistics.median(dev_s)}
     return {"value": value, "ms_per_step": 1e3 * total_s / args.steps, "e2e": e2e, "roofline": roof,
             "clocks": clk, "gpu_launches": launches * args.steps, "detail": detail}

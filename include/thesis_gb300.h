@@ -135,7 +135,7 @@ th_status th_run_reset(th_ctx* ctx);
 
 /* Device time and counters of the solidification loop so far, out[0..n): ms building
  * node windows, ms in the tracking / NoTracking steps, ms solidifying records, windows,
- * records, largest number of frontier rounds in one step, steps, node slots per step,
+ * records, most work items in one step (tracking), steps, node slots per step,
  * device-elapsed ms of th_solidify calls (host gaps included), point x node pairs of the
  * bulk solidification, all point x node pairs of the context. */
 th_status th_run_stats(th_ctx* ctx, double* out, int32_t n);
