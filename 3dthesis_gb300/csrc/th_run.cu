@@ -1,10 +1,13 @@
 // Mode drivers behind th_simulate / th_solidify / th_field.
 //
-// Solidification (src/Run.cpp:390-709) runs in windows of steps: the host lays out the
-// step times exactly as the reference accumulates them (t += dt), one kernel builds the
-// window's node lists (one warp per step), then either the persistent tracking kernel
-// (Volume / Surface) or one whole-grid kernel per step (NoTracking) advances the state,
-// and the queued liquid -> solid records are solidified in bulk.
+// Solidification (src/Run.cpp:390-709) runs in windows of steps.  The host lays out the
+// step times exactly as the reference accumulates them (t += dt); one kernel builds a
+// window's node lists (one warp per step); the persistent tracking kernel (Volume /
+// Surface) or one whole-grid kernel per step (NoTracking) advances the state; and the
+// queued liquid -> solid records are solidified in bulk.  For the tracking modes the three
+// overlap: while the tracking kernel runs window w on the context's stream, a second
+// stream builds the node lists of window w + 1 and solidifies the records of window w - 1
+// (two node windows and two record buffers, ordered by events).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -24,7 +27,17 @@ enum { F_T, F_TSOL, F_G, F_V, F_GX, F_GY, F_GZ, F_DTDT, F_EQ, F_NUMMELT, F_DEPTH
 
 constexpr int kWindowTrack = 256;     // steps per node window (tracking)
 constexpr int kWindowNoTrack = 32;    // steps per node window (NoTracking: whole grid per step)
-constexpr int kRecCap = 1 << 22;      // queued solidification records
+constexpr int kRecCap = 1 << 22;      // solidification records per buffer
+
+struct Window {
+  void* mem = nullptr;
+  NodeWindow W{};
+  double* d_t = nullptr;
+  int* d_count = nullptr;
+  int slots = 0;
+  int base = 0, n = 0;                // steps [base, base + n) in slots 1..n
+  cudaEvent_t gen0 = nullptr, gen1 = nullptr;   // around the node build
+};
 
 }  // namespace
 
@@ -32,21 +45,20 @@ struct RunState {
   TrackState S{};
   std::vector<void*> allocs;
   std::vector<std::pair<size_t, int>> alloc_fill;   // bytes and fill byte of each allocation
-  void* win_mem = nullptr;
-  NodeWindow W{};
-  double* d_t = nullptr;
-  int* d_count = nullptr;
-  int win_slots = 0;
+  Window win[2];
+  SolRec* rec[2] = {nullptr, nullptr};
   int slot_cap = 1024;
   int k = 0;              // next step
-  double t_prev = 0.0;    // time of step k - 1
-  double t_next = 0.0;    // time of step k
+  std::vector<double> times;   // step times, accumulated as the reference does
   bool done = false;
   bool initialised = false;
-  int max_rounds = 0;
+  int max_items = 0;
   double* d_field = nullptr;
-  // device time per phase (ms) and counts, for th_run_stats
-  cudaEvent_t ev[2] = {nullptr, nullptr};
+  cudaStream_t aux = nullptr;
+  int* h_err = nullptr;        // pinned: node-build error bits per window
+  cudaEvent_t ev_trk[2][2] = {};  // around each window's tracking launch
+  cudaEvent_t ev_sol[2][2] = {};  // around each record buffer's solidification
+  bool sol_timed[2] = {true, true};  // the events of ev_sol[b] have been added to ms_solid
   cudaEvent_t ev_run[2] = {nullptr, nullptr};
   double ms_nodes = 0, ms_track = 0, ms_solid = 0, ms_device = 0;
   long long windows = 0, records = 0;
@@ -55,15 +67,23 @@ struct RunState {
 void th_release_run_state(th_ctx* ctx) {
   RunState* r = ctx->run;
   if (!r) return;
+  if (r->aux) cudaStreamSynchronize(r->aux);
   for (void* p : r->allocs) cudaFree(p);
-  cudaFree(r->win_mem);
-  cudaFree(r->d_t);
-  cudaFree(r->d_count);
+  for (Window& w : r->win) {
+    cudaFree(w.mem); cudaFree(w.d_t); cudaFree(w.d_count);
+    if (w.gen0) cudaEventDestroy(w.gen0);
+    if (w.gen1) cudaEventDestroy(w.gen1);
+  }
   cudaFree(r->d_field);
-  if (r->ev[0]) cudaEventDestroy(r->ev[0]);
-  if (r->ev[1]) cudaEventDestroy(r->ev[1]);
+  if (r->h_err) cudaFreeHost(r->h_err);
+  for (int b = 0; b < 2; ++b)
+    for (int e = 0; e < 2; ++e) {
+      if (r->ev_trk[b][e]) cudaEventDestroy(r->ev_trk[b][e]);
+      if (r->ev_sol[b][e]) cudaEventDestroy(r->ev_sol[b][e]);
+    }
   if (r->ev_run[0]) cudaEventDestroy(r->ev_run[0]);
   if (r->ev_run[1]) cudaEventDestroy(r->ev_run[1]);
+  if (r->aux) cudaStreamDestroy(r->aux);
   delete r;
   ctx->run = nullptr;
 }
@@ -86,6 +106,14 @@ __global__ void k_fill_d(double* a, int64_t n, double v) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) a[i] = v;
 }
 
+double time_of(RunState* r, double dt, int k) {
+  while ((int)r->times.size() <= k) {
+    if (r->times.empty()) r->times.push_back(0.0);
+    else r->times.push_back(r->times.back() + dt);
+  }
+  return r->times[k];
+}
+
 th_status init_run(th_ctx* ctx) {
   const HostProblem& hp = ctx->hp;
   if (hp.pnum >= INT_MAX) return th_fail(ctx, TH_ERR_CAPACITY, "solidification needs fewer than 2^31 points");
@@ -97,7 +125,7 @@ th_status init_run(th_ctx* ctx) {
   th_status st = TH_OK;
 #define ALLOC(ptr, cnt, fill) if ((st = dalloc(ctx, r, &(ptr), (cnt), (fill))) != TH_OK) return st
   ALLOC(S.T, n, 0);
-  ALLOC(S.T_last, n, 0);
+  if (hp.tracking == TH_TRACK_NONE) ALLOC(S.T_last, n, 0);
   ALLOC(S.stamp, n, 0);
   ALLOC(S.outflag, n, 0);
   ALLOC(S.last_liq, n, 0xff);   // -1
@@ -119,106 +147,116 @@ th_status init_run(th_ctx* ctx) {
   if (hp.tracking != TH_TRACK_NONE) {
     S.list_cap = (int)n;
     for (int i = 0; i < 3; ++i) ALLOC(S.liq[i], n, 0);
-    // work items of one step: every claimed point, column layer and depth walk at most
-    // once, which in practice stays far below 2 * pnum
+    // work items of one step: every claimed point and column layer at most once, which
+    // in practice stays far below 2 * pnum
     S.queue_cap = (int)std::min<size_t>(2 * n + 4096, (size_t)1 << 24);
     ALLOC(S.queue, (size_t)S.queue_cap, 0);
   }
   S.rec_cap = kRecCap;
-  ALLOC(S.rec, (size_t)kRecCap, 0);
+  ALLOC(r->rec[0], (size_t)kRecCap, 0);
+  ALLOC(r->rec[1], (size_t)kRecCap, 0);
   ALLOC(S.C, 1, 0);
   ALLOC(S.bar, 2, 0);
   ALLOC(S.err, 1, 0);
 #undef ALLOC
   S.pairs = ctx->d_pairs;
+  S.rec = r->rec[0];
+  S.rec_n = &S.C->rec_n[0];
   if (hp.tracking == TH_TRACK_NONE) {                 // NoTracking starts every point at T_0
     k_fill_d<<<1024, 256, 0, ctx->stream>>>(S.T, (int64_t)n, hp.T0);
     st = th_cuda_check(ctx, cudaGetLastError(), "fill");
     if (st != TH_OK) return st;
   }
-  r->k = 0;
-  r->t_prev = 0.0;
-  r->t_next = 0.0;
-  r->initialised = true;
-  cudaEventCreate(&r->ev[0]);
-  cudaEventCreate(&r->ev[1]);
+  if ((st = th_cuda_check(ctx, cudaStreamCreateWithFlags(&r->aux, cudaStreamNonBlocking), "stream")) != TH_OK) return st;
+  if ((st = th_cuda_check(ctx, cudaHostAlloc((void**)&r->h_err, 4 * sizeof(int), cudaHostAllocDefault), "host")) != TH_OK)
+    return st;
+  for (int b = 0; b < 2; ++b) {
+    cudaEventCreate(&r->win[b].gen0); cudaEventCreate(&r->win[b].gen1);
+    for (int e = 0; e < 2; ++e) { cudaEventCreate(&r->ev_trk[b][e]); cudaEventCreate(&r->ev_sol[b][e]); }
+  }
   cudaEventCreate(&r->ev_run[0]);
   cudaEventCreate(&r->ev_run[1]);
+  r->k = 0;
+  r->initialised = true;
   return th_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "init");
 }
 
-th_status alloc_window(th_ctx* ctx, RunState* r, int slots, int slot_cap) {
-  cudaFree(r->win_mem); r->win_mem = nullptr;
-  cudaFree(r->d_t); r->d_t = nullptr;
-  cudaFree(r->d_count); r->d_count = nullptr;
+th_status alloc_window(th_ctx* ctx, Window& w, int slots, int slot_cap) {
+  cudaFree(w.mem); w.mem = nullptr;
+  cudaFree(w.d_t); w.d_t = nullptr;
+  cudaFree(w.d_count); w.d_count = nullptr;
   const size_t cap = (size_t)slots * slot_cap;
-  th_status st = th_cuda_check(ctx, cudaMalloc(&r->win_mem, cap * (8 * sizeof(double) + 10 * sizeof(float))), "cudaMalloc");
+  th_status st = th_cuda_check(ctx, cudaMalloc(&w.mem, cap * (8 * sizeof(double) + 10 * sizeof(float))), "cudaMalloc");
   if (st != TH_OK) return st;
-  st = th_cuda_check(ctx, cudaMalloc(&r->d_t, slots * sizeof(double)), "cudaMalloc");
-  if (st != TH_OK) return st;
-  st = th_cuda_check(ctx, cudaMalloc(&r->d_count, slots * sizeof(int)), "cudaMalloc");
-  if (st != TH_OK) return st;
-  double* d = (double*)r->win_mem;
+  if ((st = th_cuda_check(ctx, cudaMalloc(&w.d_t, slots * sizeof(double)), "cudaMalloc")) != TH_OK) return st;
+  if ((st = th_cuda_check(ctx, cudaMalloc(&w.d_count, slots * sizeof(int)), "cudaMalloc")) != TH_OK) return st;
+  double* d = (double*)w.mem;
   float* f = (float*)(d + 8 * cap);
-  NodeBufView& nb = r->W.nb;
+  NodeBufView& nb = w.W.nb;
   nb.cap = (int)cap;
   nb.x = d; nb.y = d + cap; nb.z = d + 2 * cap; nb.ipx = d + 3 * cap; nb.ipy = d + 4 * cap; nb.ipz = d + 5 * cap;
   nb.dtau = d + 6 * cap; nb.amp = d + 7 * cap;
   nb.kx = f; nb.ky = f + cap; nb.kz = f + 2 * cap; nb.w = f + 3 * cap; nb.xh = f + 4 * cap; nb.xl = f + 5 * cap;
   nb.yh = f + 6 * cap; nb.yl = f + 7 * cap; nb.zh = f + 8 * cap; nb.zl = f + 9 * cap;
-  r->W.slot_cap = slot_cap;
-  r->W.nslots = slots;
-  r->W.count = r->d_count;
-  r->W.t = r->d_t;
-  r->win_slots = slots;
-  r->slot_cap = slot_cap;
+  w.W.slot_cap = slot_cap;
+  w.W.nslots = slots;
+  w.W.count = w.d_count;
+  w.W.t = w.d_t;
+  w.slots = slots;
   return TH_OK;
 }
 
-// Builds the node lists of steps [k, k + n) (slots 1..n) and of step k - 1 (slot 0).
-th_status build_window(th_ctx* ctx, RunState* r, int n, std::vector<double>& ts) {
-  const HostProblem& hp = ctx->hp;
-  ts.assign(n + 1, 0.0);
-  ts[0] = r->t_prev;
-  double t = r->t_next;
-  for (int i = 1; i <= n; ++i) { ts[i] = t; t = t + hp.dt; }
+// Enqueues the node lists of steps [base, base + n) (slots 1..n) and of step base - 1
+// (slot 0) into window b on `s`; the error bits land in h_err[b] when w.gen1 completes.
+th_status enqueue_window(th_ctx* ctx, RunState* r, int b, int base, int n, cudaStream_t s) {
+  Window& w = r->win[b];
+  if (!w.mem || w.slots < n + 1 || w.W.slot_cap != r->slot_cap) {
+    th_status st = alloc_window(ctx, w, std::max(n + 1, std::max(w.slots, kWindowTrack + 1)), r->slot_cap);
+    if (st != TH_OK) return st;
+  }
+  std::vector<double> ts(n + 1);
+  ts[0] = base > 0 ? time_of(r, ctx->hp.dt, base - 1) : 0.0;
+  for (int i = 1; i <= n; ++i) ts[i] = time_of(r, ctx->hp.dt, base + i - 1);
+  w.base = base; w.n = n; w.W.base = base;
+  th_status st = th_cuda_check(ctx, cudaMemcpyAsync(w.d_t, ts.data(), (n + 1) * sizeof(double), cudaMemcpyHostToDevice, s),
+                               "cudaMemcpyAsync");
+  if (st != TH_OK) return st;
+  int* d_err = ctx->d_small + 2 + b;
+  if ((st = th_cuda_check(ctx, cudaMemsetAsync(d_err, 0, sizeof(int), s), "cudaMemsetAsync")) != TH_OK) return st;
+  const int first = base == 0 ? 1 : 0;
+  cudaEventRecord(w.gen0, s);
+  th_launch_nodes_window(ctx->dp, w.W, first, n + 1 - first, false, d_err, s);
+  if ((st = th_cuda_check(ctx, cudaGetLastError(), "node window")) != TH_OK) return st;
+  if ((st = th_cuda_check(ctx, cudaMemcpyAsync(r->h_err + b, d_err, sizeof(int), cudaMemcpyDeviceToHost, s), "copy")) != TH_OK)
+    return st;
+  cudaEventRecord(w.gen1, s);
+  r->windows++;
+  return TH_OK;
+}
+
+// Waits for window b's node build; on a capacity overflow grows the slots and rebuilds it
+// synchronously.  *ok is false when the build had to be redone.
+th_status finish_window(th_ctx* ctx, RunState* r, int b) {
+  Window& w = r->win[b];
   for (int attempt = 0; attempt < 4; ++attempt) {
-    if (!r->win_mem || r->win_slots < n + 1) {
-      th_status st = alloc_window(ctx, r, std::max(n + 1, r->win_slots), r->slot_cap);
-      if (st != TH_OK) return st;
-    }
-    r->W.base = r->k;
-    th_status st = th_cuda_check(ctx, cudaMemcpyAsync(r->d_t, ts.data(), (n + 1) * sizeof(double),
-                                                      cudaMemcpyHostToDevice, ctx->stream), "cudaMemcpyAsync");
-    if (st != TH_OK) return st;
-    st = th_cuda_check(ctx, cudaMemsetAsync(ctx->d_small + 1, 0, sizeof(int), ctx->stream), "cudaMemsetAsync");
-    if (st != TH_OK) return st;
-    const int first = r->k == 0 ? 1 : 0;
-    cudaEventRecord(r->ev[0], ctx->stream);
-    th_launch_nodes_window(ctx->dp, r->W, first, n + 1 - first, false, ctx->d_small + 1, ctx->stream);
-    cudaEventRecord(r->ev[1], ctx->stream);
-    st = th_cuda_check(ctx, cudaGetLastError(), "node window");
-    if (st != TH_OK) return st;
-    int err = 0;
-    std::vector<int> cnt(n + 1);
-    st = th_cuda_check(ctx, cudaMemcpyAsync(&err, ctx->d_small + 1, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream), "copy");
-    if (st != TH_OK) return st;
-    st = th_cuda_check(ctx, cudaMemcpyAsync(cnt.data(), r->d_count, (n + 1) * sizeof(int), cudaMemcpyDeviceToHost,
-                                            ctx->stream), "copy");
-    if (st != TH_OK) return st;
-    st = th_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "node window");
+    th_status st = th_cuda_check(ctx, cudaEventSynchronize(w.gen1), "node window");
     if (st != TH_OK) return st;
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, r->ev[0], r->ev[1]);
+    cudaEventElapsedTime(&ms, w.gen0, w.gen1);
     r->ms_nodes += ms;
-    r->windows++;
+    const int err = r->h_err[b];
     if (err & 2) return th_fail(ctx, TH_ERR_TIMEOUT, "quadrature walk exceeded its step limit");
     if (!(err & 1)) return TH_OK;
+    std::vector<int> cnt(w.n + 1);
+    st = th_cuda_check(ctx, cudaMemcpy(cnt.data(), w.d_count, (w.n + 1) * sizeof(int), cudaMemcpyDeviceToHost), "copy");
+    if (st != TH_OK) return st;
     int mx = 0;
-    for (int i = first; i <= n; ++i) mx = std::max(mx, cnt[i]);
-    r->slot_cap = ((mx + 256) / 32 + 1) * 32;
-    th_status st2 = alloc_window(ctx, r, r->win_slots, r->slot_cap);
-    if (st2 != TH_OK) return st2;
+    for (int i = (w.base == 0 ? 1 : 0); i <= w.n; ++i) mx = std::max(mx, cnt[i]);
+    r->slot_cap = std::max(r->slot_cap, ((mx + 256) / 32 + 1) * 32);
+    // the other window may still be in use by the tracking stream or the aux stream
+    cudaStreamSynchronize(r->aux);
+    cudaStreamSynchronize(ctx->stream);
+    if ((st = enqueue_window(ctx, r, b, w.base, w.n, r->aux)) != TH_OK) return st;
   }
   return th_fail(ctx, TH_ERR_CAPACITY, "node window growth did not converge");
 }
@@ -246,64 +284,137 @@ th_status read_counters(th_ctx* ctx, RunState* r, TrackCounters* h) {
   return TH_OK;
 }
 
-th_status drain_records(th_ctx* ctx, RunState* r, int nrec) {
-  if (nrec <= 0) return TH_OK;
-  th_launch_solidify(ctx->dp, r->S, std::min(nrec, r->S.rec_cap), ctx->precision, ctx->hp.do_sol, ctx->stream);
-  th_status st = th_cuda_check(ctx, cudaGetLastError(), "solidify");
-  if (st != TH_OK) return st;
-  return th_cuda_check(ctx, cudaMemsetAsync(&r->S.C->rec_n, 0, sizeof(int), ctx->stream), "cudaMemsetAsync");
+void add_elapsed(double& acc, cudaEvent_t a, cudaEvent_t b);
+
+// Solidifies record buffer b (nrec records) on stream s, then empties it.  The previous
+// use of the buffer's events has completed by then (the tracking launch in between waited
+// for it), so its time is added first.
+th_status solidify_buffer(th_ctx* ctx, RunState* r, int b, int nrec, cudaStream_t s) {
+  if (!r->sol_timed[b]) { add_elapsed(r->ms_solid, r->ev_sol[b][0], r->ev_sol[b][1]); r->sol_timed[b] = true; }
+  r->sol_timed[b] = false;
+  cudaEventRecord(r->ev_sol[b][0], s);
+  if (nrec > 0) {
+    th_launch_solidify(ctx->dp, r->S, r->rec[b], std::min(nrec, r->S.rec_cap), ctx->precision, ctx->hp.do_sol, s);
+    th_status st = th_cuda_check(ctx, cudaGetLastError(), "solidify");
+    if (st != TH_OK) return st;
+  }
+  th_status st = th_cuda_check(ctx, cudaMemsetAsync(&r->S.C->rec_n[b], 0, sizeof(int), s), "cudaMemsetAsync");
+  cudaEventRecord(r->ev_sol[b][1], s);
+  r->records += nrec;
+  return st;
 }
 
-// Advances the solidification loop until it finishes, reaches step `stop_at` (exclusive)
-// or max_steps.
-th_status advance(th_ctx* ctx, int64_t stop_at) {
+void add_elapsed(double& acc, cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, a, b) == cudaSuccess) acc += ms;
+}
+
+// Tracking modes: pipelined windows.
+th_status advance_tracking(th_ctx* ctx, int64_t stop_at) {
   RunState* r = ctx->run;
   const HostProblem& hp = ctx->hp;
-  const bool track = hp.tracking != TH_TRACK_NONE;
-  const int window = track ? kWindowTrack : kWindowNoTrack;
-  std::vector<double> ts;
-  while (!r->done && r->k < stop_at) {
-    const int n = (int)std::min<int64_t>(window, stop_at - r->k);
-    th_status st = build_window(ctx, r, n, ts);
+  cudaStream_t ts = ctx->stream, as = r->aux;
+  int b = 0;
+  int pending_rec[2] = {0, 0};
+  bool pending_sol[2] = {false, false};
+  int n0 = (int)std::min<int64_t>(kWindowTrack, stop_at - r->k);
+  if (n0 <= 0 || r->done) return TH_OK;
+  th_status st = enqueue_window(ctx, r, b, r->k, n0, as);
+  if (st != TH_OK) return st;
+  while (true) {
+    if ((st = finish_window(ctx, r, b)) != TH_OK) return st;
+    Window& w = r->win[b];
+    // the tracking launch may reuse record buffer b only after its last solidification
+    cudaStreamWaitEvent(ts, w.gen1, 0);
+    if (pending_sol[b]) cudaStreamWaitEvent(ts, r->ev_sol[b][1], 0);
+    TrackState S = r->S;
+    S.rec = r->rec[b];
+    S.rec_n = &r->S.C->rec_n[b];
+    if ((st = th_cuda_check(ctx, cudaMemsetAsync(r->S.bar, 0, 2 * sizeof(unsigned), ts), "cudaMemsetAsync")) != TH_OK) return st;
+    cudaEventRecord(r->ev_trk[b][0], ts);
+    st = th_cuda_check(ctx, th_launch_track(ctx->dp, S, w.W, w.base, w.base + w.n, ctx->precision, r->S.rec_cap / 2, ts),
+                       "cooperative launch");
     if (st != TH_OK) return st;
-    TrackCounters h;
-    cudaEventRecord(r->ev[0], ctx->stream);
-    if (track) {
-      st = th_cuda_check(ctx, cudaMemsetAsync(r->S.bar, 0, 2 * sizeof(unsigned), ctx->stream), "cudaMemsetAsync");
-      if (st != TH_OK) return st;
-      st = th_cuda_check(ctx, th_launch_track(ctx->dp, r->S, r->W, r->k, r->k + n, ctx->precision, r->S.rec_cap / 2,
-                                              ctx->stream), "cooperative launch");
-      if (st != TH_OK) return st;
-    } else {
-      for (int k = r->k; k < r->k + n; ++k) th_launch_notrack_step(ctx->dp, r->S, r->W, k, ctx->precision, ctx->stream);
-      st = th_cuda_check(ctx, cudaGetLastError(), "notrack step");
-      if (st != TH_OK) return st;
+    cudaEventRecord(r->ev_trk[b][1], ts);
+    // meanwhile, on the aux stream: solidify the previous window's records and build the
+    // next window (its buffer was last read by the previous tracking launch)
+    const int nb = b ^ 1;
+    if (pending_rec[nb] > 0 || pending_sol[nb]) {
+      cudaStreamWaitEvent(as, r->ev_trk[nb][1], 0);
+      if ((st = solidify_buffer(ctx, r, nb, pending_rec[nb], as)) != TH_OK) return st;
+      pending_rec[nb] = 0;
     }
-    cudaEventRecord(r->ev[1], ctx->stream);
-    st = read_counters(ctx, r, &h);
-    if (st != TH_OK) return st;
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, r->ev[0], r->ev[1]);
-    r->ms_track += ms;
-    cudaEventRecord(r->ev[0], ctx->stream);
-    st = drain_records(ctx, r, h.rec_n);
-    if (st != TH_OK) return st;
-    cudaEventRecord(r->ev[1], ctx->stream);
-    r->records += h.rec_n;
+    const int next_base = w.base + w.n;
+    const int next_n = (int)std::min<int64_t>(kWindowTrack, stop_at - next_base);
+    bool prefetched = false;
+    if (next_n > 0) {
+      cudaStreamWaitEvent(as, r->ev_trk[nb][1], 0);
+      if ((st = enqueue_window(ctx, r, nb, next_base, next_n, as)) != TH_OK) return st;
+      prefetched = true;
+    }
+    TrackCounters h;
+    if ((st = read_counters(ctx, r, &h)) != TH_OK) return st;
+    add_elapsed(r->ms_track, r->ev_trk[b][0], r->ev_trk[b][1]);
+    pending_rec[b] = h.rec_n[b];
+    pending_sol[b] = true;
+    r->max_items = std::max(r->max_items, h.max_items);
     const int k_new = h.step;
     if (k_new <= r->k && !h.done) return th_fail(ctx, TH_ERR_INVALID, "solidification loop made no progress");
-    // times of the steps actually run (slots are 1-based from r->k)
-    const int ran = k_new - r->k;
-    r->t_prev = ts[ran];
-    r->t_next = ran + 1 <= n ? ts[ran + 1] : ts[n] + hp.dt;
     r->k = k_new;
     r->done = h.done != 0;
-    cudaEventSynchronize(r->ev[1]);
-    cudaEventElapsedTime(&ms, r->ev[0], r->ev[1]);
-    r->ms_solid += ms;
-    r->max_rounds = std::max(r->max_rounds, h.max_items);
+    if (r->done || r->k >= stop_at) break;
+    if (r->k != next_base || !prefetched) {
+      // stopped early at the record high-water mark: rebuild the next window from here
+      cudaStreamSynchronize(as);
+      const int n = (int)std::min<int64_t>(kWindowTrack, stop_at - r->k);
+      if ((st = enqueue_window(ctx, r, nb, r->k, n, as)) != TH_OK) return st;
+    }
+    b = nb;
   }
-  return th_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "solidification");
+  // drain: both record buffers, then wait for both streams
+  for (int i = 0; i < 2; ++i) {
+    const int bb = b ^ 1 ^ i;       // the older buffer first
+    if (pending_rec[bb] > 0) {
+      cudaStreamWaitEvent(as, r->ev_trk[bb][1], 0);
+      if ((st = solidify_buffer(ctx, r, bb, pending_rec[bb], as)) != TH_OK) return st;
+      pending_rec[bb] = 0;
+    }
+  }
+  if ((st = th_cuda_check(ctx, cudaStreamSynchronize(as), "solidify")) != TH_OK) return st;
+  for (int i = 0; i < 2; ++i)
+    if (!r->sol_timed[i]) { add_elapsed(r->ms_solid, r->ev_sol[i][0], r->ev_sol[i][1]); r->sol_timed[i] = true; }
+  return th_cuda_check(ctx, cudaStreamSynchronize(ts), "solidification");
+}
+
+// NoTracking: one whole-grid kernel per step, windows built and drained in sequence.
+th_status advance_notrack(th_ctx* ctx, int64_t stop_at) {
+  RunState* r = ctx->run;
+  while (!r->done && r->k < stop_at) {
+    const int n = (int)std::min<int64_t>(kWindowNoTrack, stop_at - r->k);
+    th_status st = enqueue_window(ctx, r, 0, r->k, n, ctx->stream);
+    if (st != TH_OK) return st;
+    if ((st = finish_window(ctx, r, 0)) != TH_OK) return st;
+    TrackState S = r->S;
+    cudaEventRecord(r->ev_trk[0][0], ctx->stream);
+    for (int k = r->k; k < r->k + n; ++k) th_launch_notrack_step(ctx->dp, S, r->win[0].W, k, ctx->precision, ctx->stream);
+    if ((st = th_cuda_check(ctx, cudaGetLastError(), "notrack step")) != TH_OK) return st;
+    cudaEventRecord(r->ev_trk[0][1], ctx->stream);
+    TrackCounters h;
+    if ((st = read_counters(ctx, r, &h)) != TH_OK) return st;
+    add_elapsed(r->ms_track, r->ev_trk[0][0], r->ev_trk[0][1]);
+    if ((st = solidify_buffer(ctx, r, 0, h.rec_n[0], ctx->stream)) != TH_OK) return st;
+    if ((st = th_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "solidify")) != TH_OK) return st;
+    add_elapsed(r->ms_solid, r->ev_sol[0][0], r->ev_sol[0][1]);
+    r->sol_timed[0] = true;
+    if (h.step <= r->k && !h.done) return th_fail(ctx, TH_ERR_INVALID, "solidification loop made no progress");
+    r->k = h.step;
+    r->done = h.done != 0;
+  }
+  return TH_OK;
+}
+
+th_status advance(th_ctx* ctx, int64_t stop_at) {
+  return ctx->hp.tracking == TH_TRACK_NONE ? advance_notrack(ctx, stop_at) : advance_tracking(ctx, stop_at);
 }
 
 int field_id(const std::string& f) {
@@ -410,7 +521,8 @@ th_status th_run_reset(th_ctx* ctx) {
     if (st != TH_OK) return st;
   }
   if (ctx->hp.tracking == TH_TRACK_NONE) k_fill_d<<<1024, 256, 0, ctx->stream>>>(r->S.T, (int64_t)ctx->hp.pnum, ctx->hp.T0);
-  r->k = 0; r->t_prev = 0.0; r->t_next = 0.0; r->done = false; r->max_rounds = 0;
+  r->k = 0; r->done = false; r->max_items = 0;
+  r->sol_timed[0] = r->sol_timed[1] = true;
   r->ms_nodes = r->ms_track = r->ms_solid = r->ms_device = 0;
   r->windows = r->records = 0;
   st = th_cuda_check(ctx, cudaMemsetAsync(ctx->d_pairs, 0, 2 * sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
@@ -425,7 +537,7 @@ th_status th_run_stats(th_ctx* ctx, double* out, int32_t n) {
   th_status st = th_cuda_check(ctx, cudaMemcpy(pairs, ctx->d_pairs, sizeof(pairs), cudaMemcpyDeviceToHost), "cudaMemcpy");
   if (st != TH_OK) return st;
   const double v[11] = {r ? r->ms_nodes : 0, r ? r->ms_track : 0, r ? r->ms_solid : 0, r ? (double)r->windows : 0,
-                        r ? (double)r->records : 0, r ? (double)r->max_rounds : 0, r ? (double)r->k : 0,
+                        r ? (double)r->records : 0, r ? (double)r->max_items : 0, r ? (double)r->k : 0,
                         r ? (double)r->slot_cap : 0, r ? r->ms_device : 0, (double)pairs[1],
                         (double)pairs[0]};
   for (int i = 0; i < n && i < 11; ++i) out[i] = v[i];

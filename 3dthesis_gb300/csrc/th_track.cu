@@ -92,7 +92,7 @@ __device__ __forceinline__ int ldcg_i(const int* p) { return __ldcg(p); }
 __device__ __forceinline__ double ldcg_d(const double* p) { return __ldcg(p); }
 
 __device__ __forceinline__ void push_record(const TrackState& S, int p, int step, double t, double T, double Tl) {
-  const int i = atomicAdd(&S.C->rec_n, 1);
+  const int i = atomicAdd(S.rec_n, 1);
   if (i < S.rec_cap) { SolRec r; r.p = p; r.step = step; r.t = t; r.T = T; r.Tl = Tl; S.rec[i] = r; }
   else atomicOr(S.err, ERR_RECORDS);
   atomicAdd(&S.num_melt[p], 1);
@@ -409,21 +409,23 @@ __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx&
     }
   }
   if (liquid && lane == 0) push_liquid(S, X, p);
-  if (SURF) emit(S, X, liquid && lane == 0, IT_DEPTH, p, 0, nchild);
   // Surface expands every re-tested point, Volume only the liquid ones (src/Run.cpp:655, 531)
   if (liquid || (SURF && type == IT_RETEST)) expand<SURF>(P, S, X, p, nchild);
+  // the depth walk under a liquid surface point needs nothing else from this step
+  if (SURF && liquid) depth_walk<PREC>(P, S, X, p, pairs);
   return nchild;
 }
 
 // ------------------------------------------------------------------ the tracking loop
+constexpr int kTrackThreads = 128;   // four warps per block, one block per SM
 // One launch runs steps [k_begin, k_end) of a Volume or Surface loop (src/Run.cpp:469-709).
 // Each step is a single phase: the previous step's liquid points are re-tested, the beam
 // trace seeds the new ones, and every claimed point, column and depth walk becomes a work
 // item that any warp may take; a packed (published << 32 | completed) counter tells the
 // warps when the step has no work left, and one grid barrier ends the step.
 template <int PREC, bool SURF>
-__global__ void __launch_bounds__(256) k_track(DevProblem P, TrackState S, NodeWindow W, int k_begin, int k_end,
-                                               int high_water) {
+__global__ void __launch_bounds__(kTrackThreads) k_track(DevProblem P, TrackState S, NodeWindow W, int k_begin,
+                                                        int k_end, int high_water) {
   const int lane = threadIdx.x & 31;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   TrackCounters* C = S.C;
@@ -465,6 +467,7 @@ __global__ void __launch_bounds__(256) k_track(DevProblem P, TrackState S, NodeW
       } else {
         const unsigned j = ticket - (unsigned)X.n_init;
         bool ready = false, finished = false;
+        unsigned backoff = 8;
         while (true) {
           if (lane == 0) {
             const int tag = (j < (unsigned)S.queue_cap) ? ld_acquire_s32(&S.queue[j].x) : 0;
@@ -477,6 +480,7 @@ __global__ void __launch_bounds__(256) k_track(DevProblem P, TrackState S, NodeW
           ready = __shfl_sync(0xffffffffu, ready, 0);
           finished = __shfl_sync(0xffffffffu, finished, 0);
           if (ready || finished) break;
+          backoff = backoff < 256 ? backoff * 2 : 256;
           if (++idle > kSpinLimit) {
             if (lane == 0) {
               if (atomicOr(S.err, ERR_BARRIER) == 0) {        // first waiter to give up records its view
@@ -490,7 +494,7 @@ __global__ void __launch_bounds__(256) k_track(DevProblem P, TrackState S, NodeW
             finished = true;
             break;
           }
-          __nanosleep(20);
+          __nanosleep(backoff);
         }
         if (!ready) break;
         const int4 it = __ldcg(S.queue + j);
@@ -509,7 +513,7 @@ __global__ void __launch_bounds__(256) k_track(DevProblem P, TrackState S, NodeW
       if ((int)items > C->max_items) C->max_items = (int)items;
     }
     if (X.t > P.end_time && nLo == 0) { if (tid == 0) C->done = 1; break; }
-    if (ldcg_i(&C->rec_n) > high_water) { if (tid == 0) C->stop = 1; break; }
+    if (ldcg_i(S.rec_n) > high_water) { if (tid == 0) C->stop = 1; break; }
   }
   if (lane == 0 && pairs) atomicAdd(S.pairs, pairs);
 }
@@ -654,17 +658,17 @@ __device__ __forceinline__ double int_abs(double x) {
   return (double)(i < 0 ? -i : i);
 }
 
-__global__ void k_sol_latest(TrackState S, int nrec) {
+__global__ void k_sol_latest(TrackState S, const SolRec* rec, int nrec) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < nrec) atomicMax(&S.sol_step[S.rec[i].p], S.rec[i].step);
+  if (i < nrec) atomicMax(&S.sol_step[rec[i].p], rec[i].step);
 }
 
 // Solidification time by the reference's secant step, then gradient, Laplacian and source
 // sums at that time with the refined schedule, and the derived fields (src/Grid.cpp:316-548).
-__global__ void __launch_bounds__(128) k_solidify(DevProblem P, TrackState S, int nrec) {
+__global__ void __launch_bounds__(128) k_solidify(DevProblem P, TrackState S, const SolRec* rec, int nrec) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nrec) return;
-  const SolRec r = S.rec[i];
+  const SolRec r = rec[i];
   if (S.sol_step[r.p] != r.step) return;            // a later record of this point wins
   double x, y, z;
   point_xyz(P, r.p, x, y, z);
@@ -741,14 +745,14 @@ static cudaError_t launch_track_t(const DevProblem& P, const TrackState& S, cons
   int dev = 0, sms = 0, occ = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_track<PREC, SURF>, 256, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_track<PREC, SURF>, kTrackThreads, 0);
   const int blocks = sms * (occ < 1 ? occ : 1);
   if (blocks <= 0) return cudaErrorInvalidConfiguration;
   DevProblem Pc = P;
   TrackState Sc = S;
   NodeWindow Wc = w;
   void* args[] = {&Pc, &Sc, &Wc, &k_begin, &k_end, &hw};
-  return cudaLaunchCooperativeKernel((const void*)k_track<PREC, SURF>, dim3(blocks), dim3(256), args, 0, s);
+  return cudaLaunchCooperativeKernel((const void*)k_track<PREC, SURF>, dim3(blocks), dim3(kTrackThreads), args, 0, s);
 }
 
 cudaError_t th_launch_track(const DevProblem& P, const TrackState& S, const NodeWindow& w, int k_begin, int k_end,
@@ -768,11 +772,12 @@ void th_launch_notrack_step(const DevProblem& P, const TrackState& S, const Node
   k_notrack_finish<<<1, 1, 0, s>>>(P, S, w, k);
 }
 
-void th_launch_solidify(const DevProblem& P, const TrackState& S, int nrec, int precision, bool do_sol, cudaStream_t s) {
+void th_launch_solidify(const DevProblem& P, const TrackState& S, const SolRec* rec, int nrec, int precision,
+                        bool do_sol, cudaStream_t s) {
   (void)precision;
   if (nrec <= 0) return;
-  k_sol_latest<<<(nrec + 255) / 256, 256, 0, s>>>(S, nrec);
-  if (do_sol) k_solidify<<<(nrec + 127) / 128, 128, 0, s>>>(P, S, nrec);
+  k_sol_latest<<<(nrec + 255) / 256, 256, 0, s>>>(S, rec, nrec);
+  if (do_sol) k_solidify<<<(nrec + 127) / 128, 128, 0, s>>>(P, S, rec, nrec);
 }
 
 void th_launch_final_field(const DevProblem& P, const TrackState& S, int field, double* out, cudaStream_t s) {

@@ -31,7 +31,7 @@ struct QueueCounters {
 
 struct TrackCounters {
   int liq_n[3];     // liquid list lengths
-  int rec_n;        // solidification records queued
+  int rec_n[2];     // solidification records queued in each of the two record buffers
   int step;         // next step to run
   int done;         // finish test passed
   int stop;         // the loop stopped early (record queue high-water mark)
@@ -57,7 +57,8 @@ struct TrackState {
   int list_cap;
   int4* queue;             // work items {tag, type, point, aux}
   int queue_cap;
-  SolRec* rec;
+  SolRec* rec;             // the record buffer this launch appends to
+  int* rec_n;              // and its length (one of TrackCounters::rec_n)
   int rec_cap;
   TrackCounters* C;
   unsigned* bar;           // grid barrier: [0] arrivals, [1] generation
@@ -89,8 +90,9 @@ cudaError_t th_launch_track(const DevProblem& P, const TrackState& S, const Node
 void th_launch_notrack_step(const DevProblem& P, const TrackState& S, const NodeWindow& w, int k, int precision,
                             cudaStream_t s);
 
-// Solidification time, gradients and derived fields for the queued records.
-void th_launch_solidify(const DevProblem& P, const TrackState& S, int nrec, int precision, bool do_sol, cudaStream_t s);
+// Solidification time, gradients and derived fields for nrec records of `rec`.
+void th_launch_solidify(const DevProblem& P, const TrackState& S, const SolRec* rec, int nrec, int precision,
+                        bool do_sol, cudaStream_t s);
 
 // Final per-point field with the reference's liquid markers applied.
 void th_launch_final_field(const DevProblem& P, const TrackState& S, int field, double* out, cudaStream_t s);
