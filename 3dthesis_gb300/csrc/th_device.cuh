@@ -43,65 +43,113 @@ __device__ __forceinline__ void point_xyz(const DevProblem& P, int64_t p, double
   z = coord(P.gz, P.zmin, P.zmax, P.hz, k);
 }
 
-// One warp builds the whole node list at time t: beams in order, each beam's intervals in
-// walk order, the Gauss points of an interval spread over the lanes (lane l takes the
-// l-th point from the late end, the reference's emission order), kept nodes compacted
-// with a ballot.  Image copies for the boundary planes follow (src/Calc.cpp:584-605).
-__device__ __forceinline__ void gen_list_warp(const DevProblem& P, double t, bool is_sol, const NodeBufView& nb,
-                                              int* count, int* err) {
-  const int lane = threadIdx.x & 31;
-  const unsigned full = 0xffffffffu;
-  int n = 0;
-  int e = 0;
+// One thread block builds the whole node list at time t (the reference's GaussIntegrate
+// order: beams in order; per beam the zero-weight node at t, then the quadrature
+// intervals in walk order, each interval's Gauss points from the late end).  Thread 0
+// walks the path serially in exact FP64 (the interval schedule only needs a few FP64
+// operations per interval) and fills a shared-memory chunk of up to kChunkIntervals
+// intervals; then every thread builds candidate nodes of the chunk in parallel and a block
+// scan compacts the kept ones in order.  Image copies for the boundary planes follow
+// (src/Calc.cpp:584-605).  blockDim.x must be kGenThreads.
+constexpr int kGenThreads = 256;
+constexpr int kChunkIntervals = 256;
+
+struct GenShared {
+  double t1[kChunkIntervals], t2[kChunkIntervals];
+  int seg[kChunkIntervals], ord[kChunkIntervals], off[kChunkIntervals + 1];
+  int wsum[kGenThreads / 32];
+  int m, more, nout, err, kept;
+};
+
+__device__ __forceinline__ void gen_list_block(const DevProblem& P, double t, bool is_sol, const NodeBufView& nb,
+                                               int* count, int* err, GenShared& sh) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) { sh.nout = 0; sh.err = 0; }
+  __syncthreads();
   for (int b = 0; b < P.nbeams; ++b) {
     const DevBeam B = P.beam[b];
     const DevSeg* path = P.segs + B.seg_off;
     Walk W;
-    walk_begin(B, path, t, is_sol, W);
-    {
+    if (tid == 0) {
+      walk_begin(B, path, t, is_sol, W);
       NodeVal v;
-      const bool keep = instant_node(P, B, path, W, v);
-      if (keep) {
-        if (lane == 0 && n < nb.cap) store_node(nb, n, v);
-        ++n;
+      if (instant_node(P, B, path, W, v)) {
+        if (sh.nout < nb.cap) store_node(nb, sh.nout, v);
+        sh.nout++;
       }
     }
     int steps = 0;
-    while (W.more) {
-      if (++steps > kMaxWalkSteps) { e |= ERR_WALK_LIMIT; break; }
-      walk_interval(B, path, W);
-      const int base = W.order - 2;
-      NodeVal v;
-      bool keep = false;
-      if (lane < W.order) keep = gauss_node(P, B, path, W, base + W.order - 1 - lane, v);
-      const unsigned m = __ballot_sync(full, keep);
-      const int slot = n + __popc(m & ((1u << lane) - 1u));
-      if (keep && slot < nb.cap) store_node(nb, slot, v);
-      n += __popc(m);
-      walk_advance(W);
+    while (true) {
+      __syncthreads();
+      if (tid == 0) {                                  // next chunk of the interval schedule
+        int m = 0, off = 0;
+        while (W.more && m < kChunkIntervals) {
+          if (++steps > kMaxWalkSteps) { sh.err |= ERR_WALK_LIMIT; W.more = false; break; }
+          walk_interval(B, path, W);
+          sh.t1[m] = W.t1; sh.t2[m] = W.t2; sh.seg[m] = W.s; sh.ord[m] = W.order; sh.off[m] = off;
+          off += W.order;
+          ++m;
+          walk_advance(W);
+        }
+        sh.off[m] = off;
+        sh.m = m;
+        sh.more = W.more;
+      }
+      __syncthreads();
+      const int m = sh.m, total = sh.off[m];
+      for (int base = 0; base < total; base += kGenThreads) {
+        const int c = base + tid;
+        bool keep = false;
+        NodeVal v;
+        if (c < total) {
+          int lo = 0, hi = m - 1;                      // interval of candidate c
+          while (lo < hi) { const int mid = (lo + hi + 1) >> 1; if (sh.off[mid] <= c) lo = mid; else hi = mid - 1; }
+          const int order = sh.ord[lo], g = c - sh.off[lo];
+          Walk w;
+          w.t = t; w.t1 = sh.t1[lo]; w.t2 = sh.t2[lo]; w.s = sh.seg[lo];
+          keep = gauss_node(P, B, path, w, order - 2 + order - 1 - g, v);
+        }
+        const unsigned mk = __ballot_sync(0xffffffffu, keep);
+        if (lane == 0) sh.wsum[warp] = __popc(mk);
+        __syncthreads();
+        if (tid == 0) {
+          int acc = 0;
+          for (int i = 0; i < kGenThreads / 32; ++i) { const int x = sh.wsum[i]; sh.wsum[i] = acc; acc += x; }
+          sh.kept = acc;
+        }
+        __syncthreads();
+        const int slot = sh.nout + sh.wsum[warp] + __popc(mk & ((1u << lane) - 1u));
+        if (keep && slot < nb.cap) store_node(nb, slot, v);
+        __syncthreads();
+        if (tid == 0) sh.nout += sh.kept;
+        __syncthreads();
+      }
+      if (!sh.more) break;
     }
   }
-  const int n0 = n;
+  __syncthreads();
+  const int n0 = sh.nout;
+  int n = n0;
   if (P.n_images > 1) {
     if ((long long)n0 * P.n_images > nb.cap) {
-      e |= ERR_NODE_CAPACITY;
+      if (tid == 0) sh.err |= ERR_NODE_CAPACITY;
     } else {
-      __syncwarp();
-      for (int im = 1; im < P.n_images; ++im) {
-        for (int j = lane; j < n0; j += 32) {
-          NodeVal v;
-          v.x = image_coord(P.img[im][0], P.bcx0, P.bcx1, nb.x[j]);
-          v.y = image_coord(P.img[im][1], P.bcy0, P.bcy1, nb.y[j]);
-          v.z = image_coord(P.img[im][2], P.bcz0, P.bcz1, nb.z[j]);
-          v.ipx = nb.ipx[j]; v.ipy = nb.ipy[j]; v.ipz = nb.ipz[j]; v.dtau = nb.dtau[j]; v.amp = nb.amp[j];
-          store_node(nb, im * n0 + j, v);
-        }
+      for (int idx = tid; idx < n0 * (P.n_images - 1); idx += kGenThreads) {
+        const int im = 1 + idx / n0, j = idx % n0;
+        NodeVal v;
+        v.x = image_coord(P.img[im][0], P.bcx0, P.bcx1, nb.x[j]);
+        v.y = image_coord(P.img[im][1], P.bcy0, P.bcy1, nb.y[j]);
+        v.z = image_coord(P.img[im][2], P.bcz0, P.bcz1, nb.z[j]);
+        v.ipx = nb.ipx[j]; v.ipy = nb.ipy[j]; v.ipz = nb.ipz[j]; v.dtau = nb.dtau[j]; v.amp = nb.amp[j];
+        store_node(nb, im * n0 + j, v);
       }
     }
     n = n0 * P.n_images;
   }
-  if (n > nb.cap) e |= ERR_NODE_CAPACITY;
-  if (lane == 0) {
+  __syncthreads();
+  if (tid == 0) {
+    int e = sh.err;
+    if (n > nb.cap) e |= ERR_NODE_CAPACITY;
     *count = n;
     if (e) atomicOr(err, e);
   }

@@ -15,9 +15,10 @@ namespace {
 
 using namespace thdev;
 
-__global__ void __launch_bounds__(32) k_nodes_warp(DevProblem P, double t, int is_sol, NodeBufView nb, int* count,
-                                                   int* err) {
-  gen_list_warp(P, t, is_sol != 0, nb, count, err);
+__global__ void __launch_bounds__(kGenThreads) k_nodes_block(DevProblem P, double t, int is_sol, NodeBufView nb,
+                                                             int* count, int* err) {
+  __shared__ GenShared sh;
+  gen_list_block(P, t, is_sol != 0, nb, count, err, sh);
 }
 
 // ---------------------------------------------------------------- whole-grid sums
@@ -236,7 +237,7 @@ void launch_grid(const DevProblem& P, const NodeBufView& nb, const int* d_count,
 
 void th_launch_nodes(const DevProblem& P, double t, bool is_sol, const NodeBufView& nb, int* d_count, int* d_err,
                      cudaStream_t s) {
-  k_nodes_warp<<<1, 32, 0, s>>>(P, t, is_sol ? 1 : 0, nb, d_count, d_err);
+  k_nodes_block<<<1, kGenThreads, 0, s>>>(P, t, is_sol ? 1 : 0, nb, d_count, d_err);
 }
 
 bool th_tile_shape_supported(TileShape sh) {

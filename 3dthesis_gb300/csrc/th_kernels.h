@@ -17,8 +17,8 @@ struct NodeBufView {
 // consecutive k-points of one (i, j) column; KCH k-chunks per tile.
 struct TileShape { int kp, kch; };
 
-// Generates the node list at time t into nb with one warp; *d_count receives the
-// total, *d_err the error bits (capacity / walk limit).
+// Generates the node list at time t into nb with one thread block; *d_count receives
+// the total, *d_err the error bits (capacity / walk limit).
 void th_launch_nodes(const DevProblem& P, double t, bool is_sol, const NodeBufView& nb, int* d_count, int* d_err,
                      cudaStream_t s);
 

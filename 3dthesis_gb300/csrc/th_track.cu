@@ -36,12 +36,12 @@ __device__ __forceinline__ NodeBufView slot_view(const NodeWindow& w, int slot) 
 }
 
 // ------------------------------------------------------------------ node windows
-__global__ void __launch_bounds__(256) k_nodes_window(DevProblem P, NodeWindow w, int first, int n, int is_sol,
-                                                      int* err) {
-  const int slot = first + (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-  if (slot >= first + n) return;
+__global__ void __launch_bounds__(kGenThreads) k_nodes_window(DevProblem P, NodeWindow w, int first, int n, int is_sol,
+                                                              int* err) {
+  __shared__ GenShared sh;
+  const int slot = first + blockIdx.x;
   const NodeBufView nb = slot_view(w, slot);
-  gen_list_warp(P, w.t[slot], is_sol != 0, nb, &w.count[slot], err);
+  gen_list_block(P, w.t[slot], is_sol != 0, nb, &w.count[slot], err, sh);
 }
 
 // ------------------------------------------------------------------ warp evaluation
@@ -735,8 +735,7 @@ __global__ void k_final_field(DevProblem P, TrackState S, int f, double* out) {
 void th_launch_nodes_window(const DevProblem& P, const NodeWindow& w, int first_slot, int nslots, bool is_sol,
                             int* d_err, cudaStream_t s) {
   if (nslots <= 0) return;
-  const int blocks = (nslots + 7) / 8;
-  k_nodes_window<<<blocks, 256, 0, s>>>(P, w, first_slot, nslots, is_sol ? 1 : 0, d_err);
+  k_nodes_window<<<nslots, kGenThreads, 0, s>>>(P, w, first_slot, nslots, is_sol ? 1 : 0, d_err);
 }
 
 template <int PREC, bool SURF>
