@@ -21,7 +21,7 @@ from __future__ import annotations
 
 import ctypes
 import os
-from typing import Dict, Optional
+from typing import Dict, Optional, Sequence
 
 import numpy as np
 
@@ -40,7 +40,9 @@ FIELDS = ("T", "tSol", "G", "V", "Gx", "Gy", "Gz", "dTdt", "eqFrac", "numMelt", 
 EXPORTED = ("th_ctx_create_from_deck", "th_ctx_destroy", "th_last_error", "th_get_info", "th_snapshot_time",
             "th_nodes", "th_calc_T", "th_calc_T_device", "th_snapshot", "th_solidify", "th_field",
             "th_simulate", "th_pairs", "th_set_tile_shape", "th_last_kernel_ms", "th_sync",
-            "th_calc_T_noalloc", "th_run_stats", "th_run_reset")
+            "th_calc_T_noalloc", "th_run_stats", "th_run_reset", "th_autotune",
+            "th_batch_create", "th_batch_destroy", "th_batch_last_error", "th_batch_points", "th_batch_snapshot",
+            "th_batch_snapshot_device", "th_batch_set_tile_shape", "th_batch_autotune", "th_batch_pairs")
 
 
 class ThesisError(RuntimeError):
@@ -95,6 +97,18 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.th_pairs.argtypes = [vp, ctypes.POINTER(c_i64)]
     L.th_set_tile_shape.argtypes = [vp, c_int, c_int]
     L.th_last_kernel_ms.argtypes = [vp, ctypes.POINTER(ctypes.c_float)]
+    L.th_autotune.argtypes = [vp, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int)]
+    L.th_batch_create.argtypes = [ctypes.POINTER(ctypes.c_char_p), c_int, c_int, ctypes.POINTER(vp)]
+    L.th_batch_destroy.argtypes = [vp]
+    L.th_batch_destroy.restype = None
+    L.th_batch_last_error.argtypes = [vp]
+    L.th_batch_last_error.restype = ctypes.c_char_p
+    L.th_batch_points.argtypes = [vp, vp]
+    L.th_batch_snapshot.argtypes = [vp, c_int, vp]
+    L.th_batch_snapshot_device.argtypes = [vp, c_int, vp, vp]
+    L.th_batch_set_tile_shape.argtypes = [vp, c_int, c_int]
+    L.th_batch_autotune.argtypes = [vp, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int)]
+    L.th_batch_pairs.argtypes = [vp, ctypes.POINTER(c_i64)]
     _lib = L
     return L
 
@@ -233,4 +247,77 @@ class Simulation:
     def last_kernel_ms(self) -> float:
         v = ctypes.c_float()
         self._check(self._lib.th_last_kernel_ms(self._ctx, ctypes.byref(v)))
+        return v.value
+
+    def autotune(self, idx: int = 0):
+        """Times every tile shape on snapshot idx, keeps the fastest and returns it."""
+        kp, kch = ctypes.c_int32(), ctypes.c_int32()
+        self._check(self._lib.th_autotune(self._ctx, int(idx), ctypes.byref(kp), ctypes.byref(kch)))
+        return kp.value, kch.value
+
+
+class Batch:
+    """Many Snapshots decks evaluated together (a process-parameter sweep) on the current
+    CUDA device.  A batch snapshot returns one flat array; deck d's grid is
+    ``T[offsets[d]:offsets[d + 1]]`` in the deck's own point order."""
+
+    def __init__(self, param_inputs: Sequence[str], precision="fp32"):
+        self._lib = load_library()
+        self._b = ctypes.c_void_p()
+        names = [os.fspath(p).encode() for p in param_inputs]
+        arr = (ctypes.c_char_p * len(names))(*names)
+        st = self._lib.th_batch_create(arr, len(names), _PRECISIONS[precision], ctypes.byref(self._b))
+        if st != 0:
+            raise ThesisError(st, self._lib.th_batch_last_error(None).decode())
+        self.n = len(names)
+        self.offsets = np.zeros(self.n + 1, dtype=np.int64)
+        self._check(self._lib.th_batch_points(self._b, _ptr(self.offsets)))
+
+    def _check(self, st: int):
+        if st != 0:
+            raise ThesisError(st, self._lib.th_batch_last_error(self._b).decode())
+
+    def close(self):
+        if self._b:
+            self._lib.th_batch_destroy(self._b)
+            self._b = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def pnum(self) -> int:
+        return int(self.offsets[-1])
+
+    def snapshot(self, idx: int, out: Optional[np.ndarray] = None) -> np.ndarray:
+        if out is None:
+            out = np.empty(self.pnum)
+        self._check(self._lib.th_batch_snapshot(self._b, int(idx), _ptr(out)))
+        return out
+
+    def snapshot_device(self, idx: int, d_T: int, stream: int = 0):
+        self._check(self._lib.th_batch_snapshot_device(self._b, int(idx), ctypes.c_void_p(d_T),
+                                                       ctypes.c_void_p(stream or None)))
+
+    def set_tile_shape(self, kp: int, kch: int):
+        self._check(self._lib.th_batch_set_tile_shape(self._b, int(kp), int(kch)))
+
+    def autotune(self, idx: int = 0):
+        kp, kch = ctypes.c_int32(), ctypes.c_int32()
+        self._check(self._lib.th_batch_autotune(self._b, int(idx), ctypes.byref(kp), ctypes.byref(kch)))
+        return kp.value, kch.value
+
+    @property
+    def pairs(self) -> int:
+        v = ctypes.c_int64()
+        self._check(self._lib.th_batch_pairs(self._b, ctypes.byref(v)))
         return v.value

@@ -321,8 +321,43 @@ th_status th_last_kernel_ms(th_ctx* ctx, float* out) {
   return TH_OK;
 }
 
-// Tile shape of the whole-grid kernels (k-points per thread, k-chunks per tile); the
-// tuner in the Python layer picks one per deck.
+// Times the whole-grid kernel of snapshot idx with every supported tile shape (the node
+// list is generated once; four launches per shape, the first dropped, the best kept) and
+// keeps the fastest shape for the context.
+th_status th_autotune(th_ctx* ctx, int32_t idx, int32_t* kp_out, int32_t* kch_out) {
+  if (!ctx) return th_fail(ctx, TH_ERR_INVALID, "null context");
+  if (ctx->hp.mode != 0 || idx < 0 || idx >= (int32_t)ctx->hp.snaps.size())
+    return th_fail(ctx, TH_ERR_INVALID, "no such snapshot");
+  TH_CUDA(ctx, cudaSetDevice(ctx->device));
+  th_status st = th_gen_nodes_checked(ctx, ctx->hp.snaps[idx], false);
+  if (st != TH_OK) return st;
+  st = th_ensure(ctx, (void**)&ctx->d_T, &ctx->T_bytes, (size_t)ctx->hp.pnum * sizeof(double));
+  if (st != TH_OK) return st;
+  const TileShape shapes[7] = {{4, 2}, {4, 1}, {4, 4}, {2, 2}, {2, 4}, {8, 1}, {8, 2}};
+  float best = 1e30f;
+  TileShape best_shape = ctx->shape;
+  for (const TileShape& sh : shapes) {
+    float t_best = 1e30f;
+    for (int rep = 0; rep < 4; ++rep) {
+      TH_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+      th_launch_grid_sum(ctx->dp, ctx->nb, ctx->d_small, ctx->d_T, ctx->precision, sh, ctx->d_pairs, ctx->stream);
+      TH_CUDA(ctx, cudaGetLastError());
+      TH_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+      TH_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+      if (rep > 0) t_best = std::min(t_best, ms);
+    }
+    if (t_best < best) { best = t_best; best_shape = sh; }
+  }
+  ctx->shape = best_shape;
+  ctx->T_valid = false;
+  if (kp_out) *kp_out = best_shape.kp;
+  if (kch_out) *kch_out = best_shape.kch;
+  return TH_OK;
+}
+
+// Tile shape of the whole-grid kernels (k-points per thread, k-chunks per tile).
 th_status th_set_tile_shape(th_ctx* ctx, int32_t kp, int32_t kch) {
   if (!ctx) return th_fail(ctx, TH_ERR_INVALID, "null context");
   TileShape sh{kp, kch};

@@ -1,0 +1,315 @@
+// Batched snapshots: many independent decks (process-parameter sweeps) evaluated together.
+//
+// Every deck keeps its own path, material, beam and grid (uneven point and node counts);
+// the device holds one array of deck descriptions, one node arena and one output arena.
+// A snapshot of the whole batch is two launches - node lists (one block per deck) and a
+// persistent work-list grid over every deck's tiles - captured once into a CUDA graph per
+// (snapshot index, output buffer, tile shape) and replayed.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/thesis_gb300.h"
+#include "th_kernels.h"
+#include "th_problem.h"
+
+struct th_batch {
+  int n = 0;
+  int precision = TH_FP32_KAHAN;
+  int device = -1;
+  cudaStream_t stream = nullptr;
+  std::vector<HostProblem> hp;
+  std::vector<DevProblem> dp;
+  std::vector<long long> pnum_off;     // n + 1
+  int n_snap = 0;                       // snapshots common to every deck
+  TileShape shape{4, 2};
+  std::string err;
+  // device
+  DevSeg* d_segs = nullptr;
+  DevProblem* d_probs = nullptr;
+  NodeBufView* d_views = nullptr;
+  void* node_mem = nullptr;
+  int* d_counts = nullptr;
+  int* d_err = nullptr;
+  int* d_ticket = nullptr;
+  int* d_tile_off = nullptr;
+  long long* d_pnum_off = nullptr;
+  double* d_times = nullptr;           // n_snap x n
+  double* d_T = nullptr;               // output arena for the host-buffer call
+  unsigned long long* d_pairs = nullptr;
+  std::map<std::tuple<int, double*, int, int>, cudaGraphExec_t> graphs;
+};
+
+namespace {
+
+std::string g_batch_error;
+
+th_status fail(th_batch* b, th_status code, const std::string& m) {
+  if (b) b->err = m; else g_batch_error = m;
+  return code;
+}
+
+th_status cuda(th_batch* b, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return TH_OK;
+  return fail(b, TH_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define BCUDA(b, call)                                          \
+  do {                                                          \
+    th_status st_ = cuda((b), (call), #call);                   \
+    if (st_ != TH_OK) return st_;                               \
+  } while (0)
+
+// (Re)allocates the node arena for the given per-deck capacities and uploads the views.
+th_status layout_nodes(th_batch* b, const std::vector<int>& caps) {
+  const size_t per = 8 * sizeof(double) + 10 * sizeof(float);
+  size_t total = 0;
+  for (int c : caps) total += (size_t)c;
+  if (b->node_mem) cudaFree(b->node_mem);
+  b->node_mem = nullptr;
+  BCUDA(b, cudaMalloc(&b->node_mem, total * per));
+  std::vector<NodeBufView> views(b->n);
+  char* base = (char*)b->node_mem;
+  for (int d = 0; d < b->n; ++d) {
+    const size_t cap = caps[d];
+    double* dd = (double*)base;
+    float* f = (float*)(dd + 8 * cap);
+    NodeBufView& v = views[d];
+    v.cap = (int)cap;
+    v.x = dd; v.y = dd + cap; v.z = dd + 2 * cap; v.ipx = dd + 3 * cap; v.ipy = dd + 4 * cap; v.ipz = dd + 5 * cap;
+    v.dtau = dd + 6 * cap; v.amp = dd + 7 * cap;
+    v.kx = f; v.ky = f + cap; v.kz = f + 2 * cap; v.w = f + 3 * cap; v.xh = f + 4 * cap; v.xl = f + 5 * cap;
+    v.yh = f + 6 * cap; v.yl = f + 7 * cap; v.zh = f + 8 * cap; v.zl = f + 9 * cap;
+    base += cap * per;
+  }
+  BCUDA(b, cudaMemcpy(b->d_views, views.data(), b->n * sizeof(NodeBufView), cudaMemcpyHostToDevice));
+  return TH_OK;
+}
+
+// Builds (or reuses) the graph that fills d_T with snapshot idx of every deck.
+th_status graph_for(th_batch* b, int idx, double* d_T, cudaGraphExec_t* out) {
+  const auto key = std::make_tuple(idx, d_T, b->shape.kp, b->shape.kch);
+  auto it = b->graphs.find(key);
+  if (it != b->graphs.end()) { *out = it->second; return TH_OK; }
+  std::vector<int> tile_off(b->n + 1, 0);
+  for (int d = 0; d < b->n; ++d) tile_off[d + 1] = tile_off[d] + th_tile_count(b->dp[d], b->shape);
+  BCUDA(b, cudaMemcpy(b->d_tile_off, tile_off.data(), tile_off.size() * sizeof(int), cudaMemcpyHostToDevice));
+  cudaGraph_t g = nullptr;
+  BCUDA(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  cudaMemsetAsync(b->d_ticket, 0, sizeof(int), b->stream);
+  th_launch_batch_nodes(b->n, b->d_probs, b->d_views, b->d_times + (size_t)idx * b->n, b->d_counts, b->d_err, b->stream);
+  th_launch_batch_grid(b->shape, b->precision, b->d_probs, b->d_views, b->d_counts, d_T, b->d_pnum_off, b->d_tile_off,
+                       b->n, b->d_ticket, b->d_pairs, b->stream);
+  BCUDA(b, cudaStreamEndCapture(b->stream, &g));
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
+  cudaGraphDestroy(g);
+  BCUDA(b, e);
+  b->graphs[key] = exec;
+  *out = exec;
+  return TH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+th_status th_batch_create(const char* const* param_inputs, int32_t n, int32_t precision, th_batch** out) {
+  if (!param_inputs || n <= 0 || !out) return fail(nullptr, TH_ERR_INVALID, "bad argument");
+  if (precision != TH_FP64 && precision != TH_FP32_KAHAN) return fail(nullptr, TH_ERR_INVALID, "unknown precision");
+  *out = nullptr;
+  th_batch* b = new th_batch();
+  b->n = n;
+  b->precision = precision;
+  b->hp.resize(n);
+  for (int d = 0; d < n; ++d) {
+    std::string e;
+    if (!th_load_deck(param_inputs[d], b->hp[d], e)) {
+      g_batch_error = std::string("deck ") + std::to_string(d) + ": " + e;
+      delete b;
+      return TH_ERR_INVALID;
+    }
+    if (b->hp[d].mode != 0) {
+      g_batch_error = std::string("deck ") + std::to_string(d) + " is not a Snapshots deck";
+      delete b;
+      return TH_ERR_INVALID;
+    }
+  }
+  b->n_snap = INT32_MAX;
+  for (const HostProblem& h : b->hp) b->n_snap = std::min<int>(b->n_snap, (int)h.snaps.size());
+  auto bail = [&](th_status st) { g_batch_error = b->err; th_batch_destroy(b); return st; };
+  if (cudaGetDevice(&b->device) != cudaSuccess) { b->err = "no CUDA device"; return bail(TH_ERR_CUDA); }
+  if (cuda(b, cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "stream") != TH_OK) return bail(TH_ERR_CUDA);
+  // segments of every deck in one array; deck descriptions point into it
+  std::vector<DevSeg> segs;
+  std::vector<size_t> seg_off(n);
+  for (int d = 0; d < n; ++d) {
+    seg_off[d] = segs.size();
+    const std::vector<DevSeg> s = th_pack_segments(b->hp[d]);
+    segs.insert(segs.end(), s.begin(), s.end());
+  }
+  if (cuda(b, cudaMalloc(&b->d_segs, segs.size() * sizeof(DevSeg)), "cudaMalloc") != TH_OK) return bail(TH_ERR_CUDA);
+  if (cuda(b, cudaMemcpy(b->d_segs, segs.data(), segs.size() * sizeof(DevSeg), cudaMemcpyHostToDevice), "copy") != TH_OK)
+    return bail(TH_ERR_CUDA);
+  b->dp.resize(n);
+  std::vector<int> caps(n);
+  b->pnum_off.assign(n + 1, 0);
+  for (int d = 0; d < n; ++d) {
+    th_make_dev_problem(b->hp[d], b->d_segs + seg_off[d], b->dp[d]);
+    if (b->dp[d].n_images > TH_MAX_IMAGES) { b->err = "too many boundary images"; return bail(TH_ERR_CAPACITY); }
+    const size_t nseg = (d + 1 < n ? seg_off[d + 1] : segs.size()) - seg_off[d];
+    caps[d] = (int)std::min<size_t>((64 * nseg + 4096) * (size_t)b->dp[d].n_images, 1 << 22);
+    b->pnum_off[d + 1] = b->pnum_off[d] + b->hp[d].pnum;
+  }
+  std::vector<double> times((size_t)std::max(b->n_snap, 1) * n, 0.0);
+  for (int i = 0; i < b->n_snap; ++i)
+    for (int d = 0; d < n; ++d) times[(size_t)i * n + d] = b->hp[d].snaps[i];
+  if (cuda(b, cudaMalloc(&b->d_probs, n * sizeof(DevProblem)), "cudaMalloc") != TH_OK ||
+      cuda(b, cudaMalloc(&b->d_views, n * sizeof(NodeBufView)), "cudaMalloc") != TH_OK ||
+      cuda(b, cudaMalloc(&b->d_counts, n * sizeof(int)), "cudaMalloc") != TH_OK ||
+      cuda(b, cudaMalloc(&b->d_err, sizeof(int)), "cudaMalloc") != TH_OK ||
+      cuda(b, cudaMalloc(&b->d_ticket, sizeof(int)), "cudaMalloc") != TH_OK ||
+      cuda(b, cudaMalloc(&b->d_tile_off, (n + 1) * sizeof(int)), "cudaMalloc") != TH_OK ||
+      cuda(b, cudaMalloc(&b->d_pnum_off, (n + 1) * sizeof(long long)), "cudaMalloc") != TH_OK ||
+      cuda(b, cudaMalloc(&b->d_times, times.size() * sizeof(double)), "cudaMalloc") != TH_OK ||
+      cuda(b, cudaMalloc(&b->d_pairs, sizeof(unsigned long long)), "cudaMalloc") != TH_OK)
+    return bail(TH_ERR_CUDA);
+  cudaMemcpy(b->d_probs, b->dp.data(), n * sizeof(DevProblem), cudaMemcpyHostToDevice);
+  cudaMemcpy(b->d_pnum_off, b->pnum_off.data(), (n + 1) * sizeof(long long), cudaMemcpyHostToDevice);
+  cudaMemcpy(b->d_times, times.data(), times.size() * sizeof(double), cudaMemcpyHostToDevice);
+  cudaMemset(b->d_err, 0, sizeof(int));
+  cudaMemset(b->d_pairs, 0, sizeof(unsigned long long));
+  if (cuda(b, cudaDeviceSynchronize(), "batch set-up") != TH_OK) return bail(TH_ERR_CUDA);
+  // Size every deck's node buffer for its largest snapshot: generate each snapshot's lists
+  // once and grow the buffers that overflowed, so a captured snapshot never runs out.
+  for (int attempt = 0;; ++attempt) {
+    if (layout_nodes(b, caps) != TH_OK) return bail(TH_ERR_CUDA);
+    std::vector<int> need(caps);
+    bool grew = false;
+    std::vector<int> cnt(n);
+    for (int i = 0; i < b->n_snap; ++i) {
+      int err = 0;
+      th_launch_batch_nodes(n, b->d_probs, b->d_views, b->d_times + (size_t)i * n, b->d_counts, b->d_err, b->stream);
+      if (cuda(b, cudaMemcpyAsync(cnt.data(), b->d_counts, n * sizeof(int), cudaMemcpyDeviceToHost, b->stream), "count")
+              != TH_OK ||
+          cuda(b, cudaMemcpyAsync(&err, b->d_err, sizeof(int), cudaMemcpyDeviceToHost, b->stream), "count") != TH_OK ||
+          cuda(b, cudaStreamSynchronize(b->stream), "node sizing") != TH_OK)
+        return bail(TH_ERR_CUDA);
+      if (err & 2) { b->err = "quadrature walk exceeded its step limit"; return bail(TH_ERR_TIMEOUT); }
+      for (int d = 0; d < n; ++d)
+        if (cnt[d] > need[d]) { need[d] = cnt[d] + 1024; grew = true; }
+    }
+    cudaMemset(b->d_err, 0, sizeof(int));
+    if (!grew) break;
+    if (attempt == 2) { b->err = "node buffer growth did not converge"; return bail(TH_ERR_CAPACITY); }
+    for (int d = 0; d < n; ++d)
+      if (need[d] > (1 << 26)) { b->err = "node list larger than 2^26 nodes"; return bail(TH_ERR_CAPACITY); }
+    caps = need;
+  }
+  *out = b;
+  return TH_OK;
+}
+
+void th_batch_destroy(th_batch* b) {
+  if (!b) return;
+  if (b->device >= 0) cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
+  cudaFree(b->d_segs); cudaFree(b->d_probs); cudaFree(b->d_views); cudaFree(b->node_mem); cudaFree(b->d_counts);
+  cudaFree(b->d_err); cudaFree(b->d_ticket); cudaFree(b->d_tile_off); cudaFree(b->d_pnum_off); cudaFree(b->d_times);
+  cudaFree(b->d_T); cudaFree(b->d_pairs);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+const char* th_batch_last_error(const th_batch* b) { return b ? b->err.c_str() : g_batch_error.c_str(); }
+
+th_status th_batch_points(th_batch* b, int64_t* offsets) {
+  if (!b || !offsets) return fail(b, TH_ERR_INVALID, "null argument");
+  for (int d = 0; d <= b->n; ++d) offsets[d] = b->pnum_off[d];
+  return TH_OK;
+}
+
+th_status th_batch_set_tile_shape(th_batch* b, int32_t kp, int32_t kch) {
+  if (!b) return fail(b, TH_ERR_INVALID, "null batch");
+  if (!th_tile_shape_supported(TileShape{kp, kch})) return fail(b, TH_ERR_INVALID, "unsupported tile shape");
+  b->shape = TileShape{kp, kch};
+  return TH_OK;
+}
+
+th_status th_batch_snapshot_device(th_batch* b, int32_t idx, double* d_T, void* stream) {
+  if (!b || !d_T) return fail(b, TH_ERR_INVALID, "null argument");
+  if (idx < 0 || idx >= b->n_snap) return fail(b, TH_ERR_INVALID, "snapshot index not present in every deck");
+  BCUDA(b, cudaSetDevice(b->device));
+  cudaGraphExec_t g = nullptr;
+  th_status st = graph_for(b, idx, d_T, &g);
+  if (st != TH_OK) return st;
+  BCUDA(b, cudaGraphLaunch(g, stream ? (cudaStream_t)stream : b->stream));
+  return TH_OK;
+}
+
+th_status th_batch_snapshot(th_batch* b, int32_t idx, double* T_out) {
+  if (!b) return fail(b, TH_ERR_INVALID, "null batch");
+  BCUDA(b, cudaSetDevice(b->device));
+  if (!b->d_T) BCUDA(b, cudaMalloc(&b->d_T, std::max<long long>(b->pnum_off[b->n], 1) * sizeof(double)));
+  th_status st = th_batch_snapshot_device(b, idx, b->d_T, b->stream);
+  if (st != TH_OK) return st;
+  if (T_out)
+    BCUDA(b, cudaMemcpyAsync(T_out, b->d_T, b->pnum_off[b->n] * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  int err = 0;
+  BCUDA(b, cudaMemcpyAsync(&err, b->d_err, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  BCUDA(b, cudaStreamSynchronize(b->stream));
+  if (err & 2) return fail(b, TH_ERR_TIMEOUT, "quadrature walk exceeded its step limit");
+  if (err & 1) return fail(b, TH_ERR_CAPACITY, "a deck's node list outgrew its buffer");
+  return TH_OK;
+}
+
+th_status th_batch_pairs(th_batch* b, int64_t* out) {
+  if (!b || !out) return fail(b, TH_ERR_INVALID, "null argument");
+  unsigned long long v = 0;
+  BCUDA(b, cudaMemcpy(&v, b->d_pairs, sizeof(v), cudaMemcpyDeviceToHost));
+  *out = (int64_t)v;
+  return TH_OK;
+}
+
+// Times every supported tile shape on snapshot idx (three graph replays each, best kept)
+// and keeps the fastest for the batch.
+th_status th_batch_autotune(th_batch* b, int32_t idx, int32_t* kp_out, int32_t* kch_out) {
+  if (!b) return fail(b, TH_ERR_INVALID, "null batch");
+  BCUDA(b, cudaSetDevice(b->device));
+  if (!b->d_T) BCUDA(b, cudaMalloc(&b->d_T, std::max<long long>(b->pnum_off[b->n], 1) * sizeof(double)));
+  const TileShape shapes[7] = {{4, 2}, {4, 1}, {4, 4}, {2, 2}, {2, 4}, {8, 1}, {8, 2}};
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  TileShape best_shape = b->shape;
+  for (const TileShape& sh : shapes) {
+    b->shape = sh;
+    float t_best = 1e30f;
+    for (int rep = 0; rep < 4; ++rep) {
+      cudaEventRecord(e0, b->stream);
+      th_status st = th_batch_snapshot_device(b, idx, b->d_T, b->stream);
+      if (st != TH_OK) { cudaEventDestroy(e0); cudaEventDestroy(e1); return st; }
+      cudaEventRecord(e1, b->stream);
+      cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep > 0) t_best = std::min(t_best, ms);      // the first replay includes graph set-up
+    }
+    if (t_best < best) { best = t_best; best_shape = sh; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  b->shape = best_shape;
+  if (kp_out) *kp_out = best_shape.kp;
+  if (kch_out) *kch_out = best_shape.kch;
+  return TH_OK;
+}
+
+}  // extern "C"

@@ -53,8 +53,10 @@ __device__ __forceinline__ void point_xyz(const DevProblem& P, int64_t p, double
 // (src/Calc.cpp:584-605).  blockDim.x must be kGenThreads.
 constexpr int kGenThreads = 256;
 constexpr int kChunkIntervals = 256;
+constexpr int kSegCache = 320;        // path segments staged in shared memory per beam
 
 struct GenShared {
+  DevSeg seg_cache[kSegCache];
   double t1[kChunkIntervals], t2[kChunkIntervals];
   int seg[kChunkIntervals], ord[kChunkIntervals], off[kChunkIntervals + 1];
   int wsum[kGenThreads / 32];
@@ -69,6 +71,12 @@ __device__ __forceinline__ void gen_list_block(const DevProblem& P, double t, bo
   for (int b = 0; b < P.nbeams; ++b) {
     const DevBeam B = P.beam[b];
     const DevSeg* path = P.segs + B.seg_off;
+    if (B.nseg <= kSegCache) {                         // the walk touches every segment: stage them
+      __syncthreads();
+      for (int i = tid; i < B.nseg; i += kGenThreads) sh.seg_cache[i] = path[i];
+      __syncthreads();
+      path = sh.seg_cache;
+    }
     Walk W;
     if (tid == 0) {
       walk_begin(B, path, t, is_sol, W);

@@ -34,3 +34,14 @@ void th_launch_list_sum(const DevProblem& P, const NodeBufView& nb, const int* d
 void th_launch_nodes_export(const NodeBufView& nb, const int* d_count, double* d_out, int cap, cudaStream_t s);
 
 bool th_tile_shape_supported(TileShape shape);
+
+// Tiles of one deck's grid for a tile shape.
+int th_tile_count(const DevProblem& P, TileShape shape);
+
+// Batched decks: node lists (one block per deck), then one persistent work-list grid over
+// every deck's tiles (tile_off: exclusive prefix of tile counts, ndeck + 1 entries).
+void th_launch_batch_nodes(int ndeck, const DevProblem* probs, const NodeBufView* views, const double* times,
+                           int* counts, int* err, cudaStream_t s);
+void th_launch_batch_grid(TileShape shape, int precision, const DevProblem* probs, const NodeBufView* views,
+                          const int* counts, double* T, const long long* pnum_off, const int* tile_off, int ndeck,
+                          int* ticket, unsigned long long* pairs, cudaStream_t s);

@@ -53,10 +53,7 @@ __device__ __forceinline__ BeamLoc beam_loc(const DevProblem& P, const DevSeg* p
 __device__ __forceinline__ double ref_time(const DevBeam& B, const DevSeg* path, double tpp, int s) {
   double spp = rn_div(tpp, B.nond);
   spp = (spp < 0.0) ? 0.0 : spp;
-  if (path[s].mode == 0) {
-    const double t0 = rn_div(rn_mul(0.58870501125, B.ax), path[s].prm);
-    return rn_mul(t0, rn_sqrt(rn_add(rn_mul(12.0, spp), 1.0)));
-  }
+  if (path[s].mode == 0) return rn_mul(path[s].rt0, rn_sqrt(rn_add(rn_mul(12.0, spp), 1.0)));
   double r = rn_sub(path[s].tend, path[s - 1].tend);
   if (r == 0) r = 1.0e-9;
   return r;

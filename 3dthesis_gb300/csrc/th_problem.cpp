@@ -106,12 +106,12 @@ bool read_path_file(const std::string& file, std::vector<DevSeg>& path, std::str
   std::ifstream in(file.c_str());
   if (!in.is_open()) { err = "cannot open path file " + file; return false; }
   path.clear();
-  DevSeg origin{0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 1, 0};
+  DevSeg origin{0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 1, 0};
   path.push_back(origin);
   std::string line;
   std::getline(in, line);                       // header
   while (true) {
-    DevSeg s{0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 1, 0};
+    DevSeg s{0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 1, 0};
     if (!(in >> s.mode >> s.x >> s.y >> s.z >> s.q >> s.prm)) break;
     s.x *= 1e-3; s.y *= 1e-3; s.z *= 1e-3;
     path.push_back(s);
@@ -352,7 +352,12 @@ bool th_load_deck(const std::string& param_input, HostProblem& hp, std::string& 
 
 std::vector<DevSeg> th_pack_segments(const HostProblem& hp) {
   std::vector<DevSeg> all;
-  for (const auto& p : hp.paths) all.insert(all.end(), p.begin(), p.end());
+  for (size_t b = 0; b < hp.paths.size(); ++b)
+    for (DevSeg s : hp.paths[b]) {
+      // the line-mode step scale of Util::GetRefTime (src/Util.cpp:199), same operations
+      s.rt0 = (s.mode == 0) ? 0.58870501125 * hp.beams[b].ax / s.prm : 0.0;
+      all.push_back(s);
+    }
   return all;
 }
 

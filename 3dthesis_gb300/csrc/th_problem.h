@@ -16,6 +16,7 @@ enum { TH_TRACK_NONE = 0, TH_TRACK_VOLUME = 1, TH_TRACK_SURFACE = 2 };
 // end time.  mode 0 = line, 1 = spot.
 struct DevSeg {
   double x, y, z, q, prm, tend;
+  double rt0;               // line segments: 0.58870501125 * ax / speed of the beam that scans it
   int32_t mode, pad;
 };
 

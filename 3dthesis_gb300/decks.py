@@ -338,3 +338,32 @@ def small_spots() -> Deck:
         paths=[spot_raster_path(4, 3, 0.1, 2e-4)],
         axes=(AxisSpec(-0.1e-3, 0.4e-3, num=26), AxisSpec(-0.1e-3, 0.3e-3, num=21), AxisSpec(-0.05e-3, 0.0, num=6)),
         scan_fracs=[30, 70, 100], tracking="None")
+
+
+def small_sweep(n: int = 10, seed: int = 3) -> List[Deck]:
+    """Small uneven snapshot sweep: seeded power, speed, widths and track counts, grids
+    from 8x8x3 to 40x30x10 points, snapshots at 50 % and 100 %; deck 1 scans spots and
+    deck 2 carries two beams and deck 3 has reflecting boundaries, so node counts differ
+    by deck."""
+    rng = random.Random(seed)
+    decks = []
+    for k in range(n):
+        nx, ny, nz = rng.randint(8, 40), rng.randint(8, 30), rng.randint(3, 10)
+        w = rng.uniform(40e-6, 100e-6)
+        beams = [BeamSpec(width_x=w, width_y=rng.uniform(40e-6, 100e-6), power=rng.uniform(100, 400))]
+        paths = [raster_path(rng.randint(1, 4), 0.3, 0.05, rng.uniform(0.5, 2.0))]
+        if k == 1:
+            paths = [spot_raster_path(3, 2, 0.08, 1e-4)]
+        if k == 2:
+            beams.append(BeamSpec(width_x=60e-6, width_y=50e-6, power=200))
+            paths.append(raster_path(2, 0.25, 0.06, 1.2))
+        bcs = None
+        if k == 3:
+            bcs = {"X_min": -0.1e-3, "X_max": 0.45e-3, "Y_min": -0.08e-3, "Z_min": -0.2e-3, "Reflections": 2}
+        decks.append(Deck(
+            name=f"small_sweep{k:02d}", mode="Snapshots", beams=beams, paths=paths,
+            axes=(AxisSpec(-0.05e-3, -0.05e-3 + (nx - 1) * 1e-5, num=nx),
+                  AxisSpec(-0.05e-3, -0.05e-3 + (ny - 1) * 1e-5, num=ny),
+                  AxisSpec(-(nz - 1) * 1e-5, 0.0, num=nz)),
+            scan_fracs=[50, 100], tracking="None", bcs=bcs))
+    return decks

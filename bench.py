@@ -1,7 +1,8 @@
 """Benchmark of the 3DThesis hot path on GB300: point x node pairs per second.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload surface_serpentine|snapshot_raster] [--precision fp32|fp64]
+                    [--workload surface_serpentine|snapshot_raster|snapshot_sweep]
+                    [--precision fp32|fp64] [--tile KPxKCH]
 
 Workloads (synthetic decks in the reference's own input format, 3dthesis_gb300/decks.py):
   surface_serpentine (default; the metric's configuration) - Solidification mode, Surface
@@ -10,6 +11,8 @@ Workloads (synthetic decks in the reference's own input format, 3dthesis_gb300/d
       (31,769 timesteps to the finish test) from t = 0.
   snapshot_raster - Snapshots mode: 10 x 2 mm raster on a 200x100x40 grid, snapshots at
       25/50/100 %.  One step = the three snapshots.
+  snapshot_sweep - 256 independent Snapshots decks of uneven sizes (a process-parameter
+      sweep) evaluated as one batch: one step = one CUDA-graph replay of the batch snapshot.
 
 ``value`` = point x node pairs of the step / the step's time with the deck resident in HBM
 (inputs on the device before timing; L2 flushed with a 256 MiB write before each step,
@@ -51,6 +54,9 @@ DECK_TEXT = {
                           "eta=0.35, 50/50/1 um; grid 500x500x100 at 10 um; dt=1e-5 s; outputs tSol,G,V,dTdt",
     "snapshot_raster": "Snapshots; 10 tracks x 2 mm, hatch 0.1 mm, 1.0 m/s, P=200 W, eta=0.35, 50/50/1 um; "
                        "grid 200x100x40 at 10 um; snapshots at 25/50/100 %",
+    "snapshot_sweep": "256 independent Snapshots decks (seed 0): P~U(100,400) W, v~U(0.5,2) m/s, "
+                      "width~U(40,120) um, U{1..30} x 2 mm tracks, grids U{50..400}^2 x U{10..60} at 10 um, "
+                      "snapshot at 100 %",
 }
 
 
@@ -114,6 +120,8 @@ class ClockSampler:
 def make_deck(name: str, tmp: str):
     decks = importlib.import_module("3dthesis_gb300.decks")
     deck = getattr(decks, name)()
+    if isinstance(deck, list):
+        return deck, [d.write(os.path.join(tmp, name, d.name)) for d in deck]
     return deck, deck.write(os.path.join(tmp, name))
 
 
@@ -178,7 +186,7 @@ def run_solidification(args, th, torch, dev, path, deck, world):
         e2e_t.append(time.perf_counter() - t0)
     e2e_s = allreduce_max(statistics.median(e2e_t), world)
     e2e = {"value": pairs * world / e2e_s, "unit": "pairs/s",
-           "h2d_bytes_per_step": int(sum(len(p) for p in deck.paths) * 56 + 8 * st["steps"]),
+           "h2d_bytes_per_step": int(sum(len(p) for p in deck.paths) * 64 + 8 * st["steps"]),
            "d2h_bytes_per_step": int(8 * sim.pnum * len(outs)),
            "ms_per_step": 1e3 * e2e_s,
            "includes": "deck parse + context creation + the whole run + D2H of " + ",".join(outs)}
@@ -268,7 +276,7 @@ def run_snapshot(args, th, torch, dev, path, deck, world):
         e2e_t.append(time.perf_counter() - t0)
     e2e_s = allreduce_max(statistics.median(e2e_t), world)
     e2e = {"value": pairs_per_step * world / e2e_s, "unit": "pairs/s",
-           "h2d_bytes_per_step": int(sum(len(p) for p in deck.paths) * 56),
+           "h2d_bytes_per_step": int(sum(len(p) for p in deck.paths) * 64),
            "d2h_bytes_per_step": int(8 * pnum * len(times)), "ms_per_step": 1e3 * e2e_s,
            "includes": "deck parse + context creation + per-snapshot D2H of T into pinned memory"}
     pk, src = peaks()
@@ -291,6 +299,81 @@ def run_snapshot(args, th, torch, dev, path, deck, world):
                        "node_gen_ms": statistics.median(gen_ms)}}
 
 
+# ------------------------------------------------------------------ batched sweep workload
+def run_sweep(args, th, torch, dev, paths, deck, world):
+    """One step = the 100 % snapshot of all 256 decks: one graph replay (node lists for
+    every deck, then the work-list kernel over every deck's tiles)."""
+    b = th.Batch(paths, args.precision)
+    if args.tile:
+        b.set_tile_shape(*[int(v) for v in args.tile.split("x")])
+    else:
+        b.autotune(0)
+    pnum = b.pnum
+    d_T = torch.empty(pnum, dtype=torch.float64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    p0 = b.pairs
+    b.snapshot(0)
+    pairs_per_step = b.pairs - p0
+
+    def step():
+        b.snapshot_device(0, d_T.data_ptr(), stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(dev.index or 0)
+    clocks.start()
+    for k in range(args.steps):
+        flush.zero_()
+        ev[k][0].record(stream)
+        step()
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    barrier(world)
+    step_ms = [a.elapsed_time(c) for a, c in ev]
+    total_s = allreduce_max(sum(step_ms) / 1e3, world)
+    value = pairs_per_step * args.steps * world / total_s
+    b.snapshot(0)                       # surfaces any node-list error of the timed replays
+
+    pinned = torch.empty(pnum, dtype=torch.float64, pin_memory=True).numpy()
+    e2e_t = []
+    for _ in range(max(1, args.steps)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with th.Batch(paths, args.precision) as b2:
+            b2.snapshot(0, out=pinned)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = allreduce_max(statistics.median(e2e_t), world)
+    e2e = {"value": pairs_per_step * world / e2e_s, "unit": "pairs/s",
+           "h2d_bytes_per_step": int(sum(len(p) for d in deck for p in d.paths) * 64),
+           "d2h_bytes_per_step": int(8 * pnum), "ms_per_step": 1e3 * e2e_s,
+           "includes": "256 deck parses + batch creation (node sizing, graph capture) + D2H of T into pinned memory"}
+    pk, src = peaks()
+    clk_mhz = (clk or {}).get("sm_mhz") or pk.get("sm_max_mhz", 2070.0)
+    kernel_ms = statistics.median(step_ms)
+    achieved = pairs_per_step / (kernel_ms / 1e3)
+    peak_pairs = SM_COUNT * clk_mhz * 1e6 * min(FP32_LANES / FP32_OPS_KAHAN, MUFU_LANES)
+    roof = {"bound": "fp32_issue", "kernel": "k_batch_grid (step incl. k_batch_nodes)",
+            "achieved": achieved / 1e9, "peak": peak_pairs / 1e9, "unit": "Gpairs/s", "frac": achieved / peak_pairs,
+            "achieved_tops": achieved * OPS_PER_PAIR / 1e12, "kernel_ms": kernel_ms,
+            "pairs_per_launch": pairs_per_step,
+            "peak_basis": f"{SM_COUNT} SMs x {clk_mhz:.0f} MHz x min({FP32_LANES}/{FP32_OPS_KAHAN} FP32 issue, "
+                          f"{MUFU_LANES} MUFU) pairs/clk",
+            "hbm": {"algorithmic_bytes": int(8 * pnum), "peak_gbs": pk.get("hbm_gbs"),
+                    "achieved_gbs": 8 * pnum / (kernel_ms / 1e3) / 1e9, "peak_source": src},
+            "traffic": None}
+    b.close()
+    return {"value": value, "ms_per_step": 1e3 * total_s / args.steps, "e2e": e2e, "roofline": roof,
+            "clocks": clk, "gpu_launches": 2 * args.steps,
+            "detail": {"pairs_per_step": pairs_per_step, "points": pnum, "decks": len(paths)}}
+
+
 # ------------------------------------------------------------------ CPU oracle legs
 def cpu_sample(path, workload, threads, budget_s):
     """The CPU oracle on the same deck: solidification runs a prefix of the timesteps,
@@ -298,6 +381,16 @@ def cpu_sample(path, workload, threads, budget_s):
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_lib
     oracle_lib.load()
+    if workload == "snapshot_sweep":
+        pairs, used, n = 0, 0.0, 0
+        while used < budget_s and n < len(path):
+            o = oracle_lib.Oracle(path[n])
+            p0, t0 = o.pairs, time.perf_counter()
+            o.snapshot(0, threads=threads)
+            used += time.perf_counter() - t0
+            pairs += o.pairs - p0
+            n += 1
+        return pairs / used, f"the 100 % snapshot of the first {n} decks of the sweep ({used:.1f} s)"
     if workload == "snapshot_raster":
         o = oracle_lib.Oracle(path)
         pairs, used, n = 0, 0.0, 0
@@ -372,7 +465,8 @@ def main():
     torch.cuda.set_device(dev)
     tmp = tempfile.mkdtemp(prefix="thesis_bench_")
     deck, path = make_deck(args.workload, tmp)
-    runner = run_solidification if args.workload == "surface_serpentine" else run_snapshot
+    runner = {"surface_serpentine": run_solidification, "snapshot_raster": run_snapshot,
+              "snapshot_sweep": run_sweep}[args.workload]
     r = runner(args, th, torch, dev, path, deck, world)
     line = {"metric": METRIC, "value": r["value"], "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",

@@ -154,6 +154,38 @@ th_status th_set_tile_shape(th_ctx* ctx, int32_t kp, int32_t kch);
 /* Device time (ms) of the most recent th_snapshot's point x node kernel. */
 th_status th_last_kernel_ms(th_ctx* ctx, float* out);
 
+/* Times snapshot idx's whole-grid kernel with every supported tile shape and keeps the
+ * fastest for this context; the chosen shape is written to *kp_out / *kch_out. */
+th_status th_autotune(th_ctx* ctx, int32_t idx, int32_t* kp_out, int32_t* kch_out);
+
+/* ---- Batched snapshots -------------------------------------------------------------
+ * n independent Snapshots decks (a process-parameter sweep: power, speed, widths,
+ * material, path, grid may all differ) evaluated together.  A batch snapshot fills one
+ * flat array: deck d's grid occupies [offsets[d], offsets[d + 1]) in the deck's own point
+ * order.  Snapshot idx of the batch is snapshot idx of every deck (idx below the smallest
+ * snapshot count).  Each batch snapshot is two launches - node lists, one thread block per
+ * deck, and a persistent work-list kernel over every deck's tiles - captured once as a CUDA
+ * graph and replayed.  The reference runs such sweeps as one process per deck
+ * (bin/Main.cpp:45-94 runs one ParamInput.txt per process). */
+typedef struct th_batch th_batch;
+
+th_status th_batch_create(const char* const* param_inputs, int32_t n, int32_t precision, th_batch** out);
+void th_batch_destroy(th_batch* b);
+/* Message of the last failure on b (b NULL: of the last failed th_batch_create). */
+const char* th_batch_last_error(const th_batch* b);
+/* offsets[0..n]: exclusive prefix of the decks' point counts. */
+th_status th_batch_points(th_batch* b, int64_t* offsets);
+/* Snapshot idx of every deck into host memory T_out (offsets[n] doubles); synchronous. */
+th_status th_batch_snapshot(th_batch* b, int32_t idx, double* T_out);
+/* The same into device memory d_T, enqueued on stream (NULL: the batch's own stream);
+ * returns without waiting.  Node-list errors surface at the next th_batch_snapshot. */
+th_status th_batch_snapshot_device(th_batch* b, int32_t idx, double* d_T, void* stream);
+th_status th_batch_set_tile_shape(th_batch* b, int32_t kp, int32_t kch);
+/* Times every supported tile shape on batch snapshot idx and keeps the fastest. */
+th_status th_batch_autotune(th_batch* b, int32_t idx, int32_t* kp_out, int32_t* kch_out);
+/* Point x node pairs evaluated by the batch so far. */
+th_status th_batch_pairs(th_batch* b, int64_t* out);
+
 #ifdef __cplusplus
 }
 #endif
