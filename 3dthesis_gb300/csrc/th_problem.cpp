@@ -379,6 +379,13 @@ void th_make_dev_problem(const HostProblem& hp, const DevSeg* d_segs, DevProblem
     off += D.nseg;
   }
   dp.T0 = hp.T0; dp.TL = hp.TL; dp.a = hp.a; dp.a12 = 12.0 * hp.a;
+  {  // exact ceil((TL - T0) * 2^30): TL - T0 = s + e exactly (TwoSum), then ceil of (s + e) * 2^30
+    const double s = hp.TL - hp.T0, bb = s - hp.TL;
+    const double e = (hp.TL - (s - bb)) + (-hp.T0 - bb);
+    const double s30 = std::ldexp(s, 30), f = std::floor(s30);
+    const double r = (s30 - f) + std::ldexp(e, 30);
+    dp.tl_fix = (int64_t)f + (r > 1.0 ? 2 : (r > 0.0 ? 1 : 0));
+  }
   dp.cetN0 = hp.cetN0; dp.cetn = hp.cetn; dp.ceta = hp.ceta;
   dp.nx = hp.nx; dp.ny = hp.ny; dp.nz = hp.nz;
   dp.gx = (uint16_t)hp.nx; dp.gy = (uint16_t)hp.ny; dp.gz = (uint16_t)hp.nz;
@@ -421,5 +428,11 @@ void th_make_dev_problem(const HostProblem& hp, const DevSeg* d_segs, DevProblem
   for (int i = 0; i < dp.n_images && i < TH_MAX_IMAGES; ++i) { dp.img[i][0] = all[i][0]; dp.img[i][1] = all[i][1]; dp.img[i][2] = all[i][2]; }
   dp.dt = hp.dt; dp.sol_tol = hp.sol_tol; dp.sol_iter = hp.sol_iter;
   dp.tracking = hp.tracking; dp.rcheck = hp.rcheck; dp.end_time = hp.end_time;
+  for (int b = 0; b < dp.nbeams; ++b) {   // src/Melt.cpp:24-31, rounded step by step as there
+    DevBeam& D = dp.beam[b];
+    const double rc2 = hp.rcheck * hp.rcheck;
+    D.tsub = ((rc2 - 1.0) * D.ax2) / (12.0 * dp.a);
+    D.r2 = (rc2 * D.ax) * D.ax;
+  }
   th_gauss_tables(dp.gl_loc, dp.gl_w);
 }

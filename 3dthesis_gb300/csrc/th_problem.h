@@ -26,6 +26,8 @@ struct DevBeam {
   double nond;              // ax^2 / a
   double beta;              // (3/pi)^1.5 * q / (rho c)
   double tlast;             // end time of this beam's path
+  double tsub;              // beam-trace look-back (CheckRadius^2 - 1) ax^2 / (12 a)
+  double r2;                // beam-trace radius squared, CheckRadius^2 ax^2
   int32_t seg_off, nseg;    // segments [seg_off, seg_off + nseg) of DevProblem::segs
 };
 
@@ -35,6 +37,7 @@ struct DevProblem {
   DevBeam beam[TH_MAX_BEAMS];
   // material
   double T0, TL, a, a12;    // a12 = 12 * a
+  int64_t tl_fix;           // ceil((TL - T0) * 2^30): the liquidus in the FP32 tracking's fixed point
   double cetN0, cetn, ceta;
   // domain
   int32_t nx, ny, nz;       // axis counts

@@ -34,6 +34,8 @@ struct Window {
   NodeWindow W{};
   double* d_t = nullptr;
   int* d_count = nullptr;
+  int* d_seeds = nullptr;
+  int* d_nseed = nullptr;
   int slots = 0;
   int base = 0, n = 0;                // steps [base, base + n) in slots 1..n
   cudaEvent_t gen0 = nullptr, gen1 = nullptr;   // around the node build
@@ -48,12 +50,14 @@ struct RunState {
   Window win[2];
   SolRec* rec[2] = {nullptr, nullptr};
   int slot_cap = 1024;
+  int seed_cap = 256;     // beam-trace candidates per step
   int k = 0;              // next step
   std::vector<double> times;   // step times, accumulated as the reference does
   bool done = false;
   bool initialised = false;
   int max_items = 0;
   double* d_field = nullptr;
+  float2* d_axis = nullptr;
   cudaStream_t aux = nullptr;
   int* h_err = nullptr;        // pinned: node-build error bits per window
   cudaEvent_t ev_trk[2][2] = {};  // around each window's tracking launch
@@ -70,11 +74,12 @@ void th_release_run_state(th_ctx* ctx) {
   if (r->aux) cudaStreamSynchronize(r->aux);
   for (void* p : r->allocs) cudaFree(p);
   for (Window& w : r->win) {
-    cudaFree(w.mem); cudaFree(w.d_t); cudaFree(w.d_count);
+    cudaFree(w.mem); cudaFree(w.d_t); cudaFree(w.d_count); cudaFree(w.d_seeds); cudaFree(w.d_nseed);
     if (w.gen0) cudaEventDestroy(w.gen0);
     if (w.gen1) cudaEventDestroy(w.gen1);
   }
   cudaFree(r->d_field);
+  cudaFree(r->d_axis);
   if (r->h_err) cudaFreeHost(r->h_err);
   for (int b = 0; b < 2; ++b)
     for (int e = 0; e < 2; ++e) {
@@ -149,7 +154,7 @@ th_status init_run(th_ctx* ctx) {
     for (int i = 0; i < 3; ++i) ALLOC(S.liq[i], n, 0);
     // work items of one step: every claimed point and column layer at most once, which
     // in practice stays far below 2 * pnum
-    S.queue_cap = (int)std::min<size_t>(2 * n + 4096, (size_t)1 << 24);
+    S.queue_cap = (int)std::min<size_t>(2 * n + 4096, ((size_t)1 << 24) - 1);   // fits the step word's fields
     ALLOC(S.queue, (size_t)S.queue_cap, 0);
   }
   S.rec_cap = kRecCap;
@@ -159,6 +164,25 @@ th_status init_run(th_ctx* ctx) {
   ALLOC(S.bar, 2, 0);
   ALLOC(S.err, 1, 0);
 #undef ALLOC
+  {  // point coordinates (the device's coord(): min + i * h, or max on a one-point axis) as float pairs
+    const DevProblem& D = ctx->dp;
+    std::vector<float2> ax;
+    auto axis = [&](int g, int cnt, double vmin, double vmax, double h) {
+      for (int i = 0; i < cnt; ++i) {
+        const double v = (g - 1) ? vmin + (double)i * h : vmax;
+        const float hi = (float)v;
+        ax.push_back(make_float2(hi, (float)(v - (double)hi)));
+      }
+    };
+    axis(D.gx, D.nx, D.xmin, D.xmax, D.hx);
+    axis(D.gy, D.ny, D.ymin, D.ymax, D.hy);
+    axis(D.gz, D.nz, D.zmin, D.zmax, D.hz);
+    if ((st = th_cuda_check(ctx, cudaMalloc(&r->d_axis, ax.size() * sizeof(float2)), "cudaMalloc")) != TH_OK) return st;
+    if ((st = th_cuda_check(ctx, cudaMemcpy(r->d_axis, ax.data(), ax.size() * sizeof(float2), cudaMemcpyHostToDevice),
+                            "copy")) != TH_OK)
+      return st;
+    S.axis = r->d_axis;
+  }
   S.pairs = ctx->d_pairs;
   S.rec = r->rec[0];
   S.rec_n = &S.C->rec_n[0];
@@ -181,15 +205,21 @@ th_status init_run(th_ctx* ctx) {
   return th_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "init");
 }
 
-th_status alloc_window(th_ctx* ctx, Window& w, int slots, int slot_cap) {
+th_status alloc_window(th_ctx* ctx, Window& w, int slots, int slot_cap, int seed_cap) {
   cudaFree(w.mem); w.mem = nullptr;
   cudaFree(w.d_t); w.d_t = nullptr;
   cudaFree(w.d_count); w.d_count = nullptr;
+  cudaFree(w.d_seeds); w.d_seeds = nullptr;
+  cudaFree(w.d_nseed); w.d_nseed = nullptr;
   const size_t cap = (size_t)slots * slot_cap;
   th_status st = th_cuda_check(ctx, cudaMalloc(&w.mem, cap * (8 * sizeof(double) + 10 * sizeof(float))), "cudaMalloc");
   if (st != TH_OK) return st;
   if ((st = th_cuda_check(ctx, cudaMalloc(&w.d_t, slots * sizeof(double)), "cudaMalloc")) != TH_OK) return st;
   if ((st = th_cuda_check(ctx, cudaMalloc(&w.d_count, slots * sizeof(int)), "cudaMalloc")) != TH_OK) return st;
+  if ((st = th_cuda_check(ctx, cudaMalloc(&w.d_seeds, (size_t)slots * seed_cap * sizeof(int)), "cudaMalloc")) != TH_OK)
+    return st;
+  if ((st = th_cuda_check(ctx, cudaMalloc(&w.d_nseed, slots * sizeof(int)), "cudaMalloc")) != TH_OK) return st;
+  if ((st = th_cuda_check(ctx, cudaMemset(w.d_nseed, 0, slots * sizeof(int)), "cudaMemset")) != TH_OK) return st;
   double* d = (double*)w.mem;
   float* f = (float*)(d + 8 * cap);
   NodeBufView& nb = w.W.nb;
@@ -202,6 +232,9 @@ th_status alloc_window(th_ctx* ctx, Window& w, int slots, int slot_cap) {
   w.W.nslots = slots;
   w.W.count = w.d_count;
   w.W.t = w.d_t;
+  w.W.seeds = w.d_seeds;
+  w.W.nseed = w.d_nseed;
+  w.W.seed_cap = seed_cap;
   w.slots = slots;
   return TH_OK;
 }
@@ -210,8 +243,9 @@ th_status alloc_window(th_ctx* ctx, Window& w, int slots, int slot_cap) {
 // (slot 0) into window b on `s`; the error bits land in h_err[b] when w.gen1 completes.
 th_status enqueue_window(th_ctx* ctx, RunState* r, int b, int base, int n, cudaStream_t s) {
   Window& w = r->win[b];
-  if (!w.mem || w.slots < n + 1 || w.W.slot_cap != r->slot_cap) {
-    th_status st = alloc_window(ctx, w, std::max(n + 1, std::max(w.slots, kWindowTrack + 1)), r->slot_cap);
+  if (!w.mem || w.slots < n + 1 || w.W.slot_cap != r->slot_cap || w.W.seed_cap != r->seed_cap) {
+    th_status st = alloc_window(ctx, w, std::max(n + 1, std::max(w.slots, kWindowTrack + 1)), r->slot_cap,
+                                r->seed_cap);
     if (st != TH_OK) return st;
   }
   std::vector<double> ts(n + 1);
@@ -246,13 +280,16 @@ th_status finish_window(th_ctx* ctx, RunState* r, int b) {
     r->ms_nodes += ms;
     const int err = r->h_err[b];
     if (err & 2) return th_fail(ctx, TH_ERR_TIMEOUT, "quadrature walk exceeded its step limit");
-    if (!(err & 1)) return TH_OK;
-    std::vector<int> cnt(w.n + 1);
+    if (!(err & (1 | ERR_SEED_CAPACITY))) return TH_OK;
+    std::vector<int> cnt(w.n + 1), ns(w.n + 1);
     st = th_cuda_check(ctx, cudaMemcpy(cnt.data(), w.d_count, (w.n + 1) * sizeof(int), cudaMemcpyDeviceToHost), "copy");
     if (st != TH_OK) return st;
-    int mx = 0;
-    for (int i = (w.base == 0 ? 1 : 0); i <= w.n; ++i) mx = std::max(mx, cnt[i]);
-    r->slot_cap = std::max(r->slot_cap, ((mx + 256) / 32 + 1) * 32);
+    st = th_cuda_check(ctx, cudaMemcpy(ns.data(), w.d_nseed, (w.n + 1) * sizeof(int), cudaMemcpyDeviceToHost), "copy");
+    if (st != TH_OK) return st;
+    int mx = 0, ms_ = 0;
+    for (int i = (w.base == 0 ? 1 : 0); i <= w.n; ++i) { mx = std::max(mx, cnt[i]); ms_ = std::max(ms_, ns[i]); }
+    if (err & 1) r->slot_cap = std::max(r->slot_cap, ((mx + 256) / 32 + 1) * 32);
+    if (err & ERR_SEED_CAPACITY) r->seed_cap = std::max(r->seed_cap, ((ms_ + 64) / 32 + 1) * 32);
     // the other window may still be in use by the tracking stream or the aux stream
     cudaStreamSynchronize(r->aux);
     cudaStreamSynchronize(ctx->stream);
@@ -536,11 +573,19 @@ th_status th_run_stats(th_ctx* ctx, double* out, int32_t n) {
   unsigned long long pairs[2] = {0, 0};
   th_status st = th_cuda_check(ctx, cudaMemcpy(pairs, ctx->d_pairs, sizeof(pairs), cudaMemcpyDeviceToHost), "cudaMemcpy");
   if (st != TH_OK) return st;
-  const double v[11] = {r ? r->ms_nodes : 0, r ? r->ms_track : 0, r ? r->ms_solid : 0, r ? (double)r->windows : 0,
+  unsigned long long prof[18] = {};
+  if (r && r->S.C) {
+    st = th_cuda_check(ctx, cudaMemcpy(prof, r->S.C->prof, sizeof(prof), cudaMemcpyDeviceToHost), "cudaMemcpy");
+    if (st != TH_OK) return st;
+  }
+  const double v[28] = {r ? r->ms_nodes : 0, r ? r->ms_track : 0, r ? r->ms_solid : 0, r ? (double)r->windows : 0,
                         r ? (double)r->records : 0, r ? (double)r->max_items : 0, r ? (double)r->k : 0,
                         r ? (double)r->slot_cap : 0, r ? r->ms_device : 0, (double)pairs[1],
-                        (double)pairs[0]};
-  for (int i = 0; i < n && i < 11; ++i) out[i] = v[i];
+                        (double)pairs[0], prof[0] * 1e-6, prof[1] * 1e-6, (double)prof[2], (double)prof[3],
+                        (double)prof[4], (double)prof[5], (double)prof[6], (double)prof[7], (double)prof[8],
+                        prof[10] * 1e-6, prof[11] * 1e-6, prof[12] * 1e-6, prof[13] * 1e-6,
+                        prof[14] * 1e-6, prof[15] * 1e-6, prof[16] * 1e-6, prof[17] * 1e-6};
+  for (int i = 0; i < n && i < 28; ++i) out[i] = v[i];
   return TH_OK;
 }
 

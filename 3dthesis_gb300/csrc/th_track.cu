@@ -13,6 +13,7 @@
 // are the same whatever order the claims happen in.  Liquid -> solid transitions are
 // queued as (point, step, T, T_last) records and their solidification time and gradients
 // are computed afterwards, in bulk, one thread per record.
+#include <algorithm>
 #include <cfloat>
 #include <climits>
 #include <cstdint>
@@ -35,15 +36,6 @@ __device__ __forceinline__ NodeBufView slot_view(const NodeWindow& w, int slot) 
   return v;
 }
 
-// ------------------------------------------------------------------ node windows
-__global__ void __launch_bounds__(kGenThreads) k_nodes_window(DevProblem P, NodeWindow w, int first, int n, int is_sol,
-                                                              int* err) {
-  __shared__ GenShared sh;
-  const int slot = first + blockIdx.x;
-  const NodeBufView nb = slot_view(w, slot);
-  gen_list_block(P, w.t[slot], is_sol != 0, nb, &w.count[slot], err, sh);
-}
-
 // ------------------------------------------------------------------ warp evaluation
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
@@ -51,41 +43,175 @@ __device__ __forceinline__ double warp_sum_d(double v) {
   return v;
 }
 
-// T at point p from one node list, the 32 lanes of a warp splitting the nodes; every lane
-// returns the same value.
+// The current step's node list staged in shared memory (array-of-structures, one copy per
+// block): FP32 A = (xh, yh, zh, kx), B = (xl, yl, zl, ky), C = (kz, w); FP64 four double2
+// (x, y), (z, 1/phix), (1/phiy, 1/phiz), (dtau, amp).  Nodes at and beyond n_sm are read
+// from the window in global memory.
+struct Staged {
+  const unsigned char* base;
+  int n_sm;                // staged nodes
+  int cap;                 // nodes per staged array
+};
+
 template <int PREC>
-__device__ __forceinline__ double warp_T(const DevProblem& P, const NodeBufView& nb, int nn, int64_t p) {
-  const int lane = threadIdx.x & 31;
-  double x, y, z;
-  point_xyz(P, p, x, y, z);
-  double part;
+__host__ __device__ constexpr int staged_bytes_per_node() { return PREC == 0 ? 64 : 40; }
+
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Issues the block's asynchronous copies of the first m nodes of nb into buf (field-major
+// order, so consecutive threads read consecutive nodes of one field).
+template <int PREC>
+__device__ __forceinline__ void stage_issue(const NodeBufView& nb, int m, unsigned char* buf, int cap) {
   if (PREC == 0) {
-    double s = 0.0;
-    for (int n = lane; n < nn; n += 32) {
-      const double dx = x - __ldg(nb.x + n), dy = y - __ldg(nb.y + n), dz = z - __ldg(nb.z + n);
-      s += __ldg(nb.dtau + n) * __ldg(nb.amp + n) *
-           exp(-3.0 * (dx * dx * __ldg(nb.ipx + n) + dy * dy * __ldg(nb.ipy + n) + dz * dz * __ldg(nb.ipz + n)));
+    const double* src[8] = {nb.x, nb.y, nb.z, nb.ipx, nb.ipy, nb.ipz, nb.dtau, nb.amp};
+    for (int i = threadIdx.x; i < 8 * m; i += blockDim.x) {
+      const int f = i / m, n = i - f * m;
+      double* dst = (double*)(buf + (size_t)(f >> 1) * cap * 16) + 2 * n + (f & 1);
+      cp_async8(dst, src[f] + n);
     }
-    part = s;
   } else {
-    const float xh = __double2float_rn(x), yh = __double2float_rn(y), zh = __double2float_rn(z);
-    const float xl = __double2float_rn(x - (double)xh), yl = __double2float_rn(y - (double)yh),
-                zl = __double2float_rn(z - (double)zh);
-    float s = 0.f, c = 0.f;
-    for (int n = lane; n < nn; n += 32) {
-      const float dx = (xh - __ldg(nb.xh + n)) + (xl - __ldg(nb.xl + n));
-      const float dy = (yh - __ldg(nb.yh + n)) + (yl - __ldg(nb.yl + n));
-      const float dz = (zh - __ldg(nb.zh + n)) + (zl - __ldg(nb.zl + n));
-      const float e = fmaf(dz * dz, __ldg(nb.kz + n), fmaf(dy * dy, __ldg(nb.ky + n), dx * dx * __ldg(nb.kx + n)));
-      const float v = ex2_approx(e) * __ldg(nb.w + n);
-      const float yy = v - c;
-      const float tt = s + yy;
-      c = (tt - s) - yy;
-      s = tt;
+    const float* src[10] = {nb.xh, nb.yh, nb.zh, nb.kx, nb.xl, nb.yl, nb.zl, nb.ky, nb.kz, nb.w};
+    for (int i = threadIdx.x; i < 10 * m; i += blockDim.x) {
+      const int f = i / m, n = i - f * m;
+      float* dst = f < 8 ? (float*)(buf + (size_t)(f >> 2) * cap * 16) + 4 * n + (f & 3)
+                         : (float*)(buf + (size_t)cap * 32) + 2 * n + (f - 8);
+      cp_async4(dst, src[f] + n);
     }
-    part = (double)s - (double)c;
   }
-  return P.T0 + warp_sum_d(part);
+  cp_async_commit();
+}
+
+// round(x * 2^30) as an integer, from the float's bits alone (no FP64 or conversion unit):
+// |x| below 2^32; values under 2^-31 give 0.
+__device__ __forceinline__ long long to_fix30(float x) {
+  const int b = __float_as_int(x);
+  const int e = (b >> 23) & 0xff;
+  const long long m = (long long)((b & 0x7fffff) | 0x800000);
+  const int sh = e - 120;                                // value = m * 2^(e - 150); times 2^30
+  long long v;
+  if (e == 0 || sh < -24) v = 0;
+  else if (sh >= 0) v = m << min(sh, 38);
+  else v = (m + (1ll << (-sh - 1))) >> -sh;
+  return b < 0 ? -v : v;
+}
+
+// One evaluation's result: T, and T >= T_L decided exactly.
+struct EvalT { double T; bool liquid; };
+
+// T at NP points from one node list, the 32 lanes of a warp splitting the nodes; every
+// lane returns the same values.  Each node is read once for all NP points, so a pass over
+// four points costs little more than a pass over one.
+//
+// FP32 form: the points' coordinates come as (hi, lo) float pairs from per-axis tables;
+// each lane sums its share with Kahan compensation; the lanes' results are reduced as
+// 64-bit fixed point (2^-30 K), which is exact and independent of the order, and the
+// liquid test is an integer comparison with ceil((T_L - T_0) 2^30).  No FP64 operation
+// sits on the evaluation's path; T itself is formed in FP64 once, for storing.
+template <int PREC, int NP>
+__device__ __forceinline__ void warp_T_n(const DevProblem& P, const TrackState& S, const NodeBufView& nb, int nn,
+                                         const int (&pts)[NP], const Staged& st, EvalT (&out)[NP]) {
+  const int lane = threadIdx.x & 31;
+  const int n_sm = min(st.n_sm, nn);
+  unsigned pi[NP], pj[NP], pk[NP];
+#pragma unroll
+  for (int q = 0; q < NP; ++q) {
+    const unsigned pu = (unsigned)pts[q], col = pu / (unsigned)P.nz;
+    pk[q] = pu - col * (unsigned)P.nz;
+    pi[q] = col / (unsigned)P.ny;
+    pj[q] = col - pi[q] * (unsigned)P.ny;
+  }
+  if constexpr (PREC == 0) {
+    double x[NP], y[NP], z[NP], s[NP];
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+      x[q] = coord(P.gx, P.xmin, P.xmax, P.hx, (int)pi[q]);
+      y[q] = coord(P.gy, P.ymin, P.ymax, P.hy, (int)pj[q]);
+      z[q] = coord(P.gz, P.zmin, P.zmax, P.hz, (int)pk[q]);
+      s[q] = 0.0;
+    }
+    const double2* D = (const double2*)st.base;
+    auto acc = [&](double2 a, double2 b, double2 c, double2 d) {
+      const double wa = d.x * d.y;
+#pragma unroll
+      for (int q = 0; q < NP; ++q) {
+        const double dx = x[q] - a.x, dy = y[q] - a.y, dz = z[q] - b.x;
+        s[q] += wa * exp(-3.0 * (dx * dx * b.y + dy * dy * c.x + dz * dz * c.y));
+      }
+    };
+    int n = lane;
+    for (; n < n_sm; n += 32) acc(D[n], D[st.cap + n], D[2 * st.cap + n], D[3 * st.cap + n]);
+    for (; n < nn; n += 32)
+      acc(make_double2(__ldg(nb.x + n), __ldg(nb.y + n)), make_double2(__ldg(nb.z + n), __ldg(nb.ipx + n)),
+          make_double2(__ldg(nb.ipy + n), __ldg(nb.ipz + n)), make_double2(__ldg(nb.dtau + n), __ldg(nb.amp + n)));
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+      out[q].T = P.T0 + warp_sum_d(s[q]);
+      out[q].liquid = out[q].T >= P.TL;
+    }
+  } else {
+    float2 X[NP], Y[NP], Z[NP];
+    float s[2][NP], c[2][NP];                    // two independent Kahan sums per point
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+      X[q] = __ldg(S.axis + pi[q]);
+      Y[q] = __ldg(S.axis + P.nx + pj[q]);
+      Z[q] = __ldg(S.axis + P.nx + P.ny + pk[q]);
+      s[0][q] = s[1][q] = 0.f;
+      c[0][q] = c[1][q] = 0.f;
+    }
+    auto acc = [&](int h, float4 a, float4 b, float2 cc) {
+#pragma unroll
+      for (int q = 0; q < NP; ++q) {
+        const float dx = (X[q].x - a.x) + (X[q].y - b.x);
+        const float dy = (Y[q].x - a.y) + (Y[q].y - b.y);
+        const float dz = (Z[q].x - a.z) + (Z[q].y - b.z);
+        const float e = fmaf(dz * dz, cc.x, fmaf(dy * dy, b.w, dx * dx * a.w));
+        const float v = ex2_approx(e) * cc.y;
+        const float yy = v - c[h][q];
+        const float tt = s[h][q] + yy;
+        c[h][q] = (tt - s[h][q]) - yy;
+        s[h][q] = tt;
+      }
+    };
+    const float4* A = (const float4*)st.base;
+    const float4* B = A + st.cap;
+    const float2* C = (const float2*)(B + st.cap);
+    int n = lane;
+    for (; n + 32 < n_sm; n += 64) {              // two nodes per round, one per sum
+      const float4 a0 = A[n], b0 = B[n], a1 = A[n + 32], b1 = B[n + 32];
+      const float2 c0 = C[n], c1 = C[n + 32];
+      acc(0, a0, b0, c0);
+      acc(1, a1, b1, c1);
+    }
+    for (; n < n_sm; n += 32) acc(0, A[n], B[n], C[n]);
+    for (; n < nn; n += 32)
+      acc(0, make_float4(__ldg(nb.xh + n), __ldg(nb.yh + n), __ldg(nb.zh + n), __ldg(nb.kx + n)),
+          make_float4(__ldg(nb.xl + n), __ldg(nb.yl + n), __ldg(nb.zl + n), __ldg(nb.ky + n)),
+          make_float2(__ldg(nb.kz + n), __ldg(nb.w + n)));
+    long long f[NP];
+#pragma unroll
+    for (int q = 0; q < NP; ++q)
+      f[q] = (to_fix30(s[0][q]) - to_fix30(c[0][q])) + (to_fix30(s[1][q]) - to_fix30(c[1][q]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+      for (int q = 0; q < NP; ++q) f[q] += __shfl_xor_sync(0xffffffffu, f[q], o);
+    }
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+      out[q].liquid = f[q] >= P.tl_fix;
+      out[q].T = fma((double)f[q], 0x1p-30, P.T0);
+    }
+  }
 }
 
 __device__ __forceinline__ int ldcg_i(const int* p) { return __ldcg(p); }
@@ -98,51 +224,31 @@ __device__ __forceinline__ void push_record(const TrackState& S, int p, int step
   atomicAdd(&S.num_melt[p], 1);
 }
 
+// A block's solidification records, gathered in shared memory and appended to the launch's
+// record buffer when half full and at the end of the launch (one atomic per flush), so
+// items never wait on the global record counter.  A full buffer falls back to the global
+// list.
+constexpr int kBlkRec = 256;
+struct BlockBuf {
+  int nrec, base_rec;
+  SolRec rec[kBlkRec];
+};
+
+// The step word of QueueCounters::state: items completed (bits 0-23), items published
+// (24-47), blocks that have entered the step (48-63).
+constexpr unsigned long long kField = 0xffffffull, kArrive = 1ull << 48;
+
 // Grid::Calc_T with set = true (src/Grid.cpp:300-311): the liquid markers (G = V = DBL_MIN,
 // eqFrac = -1) are applied when fields are read, from last_liq.
-__device__ __forceinline__ void set_T(const TrackState& S, const DevProblem& P, int p, double T, int step) {
-  S.T[p] = T;
-  if (T >= P.TL) { S.outflag[p] = 1; S.last_liq[p] = step; }
+__device__ __forceinline__ void set_T(const TrackState& S, int p, const EvalT& e, int step) {
+  S.T[p] = e.T;
+  if (e.liquid) { S.outflag[p] = 1; S.last_liq[p] = step; }
 }
 
-// Grid-wide barrier for the cooperative launch.  The wait is bounded: after kSpinLimit
-// polls it latches ERR_BARRIER and every block leaves the kernel at its next check.
+// Bound on the polls of one wait for work (about 8 s at the longest back-off); past it the
+// waiter latches ERR_BARRIER and releases every warp of the launch.
 constexpr long long kSpinLimit = 1ll << 25;
 
-__device__ __forceinline__ bool grid_sync(const TrackState& S) {
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    volatile unsigned* gen = S.bar + 1;
-    const unsigned g = *gen;
-    __threadfence();
-    if (atomicAdd(S.bar, 1u) == gridDim.x - 1) {
-      atomicExch(S.bar, 0u);
-      __threadfence();
-      atomicAdd(S.bar + 1, 1u);
-    } else {
-      long long spins = 0;
-      while (*gen == g) {
-        if (++spins > kSpinLimit) {
-          if (atomicOr(S.err, ERR_BARRIER) == 0) { S.C->diag[0] = 2; S.C->diag[2] = (int)blockIdx.x; S.C->diag[4] = (int)*S.bar; }
-          break;
-        }
-        __nanosleep(32);
-      }
-    }
-    __threadfence();
-  }
-  __syncthreads();
-  return (*(volatile int*)S.err & ERR_BARRIER) == 0;
-}
-
-__device__ __forceinline__ int first_ge(const DevSeg* path, int ns, double t) {
-  int lo = 0, hi = ns - 1;                 // first s with t_end >= t, clamped to the last
-  while (lo < hi) {
-    const int mid = (lo + hi) >> 1;
-    if (path[mid].tend < t) lo = mid + 1; else hi = mid;
-  }
-  return lo;
-}
 
 __device__ __forceinline__ int64_t pid(const DevProblem& P, int i, int j, int k) {
   return (int64_t)i * ((int64_t)P.ny * P.nz) + (int64_t)j * P.nz + k;
@@ -151,14 +257,25 @@ __device__ __forceinline__ int64_t pid(const DevProblem& P, int i, int j, int k)
 // Claim for this step (the reference's T_calc_flag test-and-set, src/Melt.cpp:213-218):
 // a point counts as claimed in step k when its stamp is >= k + 1.
 __device__ __forceinline__ bool claim(const TrackState& S, int q, unsigned stamp) {
-  if (__ldcg(S.stamp + q) >= stamp) return false;
   return atomicMax(S.stamp + q, stamp) < stamp;
 }
 
+__device__ __forceinline__ unsigned long long globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
 // ------------------------------------------------------------------ step work queue
-enum { IT_RETEST = 0, IT_SEEDS = 1, IT_VISIT = 2, IT_COLUMN = 3, IT_DEPTH = 4 };
+enum { IT_RETEST = 0, IT_VISIT = 2, IT_COLUMN = 3 };
+
+__device__ constexpr Staged kNoStage = {nullptr, 0, 0};
 
 struct StepCtx {
+  Staged st;               // this step's node list in shared memory
+  BlockBuf* bb;            // this block's buffered records
+  mutable unsigned long long ev_n, ev_c;  // point evaluations and their SM clocks (profile)
+  int depth;               // chain depth of the item being run (its children get depth + 1)
   int k;                   // step
   unsigned stamp;          // k + 1
   double t;
@@ -176,33 +293,65 @@ __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long
   asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ int ld_acquire_s32(const int* p) {
-  int v;
-  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+__device__ __forceinline__ void st_relaxed_v2(ulonglong2* p, unsigned long long a, unsigned long long b) {
+  asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(p), "l"(a), "l"(b) : "memory");
+}
+__device__ __forceinline__ ulonglong2 ld_relaxed_v2(const ulonglong2* p) {
+  ulonglong2 v;
+  asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ void st_release_s32(int* p, int v) {
-  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+template <int PREC>
+__device__ __forceinline__ EvalT eval_T(const DevProblem& P, const TrackState& S, const StepCtx& X,
+                                        const NodeBufView& nb, int nn, int64_t p, const Staged& st) {
+  const long long c0 = clock64();
+  const int pts[1] = {(int)p};
+  EvalT T[1];
+  warp_T_n<PREC, 1>(P, S, nb, nn, pts, st, T);
+  X.ev_c += clock64() - c0;
+  X.ev_n += 1;
+  return T[0];
+}
+
+// Four points of this step's list in one pass (entries the caller does not need may repeat
+// a valid point).
+template <int PREC>
+__device__ __forceinline__ void eval_T4(const DevProblem& P, const TrackState& S, const StepCtx& X,
+                                        const int (&pts)[4], EvalT (&T)[4]) {
+  const long long c0 = clock64();
+  warp_T_n<PREC, 4>(P, S, X.nb, X.nn, pts, X.st, T);
+  X.ev_c += clock64() - c0;
+  X.ev_n += 1;
 }
 
 // Publishes one child item per lane that has one (warp-uniform call).  The children are
 // counted as published in the same atomic that hands out their slots, before any of them
 // can be taken, so "completed == initial + published" can only hold once the step has no
-// work left; each slot's tag is released after its payload.
+// work left.  Both 64-bit words of a slot carry the step's stamp, so a reader that sees
+// the stamp in both has the whole item without any further ordering.
 __device__ __forceinline__ void emit(const TrackState& S, const StepCtx& X, bool has, int type, int p, int aux,
                                      int& nchild) {
   const int lane = threadIdx.x & 31;
   const unsigned m = __ballot_sync(0xffffffffu, has);
   if (!m) return;
   unsigned base = 0;
-  if (lane == 0) base = (unsigned)(atomicAdd(&X.qc->state, (unsigned long long)__popc(m) << 32) >> 32);
+  if (lane == 0) base = (unsigned)((atomicAdd(&X.qc->state, (unsigned long long)__popc(m) << 24) >> 24) & kField);
   base = __shfl_sync(0xffffffffu, base, 0);
   if (has) {
     const unsigned j = base + __popc(m & ((1u << lane) - 1u));
     if (j < (unsigned)S.queue_cap) {
-      int4* slot = S.queue + j;
-      slot->y = type; slot->z = p; slot->w = aux;
-      st_release_s32(&slot->x, (int)X.stamp);
+      const unsigned long long hi = (unsigned long long)X.stamp << 32;
+      st_relaxed_v2(S.queue + j, hi | (unsigned)p,
+                    hi | (unsigned)(type | ((X.depth + 1) << 8) | (aux << 16)));
     } else {
       atomicOr(S.err, ERR_QUEUE);
     }
@@ -231,123 +380,273 @@ __device__ __forceinline__ void expand(const DevProblem& P, const TrackState& S,
 }
 
 __device__ __forceinline__ void push_liquid(const TrackState& S, const StepCtx& X, int p) {
+  atomicMax(S.stamp + p, X.stamp + 1u);   // already claimed for the next step's re-test
   const int i = atomicAdd(X.lo_n, 1);
   if (i < S.list_cap) X.Lo[i] = p; else atomicOr(S.err, ERR_LISTS);
-  atomicMax(S.stamp + p, X.stamp + 1u);   // already claimed for the next step's re-test
 }
 
-// Perimeter seeds of one anchor point (src/Melt.cpp:36-55, 69-77): when the anchor lies
-// outside the grid, surface points along that edge within CheckRadius * ax are tested.
-__device__ void perimeter(const DevProblem& P, const TrackState& S, const StepCtx& X, double x, double y, double r2,
-                          int& nchild) {
+__device__ __forceinline__ bool step_over(unsigned long long v, int n_init, unsigned blocks) {
+  return (v >> 48) == blocks && (v & kField) == (unsigned long long)n_init + ((v >> 24) & kField);
+}
+
+// Run by the one lane whose update ended step k: clears the counters of steps k + 1 (its
+// queue) and k + 2 (the liquid list it will fill), records the step, then publishes the
+// step's end.  Every block has entered step k and no item of it is left, so nothing reads
+// those counters any more and nothing of step k + 1 has started.
+// It also takes the step's verdict for every warp: the finish test (src/Util.cpp:239-243)
+// and the record queue's high-water mark, from the step's final counts.
+__device__ void finish_step(const DevProblem& P, const TrackState& S, const StepCtx& X, int k, unsigned long long v,
+                            int high_water) {
+  TrackCounters* C = S.C;
+  QueueCounters& q = C->q[(k + 1) % 3];
+  q.head = 0; q.depth = 0; q.state = 0ull;
+  for (int l = 0; l < 4; ++l) { q.lvl_start[l] = 0; q.lvl_end[l] = 0; }
+  C->liq_n[(k + 2) % 3] = 0;
+  C->step = k + 1;
+  const int items = X.n_init + (int)((v >> 24) & kField);
+  if (items > C->max_items) C->max_items = items;
+  unsigned flags = 0;
+  if (X.t > P.end_time && __ldcg(X.lo_n) == 0) { flags |= 1u; C->done = 1; }
+  else if (__ldcg(S.rec_n) > high_water) { flags |= 2u; C->stop = 1; }
+  C->verdict = (X.stamp << 2) | flags;
+  __threadfence();
+  st_release_u32(&C->finished, X.stamp);
+}
+
+__device__ __forceinline__ void push_rec(const TrackState& S, const StepCtx& X, int p, double T, double Tl) {
+  const int b = atomicAdd(&X.bb->nrec, 1);
+  if (b < kBlkRec) {
+    SolRec& r = X.bb->rec[b];
+    r.p = p; r.step = X.k; r.t = X.t; r.T = T; r.Tl = Tl;
+    atomicAdd(&S.num_melt[p], 1);
+  } else {
+    push_record(S, p, X.k, X.t, T, Tl);
+  }
+}
+
+// Appends the block's buffered records to the launch's record buffer (all threads of the
+// block; ends with the buffer empty).
+__device__ void flush_block(const TrackState& S, BlockBuf* bbp, int* rec_n) {
+  BlockBuf& bb = *bbp;
+  __syncthreads();
+  const int nr = min(bb.nrec, kBlkRec);
+  if (threadIdx.x == 0) bb.base_rec = nr ? atomicAdd(rec_n, nr) : 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+    const int j = bb.base_rec + i;
+    if (j < S.rec_cap) S.rec[j] = bb.rec[i]; else atomicOr(S.err, ERR_RECORDS);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) bb.nrec = 0;
+  __syncthreads();
+}
+
+// First segment whose end time is >= t, clamped to the last (src/Melt.cpp:58-60), found by
+// the whole warp: each round probes 32 evenly spaced segments, so a path of up to 1024
+// segments takes two dependent loads instead of ten.  Every lane returns the same index.
+__device__ __forceinline__ int warp_first_ge(const DevSeg* path, int ns, double t) {
   const int lane = threadIdx.x & 31;
-  const int xg = (int)floor(rn_div(rn_sub(x, P.xmin), P.xres));
-  const int yg = (int)floor(rn_div(rn_sub(y, P.ymin), P.yres));
-  for (int edge = 0; edge < 4; ++edge) {
-    int fixed;
-    bool xfixed;
-    if (edge == 0) { if (!(xg < 0)) continue; fixed = 0; xfixed = true; }
-    else if (edge == 1) { if (!(xg > P.nx - 1)) continue; fixed = P.nx - 1; xfixed = true; }
-    else if (edge == 2) { if (!(yg < 0)) continue; fixed = 0; xfixed = false; }
-    else { if (!(yg > P.ny - 1)) continue; fixed = P.ny - 1; xfixed = false; }
-    const int hi = xfixed ? P.ny : P.nx;
-    for (int v0 = 0; v0 < hi; v0 += 32) {
-      const int v = v0 + lane;
-      bool got = false;
-      int q = 0;
-      if (v < hi) {
-        const int i = xfixed ? fixed : v, j = xfixed ? v : fixed;
-        const double dx = rn_sub(rn_add(P.xmin, rn_mul((double)i, P.xres)), x);
-        const double dy = rn_sub(rn_add(P.ymin, rn_mul((double)j, P.yres)), y);
-        if (rn_add(rn_mul(dx, dx), rn_mul(dy, dy)) < r2) {
-          q = (int)pid(P, i, j, P.nz - 1);
-          got = claim(S, q, X.stamp);
+  int lo = 0, hi = ns - 1;                 // the answer lies in [lo, hi]
+  while (lo < hi) {
+    const int step = (hi - lo + 32) / 32;  // probes lo, lo + step, ... cover [lo, hi]
+    const int idx = min(lo + lane * step, hi);
+    const unsigned m = __ballot_sync(0xffffffffu, __ldg(&path[idx].tend) >= t);
+    if (m == 0u) { lo = min(lo + 31 * step, hi) + 1; if (lo > hi) lo = hi; continue; }
+    const int f = __ffs(m) - 1;
+    const int top = min(lo + f * step, hi);
+    lo = f == 0 ? lo : min(lo + (f - 1) * step, hi) + 1;
+    hi = top;
+    if (step == 1) lo = hi;
+  }
+  return lo;
+}
+
+// Surface points of one grid edge within the trace radius of an anchor outside the grid
+// (the perimeter lambda of src/Melt.cpp:36-55).  Only points whose distance along the edge
+// can be below the radius are tested - a window of +-(r / res + 2) points around the
+// anchor's projection - with the reference's exact FP64 test.
+template <class Sink>
+__device__ void perimeter_edge(const DevProblem& P, bool xfixed, int fixed, double x, double y, double r2,
+                               Sink& sink) {
+  const int lane = threadIdx.x & 31;
+  const int hi = xfixed ? P.ny : P.nx;
+  const double c = xfixed ? (y - P.ymin) / P.yres : (x - P.xmin) / P.xres;
+  const double w = sqrt(r2) / (xfixed ? P.yres : P.xres) + 2.0;
+  const int v_lo = (int)fmin(fmax(0.0, floor(c - w)), (double)hi);
+  const int v_hi = (int)fmax(fmin((double)hi, ceil(c + w) + 1.0), 0.0);
+  for (int v0 = v_lo; v0 < v_hi; v0 += 32) {
+    const int v = v0 + lane;
+    bool has = false;
+    int q = 0;
+    if (v < v_hi) {
+      const int i = xfixed ? fixed : v, j = xfixed ? v : fixed;
+      const double dx = rn_sub(rn_add(P.xmin, rn_mul((double)i, P.xres)), x);
+      const double dy = rn_sub(rn_add(P.ymin, rn_mul((double)j, P.yres)), y);
+      if (rn_add(rn_mul(dx, dx), rn_mul(dy, dy)) < r2) { q = (int)pid(P, i, j, P.nz - 1); has = true; }
+    }
+    sink(has, q);
+  }
+}
+
+// Melt::beam_trace for (t - dt, t] (src/Melt.cpp:20-183): every surface point the trace
+// tests, handed to the sink (warp-collective; claims are taken by the consumer).  The
+// anchors of a beam (segment end points in the window, then the beam's position) are
+// handled one per lane; perimeter scans (anchors outside the grid, src/Melt.cpp:62-77) and
+// the 2 x 2 surface cells at and after anchors inside it (src/Melt.cpp:122-146) follow.
+template <class Sink>
+__device__ void beam_trace(const DevProblem& P, double t_end, Sink& sink) {
+  const int lane = threadIdx.x & 31;
+  const double t_start = rn_sub(t_end, P.dt);
+  for (int b = 0; b < P.nbeams; ++b) {
+    const DevBeam& B = P.beam[b];
+    const DevSeg* path = P.segs + B.seg_off;
+    const double ts = (rn_sub(t_end, B.tsub) < 0.0) ? 0.0 : rn_sub(t_end, B.tsub);
+    const int s1 = warp_first_ge(path, B.nseg, t_end);
+    const int s0 = warp_first_ge(path, B.nseg, ts);
+    const int c0 = warp_first_ge(path, B.nseg, t_start);
+    const bool moving = path[s1].mode == 0 && t_end < B.tlast;
+    for (int pass = 0; pass < 2; ++pass) {    // 0: perimeter anchors from ts, 1: cell anchors from t_start
+      const int first = max((pass == 0 ? s0 : c0) - 1, 0);
+      const int na = s1 - first + 1 + (moving ? 1 : 0);
+      for (int a0 = 0; a0 < na; a0 += 32) {
+        const int a = a0 + lane;
+        double x = 0.0, y = 0.0;
+        int xg = 0, yg = 0;
+        if (a < na) {
+          if (first + a <= s1) { x = __ldg(&path[first + a].x); y = __ldg(&path[first + a].y); }
+          else { const BeamLoc L = beam_loc(P, path, t_end, s1); x = L.x; y = L.y; }
+          xg = (int)floor(rn_div(rn_sub(x, P.xmin), P.xres));
+          yg = (int)floor(rn_div(rn_sub(y, P.ymin), P.yres));
+        }
+        const bool inside = !(xg < 0 || xg > P.nx - 1 || yg < 0 || yg > P.ny - 1);
+        if (pass == 0) {
+          unsigned todo = __ballot_sync(0xffffffffu, a < na && !inside);
+          while (todo) {
+            const int src = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const double ax = __shfl_sync(0xffffffffu, x, src), ay = __shfl_sync(0xffffffffu, y, src);
+            const int gx = __shfl_sync(0xffffffffu, xg, src), gy = __shfl_sync(0xffffffffu, yg, src);
+            if (gx < 0) perimeter_edge(P, true, 0, ax, ay, B.r2, sink);
+            if (gx > P.nx - 1) perimeter_edge(P, true, P.nx - 1, ax, ay, B.r2, sink);
+            if (gy < 0) perimeter_edge(P, false, 0, ax, ay, B.r2, sink);
+            if (gy > P.ny - 1) perimeter_edge(P, false, P.ny - 1, ax, ay, B.r2, sink);
+          }
+        } else {
+          // eight anchors per round, four lanes each
+          const unsigned in_m = __ballot_sync(0xffffffffu, a < na && inside);
+          for (int g = 0; g < 32 && (in_m >> g) != 0u; g += 8) {
+            const int src = g + (lane >> 2);
+            const int gx = __shfl_sync(0xffffffffu, xg, src), gy = __shfl_sync(0xffffffffu, yg, src);
+            bool has = false;
+            int q = 0;
+            if ((in_m >> src) & 1u) {
+              const int i = gx + ((lane & 3) >> 1), j = gy + (lane & 1);
+              if (!(i < 0 || i > P.nx - 1 || j < 0 || j > P.ny - 1)) { q = (int)pid(P, i, j, P.nz - 1); has = true; }
+            }
+            sink(has, q);
+          }
         }
       }
-      emit(S, X, got, IT_VISIT, q, 0, nchild);
     }
   }
 }
 
-// The 2 x 2 surface cells at and after an anchor inside the grid (src/Melt.cpp:122-146).
-__device__ void cell(const DevProblem& P, const TrackState& S, const StepCtx& X, double x, double y, int& nchild) {
-  const int lane = threadIdx.x & 31;
-  const int xg = (int)floor(rn_div(rn_sub(x, P.xmin), P.xres));
-  const int yg = (int)floor(rn_div(rn_sub(y, P.ymin), P.yres));
-  if (xg < 0 || xg > P.nx - 1 || yg < 0 || yg > P.ny - 1) return;
-  bool got = false;
-  int q = 0;
-  if (lane < 4) {
-    const int i = xg + (lane >> 1), j = yg + (lane & 1);
-    if (!(i < 0 || i > P.nx - 1 || j < 0 || j > P.ny - 1)) {
-      q = (int)pid(P, i, j, P.nz - 1);
-      got = claim(S, q, X.stamp);
+// Appends the trace's points to a slot's seed list (warp-collective; n counts past the cap).
+struct SeedSink {
+  int* out;
+  int cap;
+  int n;
+  __device__ void operator()(bool has, int q) {
+    const int lane = threadIdx.x & 31;
+    const unsigned m = __ballot_sync(0xffffffffu, has);
+    if (has) {
+      const int i = n + __popc(m & ((1u << lane) - 1u));
+      if (i < cap) out[i] = q;
     }
+    n += __popc(m);
   }
-  emit(S, X, got, IT_VISIT, q, 0, nchild);
-}
+};
 
-// Melt::beam_trace for (t - dt, t] (src/Melt.cpp:20-183), claims queued as visits.
-__device__ void beam_trace(const DevProblem& P, const TrackState& S, const StepCtx& X, int& nchild) {
-  const double t_end = X.t, t_start = rn_sub(X.t, P.dt);
-  for (int b = 0; b < P.nbeams; ++b) {
-    const DevBeam& B = P.beam[b];
-    const DevSeg* path = P.segs + B.seg_off;
-    const double rc2 = rn_mul(P.rcheck, P.rcheck);
-    const double tsub = rn_div(rn_mul(rn_sub(rc2, 1.0), B.ax2), rn_mul(12.0, P.a));
-    const double ts = (rn_sub(t_end, tsub) < 0.0) ? 0.0 : rn_sub(t_end, tsub);
-    const double r2 = rn_mul(rn_mul(rc2, B.ax), B.ax);
-    const int s0 = first_ge(path, B.nseg, ts), s1 = first_ge(path, B.nseg, t_end);
-    for (int s = max(s0 - 1, 0); s <= s1; ++s) perimeter(P, S, X, path[s].x, path[s].y, r2, nchild);
-    if (path[s1].mode == 0 && t_end < B.tlast) {
-      const BeamLoc L = beam_loc(P, path, t_end, s1);
-      perimeter(P, S, X, L.x, L.y, r2, nchild);
-    }
-  }
-  for (int b = 0; b < P.nbeams; ++b) {
-    const DevBeam& B = P.beam[b];
-    const DevSeg* path = P.segs + B.seg_off;
-    const int s0 = first_ge(path, B.nseg, t_start), s1 = first_ge(path, B.nseg, t_end);
-    for (int s = max(s0 - 1, 0); s <= s1; ++s) cell(P, S, X, path[s].x, path[s].y, nchild);
-    if (path[s1].mode == 0 && t_end < B.tlast) {
-      const BeamLoc L = beam_loc(P, path, t_end, s1);
-      cell(P, S, X, L.x, L.y, nchild);
+// ------------------------------------------------------------------ node windows
+__global__ void __launch_bounds__(kGenThreads) k_nodes_window(DevProblem P, NodeWindow w, int first, int n, int is_sol,
+                                                              int* err) {
+  __shared__ GenShared sh;
+  const int slot = first + blockIdx.x;
+  const NodeBufView nb = slot_view(w, slot);
+  gen_list_block(P, w.t[slot], is_sol != 0, nb, &w.count[slot], err, sh);
+  if (P.tracking != TH_TRACK_NONE && threadIdx.x < 32) {   // the step's beam-trace candidates
+    SeedSink sink{w.seeds + (size_t)slot * w.seed_cap, w.seed_cap, 0};
+    beam_trace(P, w.t[slot], sink);
+    if (threadIdx.x == 0) {
+      w.nseed[slot] = sink.n;
+      if (sink.n > w.seed_cap) atomicOr(err, ERR_SEED_CAPACITY);
     }
   }
 }
 
 // Depth walk under a liquid surface point and the running depth maximum
-// (src/Melt.cpp:271-357): walk down while liquid, else walk up solidifying.
+// (src/Melt.cpp:271-357): walk down while liquid, else walk up solidifying.  The walk is
+// sequential in the reference; here the layers it is likely to visit are evaluated four
+// at a time ahead of it - the caller's first pass already holds D + 1, D + 2 (down) and
+// D (up) - and only the layers the walk reaches are committed.  T at a layer does not
+// depend on the walk.
 template <int PREC>
-__device__ void depth_walk(const DevProblem& P, const TrackState& S, const StepCtx& X, int p,
-                           unsigned long long& pairs) {
+__device__ void depth_walk(const DevProblem& P, const TrackState& S, const StepCtx& X, int p, int D,
+                           const EvalT (&first)[4], unsigned long long& pairs) {
   const int lane = threadIdx.x & 31;
   const int col = p / P.nz;
-  const int D = ldcg_i(S.depths + col);
+  const int top = col * P.nz + (P.nz - 1);            // layer d of the column is point top - d
+  EvalT Tc[4], Tu[4];
+  int cb = D + 1, cn = (D + 1 <= P.nz - 1) ? ((D + 2 <= P.nz - 1) ? 2 : 1) : 0;   // down: cb..cb+cn-1
+  int ub = D, un = D >= 1 ? 1 : 0;                                                   // up: ub..ub-un+1
+  Tc[0] = first[1]; Tc[1] = first[2]; Tu[0] = first[3];
   int d = D;
   bool none_deeper = true;
   while (true) {
     ++d;
     if (d == P.nz) break;
-    const int q = col * P.nz + (P.nz - 1 - d);
-    const double T = warp_T<PREC>(P, X.nb, X.nn, q);
+    if (d >= cb + cn) {                               // next four layers down
+      int pts[4];
+      cn = 0;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const bool ok = d + q <= P.nz - 1;
+        pts[q] = ok ? top - (d + q) : p;
+        cn += ok ? 1 : 0;
+      }
+      cb = d;
+      eval_T4<PREC>(P, S, X, pts, Tc);
+    }
+    const EvalT T = Tc[d - cb];
     pairs += X.nn;
-    if (lane == 0) set_T(S, P, q, T, X.k);
-    if (!(T >= P.TL)) break;
+    if (lane == 0) set_T(S, top - d, T, X.k);
+    if (!T.liquid) break;
     none_deeper = false;
   }
   while (true) {
     --d;
     if (d == 0 || !none_deeper) break;
-    const int q = col * P.nz + (P.nz - 1 - d);
+    if (!(d <= ub && d > ub - un)) {                  // next four layers up
+      int pts[4];
+      un = 0;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const bool ok = d - q >= 1;
+        pts[q] = ok ? top - (d - q) : p;
+        un += ok ? 1 : 0;
+      }
+      ub = d;
+      eval_T4<PREC>(P, S, X, pts, Tu);
+    }
+    const int q = top - d;
     const double Told = ldcg_d(S.T + q);
-    const double T = warp_T<PREC>(P, X.nb, X.nn, q);
+    const EvalT T = Tu[ub - d];
     pairs += X.nn;
-    if (lane == 0) set_T(S, P, q, T, X.k);
-    if (!(T >= P.TL)) {
+    if (lane == 0) set_T(S, q, T, X.k);
+    if (!T.liquid) {
       double Tl = Told;                                   // T of the previous step
-      if (d != D) { Tl = warp_T<PREC>(P, X.nbl, X.nnl, q); pairs += X.nnl; }
-      if (lane == 0) push_record(S, q, X.k, X.t, T, Tl);
+      if (d != D) { Tl = eval_T<PREC>(P, S, X, X.nbl, X.nnl, q, kNoStage).T; pairs += X.nnl; }
+      if (lane == 0) push_rec(S, X, q, T.T, Tl);
     } else {
       break;
     }
@@ -377,30 +676,43 @@ __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx&
                         unsigned long long& pairs) {
   const int lane = threadIdx.x & 31;
   int nchild = 0;
-  if (type == IT_SEEDS) {
-    beam_trace(P, S, X, nchild);
-    return nchild;
-  }
-  if (type == IT_DEPTH) {
-    depth_walk<PREC>(P, S, X, p, pairs);
-    return 0;
-  }
   const double Told = ldcg_d(S.T + p);
-  const double T = warp_T<PREC>(P, X.nb, X.nn, p);
-  pairs += X.nn;
-  if (lane == 0) set_T(S, P, p, T, X.k);
-  const bool liquid = T >= P.TL;
   if (type == IT_COLUMN) {                 // a layer under a surface point that solidified
+    const EvalT T = eval_T<PREC>(P, S, X, X.nb, X.nn, p, X.st);
+    pairs += X.nn;
+    if (lane == 0) set_T(S, p, T, X.k);
     double Tl = Told;
-    if (aux) { Tl = warp_T<PREC>(P, X.nbl, X.nnl, p); pairs += X.nnl; }
-    if (lane == 0) push_record(S, p, X.k, X.t, T, Tl);
+    if (aux) { Tl = eval_T<PREC>(P, S, X, X.nbl, X.nnl, p, kNoStage).T; pairs += X.nnl; }
+    if (lane == 0) push_rec(S, X, p, T.T, Tl);
     return 0;
   }
-  if (type == IT_RETEST && !liquid) {      // cooled below T_L since the last step
-    if (lane == 0) push_record(S, p, X.k, X.t, T, Told);
+  // Surface re-tests expand whatever their temperature (src/Run.cpp:655): claim first, so
+  // the neighbours' items start while this point is evaluated.
+  if (SURF && type == IT_RETEST) expand<SURF>(P, S, X, p, nchild);
+  EvalT T4[4];
+  int D = 0;
+  if (SURF) {                              // the point and the layers its depth walk starts with
+    const int col = p / P.nz, top = col * P.nz + (P.nz - 1);
+    D = ldcg_i(S.depths + col);
+    const int pts[4] = {p, D + 1 <= P.nz - 1 ? top - (D + 1) : p, D + 2 <= P.nz - 1 ? top - (D + 2) : p,
+                        D >= 1 ? top - D : p};
+    eval_T4<PREC>(P, S, X, pts, T4);
+  } else {
+    T4[0] = eval_T<PREC>(P, S, X, X.nb, X.nn, p, X.st);
+  }
+  const EvalT T = T4[0];
+  pairs += X.nn;
+  if (lane == 0) set_T(S, p, T, X.k);
+  if (T.liquid) {
+    // Volume expands the liquid points; Surface the liquid visits (re-tests did above)
+    if (!(SURF && type == IT_RETEST)) expand<SURF>(P, S, X, p, nchild);
+    // the depth walk under a liquid surface point needs nothing else from this step
+    if (SURF) depth_walk<PREC>(P, S, X, p, D, T4, pairs);
+    if (lane == 0) push_liquid(S, X, p);
+  } else if (type == IT_RETEST) {          // cooled below T_L since the last step
+    if (lane == 0) push_rec(S, X, p, T.T, Told);
     if (SURF) {
       const int col = p / P.nz;
-      const int D = ldcg_i(S.depths + col);
       for (int d0 = 1; d0 <= D; d0 += 32) {
         const int d = d0 + lane;
         emit(S, X, d <= D, IT_COLUMN, col * P.nz + (P.nz - 1 - d), d != D, nchild);
@@ -408,11 +720,6 @@ __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx&
       if (lane == 0) S.depths[col] = 0;
     }
   }
-  if (liquid && lane == 0) push_liquid(S, X, p);
-  // Surface expands every re-tested point, Volume only the liquid ones (src/Run.cpp:655, 531)
-  if (liquid || (SURF && type == IT_RETEST)) expand<SURF>(P, S, X, p, nchild);
-  // the depth walk under a liquid surface point needs nothing else from this step
-  if (SURF && liquid) depth_walk<PREC>(P, S, X, p, pairs);
   return nchild;
 }
 
@@ -424,58 +731,105 @@ constexpr int kTrackThreads = 128;   // four warps per block, one block per SM
 // item that any warp may take; a packed (published << 32 | completed) counter tells the
 // warps when the step has no work left, and one grid barrier ends the step.
 template <int PREC, bool SURF>
-__global__ void __launch_bounds__(kTrackThreads) k_track(DevProblem P, TrackState S, NodeWindow W, int k_begin,
-                                                        int k_end, int high_water) {
+__global__ void __launch_bounds__(kTrackThreads, 1) k_track(DevProblem P, TrackState S, NodeWindow W, int k_begin,
+                                                            int k_end, int high_water, int stage_cap) {
+  extern __shared__ __align__(16) unsigned char stage_mem[];
+  __shared__ BlockBuf bbuf;
   const int lane = threadIdx.x & 31;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n_warps = (gridDim.x * blockDim.x) >> 5;
   TrackCounters* C = S.C;
   unsigned long long pairs = 0;
-  for (int k = k_begin; k < k_end; ++k) {
+  const size_t buf_bytes = (size_t)stage_cap * staged_bytes_per_node<PREC>();
+  if (threadIdx.x == 0) bbuf.nrec = 0;
+  if (k_begin < k_end) {                    // the first step's list; later ones are prefetched
+    const int slot = k_begin - W.base + 1;
+    stage_issue<PREC>(slot_view(W, slot), min(W.count[slot], stage_cap), stage_mem + (k_begin & 1) * buf_bytes,
+                      stage_cap);
+  }
+  unsigned long long t_work = 0, n_items = 0, c_items = 0, c_wait = 0, depth_sum = 0;
+  unsigned long long ev_n = 0, ev_c = 0, lvl_s[4] = {0, 0, 0, 0}, lvl_e[4] = {0, 0, 0, 0};
+  int k = k_begin;
+  for (; k < k_end; ++k) {
+    // this step's list has landed in every thread's share; the block's warps have all left
+    // the previous step
+    cp_async_wait_all();
+    if (__syncthreads_or(threadIdx.x == 0 && bbuf.nrec >= kBlkRec / 2)) flush_block(S, &bbuf, S.rec_n);
     StepCtx X;
+    X.ev_n = 0;
+    X.ev_c = 0;
     const int slot = k - W.base + 1;
-    X.k = k;
+    const unsigned long long g0 = globaltimer();
+    int max_depth = 0;
+    const int b0 = k % 3, b1 = (k + 1) % 3;
+    X.qc = &C->q[b0];
     X.stamp = (unsigned)k + 1u;
+    X.nL = ldcg_i(&C->liq_n[b0]);
+    // the beam trace runs for k > 0 while t < end + dt (src/Run.cpp:661)
+    X.t = W.t[slot];
+    const bool seeds = k > 0 && X.t < P.end_time + P.dt;
+    const int n_seed = seeds ? min(W.nseed[slot], W.seed_cap) : 0;
+    const int* seed = W.seeds + (size_t)slot * W.seed_cap;
+    X.n_init = X.nL + n_seed;
+    if (k + 1 < k_end)                      // next step's list, copied while this step runs
+      stage_issue<PREC>(slot_view(W, slot + 1), min(W.count[slot + 1], stage_cap),
+                        stage_mem + ((k + 1) & 1) * buf_bytes, stage_cap);
+    X.bb = &bbuf;
+    X.st.base = stage_mem + (k & 1) * buf_bytes;
+    X.st.cap = stage_cap;
+    X.st.n_sm = min(W.count[slot], stage_cap);
+    X.k = k;
     X.nb = slot_view(W, slot);
     X.nbl = slot_view(W, slot - 1);
-    X.nn = W.count[slot];
-    X.nnl = (k == 0) ? 0 : W.count[slot - 1];
-    X.t = W.t[slot];
-    const int b0 = k % 3, b1 = (k + 1) % 3, b2 = (k + 2) % 3;
-    X.nL = ldcg_i(&C->liq_n[b0]);
+    X.nn = min(W.count[slot], W.slot_cap);
+    X.nnl = (k == 0) ? 0 : min(W.count[slot - 1], W.slot_cap);
     X.L = S.liq[b0];
     X.Lo = S.liq[b1];
     X.lo_n = &C->liq_n[b1];
-    X.qc = &C->q[b0];
-    const bool seeds = k > 0 && X.t < P.end_time + P.dt;
-    X.n_init = X.nL + (seeds ? 1 : 0);
-    if (tid == 0) {                       // buffers of the step after next
-      C->liq_n[b2] = 0;
-      C->q[b1].head = 0; C->q[b1].state = 0ull;
+    if (threadIdx.x == 0) {                 // this block has entered the step
+      const unsigned long long st = atomicAdd(&X.qc->state, kArrive);
+      if (step_over(st + kArrive, X.n_init, gridDim.x)) finish_step(P, S, X, k, st + kArrive, high_water);
     }
-    // the work loop
+    // The work loop.  The step's initial items - re-tests of the previous liquid points,
+    // then the beam trace's candidates - are dealt to the warps in order (warp w takes
+    // w, w + warps, ...), so they all start at once; items published during the step are
+    // taken with tickets from the queue.  The step is over when every block has entered
+    // it and every item has completed; whoever's update of the step word makes that true
+    // resets the counters the next steps use and publishes the step's stamp, which the
+    // waiting warps see.  No grid barrier separates steps.
+    int next_init = tid >> 5;
     long long idle = 0;
     while (true) {
-      unsigned ticket = 0;
-      if (lane == 0) ticket = atomicAdd(&X.qc->head, 1u);
-      ticket = __shfl_sync(0xffffffffu, ticket, 0);
+      const long long c0 = clock64();
       int type, p = 0, aux = 0;
-      if (ticket < (unsigned)X.nL) {
-        type = IT_RETEST;
-        p = __ldcg(X.L + ticket);
-      } else if (ticket < (unsigned)X.n_init) {
-        type = IT_SEEDS;
+      bool run = true;
+      if (next_init < X.n_init) {
+        const int t = next_init;
+        next_init += n_warps;
+        X.depth = 0;
+        if (t < X.nL) {
+          type = IT_RETEST;
+          p = __ldcg(X.L + t);
+        } else {                            // a trace candidate: visited if this claim takes it
+          type = IT_VISIT;
+          p = __ldg(seed + (t - X.nL));
+          bool got = false;
+          if (lane == 0) got = claim(S, p, X.stamp);
+          run = __shfl_sync(0xffffffffu, got, 0);
+        }
       } else {
-        const unsigned j = ticket - (unsigned)X.n_init;
+        unsigned ticket = 0;
+        if (lane == 0) ticket = atomicAdd(&X.qc->head, 1u);
+        ticket = __shfl_sync(0xffffffffu, ticket, 0);
+        const unsigned j = ticket;
         bool ready = false, finished = false;
         unsigned backoff = 8;
+        ulonglong2 it = make_ulonglong2(0ull, 0ull);
         while (true) {
           if (lane == 0) {
-            const int tag = (j < (unsigned)S.queue_cap) ? ld_acquire_s32(&S.queue[j].x) : 0;
-            ready = tag == (int)X.stamp;
-            if (!ready) {
-              const unsigned long long st = ld_relaxed_u64(&X.qc->state);
-              finished = (unsigned)(st & 0xffffffffu) == (unsigned)X.n_init + (unsigned)(st >> 32);
-            }
+            if (j < (unsigned)S.queue_cap) it = ld_relaxed_v2(S.queue + j);
+            ready = (unsigned)(it.x >> 32) == X.stamp && (unsigned)(it.y >> 32) == X.stamp;
+            if (!ready) finished = ld_acquire_u32(&C->finished) >= X.stamp;
           }
           ready = __shfl_sync(0xffffffffu, ready, 0);
           finished = __shfl_sync(0xffffffffu, finished, 0);
@@ -486,36 +840,78 @@ __global__ void __launch_bounds__(kTrackThreads) k_track(DevProblem P, TrackStat
               if (atomicOr(S.err, ERR_BARRIER) == 0) {        // first waiter to give up records its view
                 const unsigned long long st = ld_relaxed_u64(&X.qc->state);
                 int* g = S.C->diag;
-                g[0] = 1; g[1] = k; g[2] = (int)ticket; g[3] = X.n_init;
-                g[4] = (int)*(volatile unsigned*)&X.qc->head; g[5] = (int)(st >> 32);
-                g[6] = (int)(st >> 32); g[7] = (int)(st & 0xffffffffu);
+                g[0] = 1; g[1] = k; g[2] = (int)j; g[3] = X.n_init;
+                g[4] = (int)*(volatile unsigned*)&X.qc->head; g[5] = (int)(st >> 48);
+                g[6] = (int)((st >> 24) & kField); g[7] = (int)(st & kField);
               }
+              st_release_u32(&C->finished, 0xffffffffu);     // let every warp leave
             }
             finished = true;
             break;
           }
           __nanosleep(backoff);
         }
-        if (!ready) break;
-        const int4 it = __ldcg(S.queue + j);
-        type = it.y; p = it.z; aux = it.w;
+        if (!ready) { c_wait += clock64() - c0; break; }
+        const unsigned w0 = __shfl_sync(0xffffffffu, (unsigned)it.x, 0);
+        const unsigned w1 = __shfl_sync(0xffffffffu, (unsigned)it.y, 0);
+        p = (int)w0;
+        type = w1 & 0xff;
+        X.depth = (w1 >> 8) & 0xff;
+        aux = (int)(w1 >> 16);
       }
-      run_item<PREC, SURF>(P, S, X, type, p, aux, pairs);
+      const long long c1 = clock64();
+      c_wait += c1 - c0;
+      if (X.depth > max_depth) {
+        max_depth = X.depth;
+        if (lane == 0) atomicMax(&X.qc->depth, (unsigned)max_depth);
+      }
+      const unsigned long long g_item = globaltimer();
+      if (run) run_item<PREC, SURF>(P, S, X, type, p, aux, pairs);
+      if (lane == 0) {
+        const int l = min(X.depth, 3);
+        atomicMax(&X.qc->lvl_start[l], (unsigned)(g_item - g0));
+        atomicMax(&X.qc->lvl_end[l], (unsigned)(globaltimer() - g0));
+      }
       __threadfence();
-      if (lane == 0) atomicAdd(&X.qc->state, 1ull);             // completed
+      if (lane == 0) {                                           // completed
+        const unsigned long long st = atomicAdd(&X.qc->state, 1ull);
+        if (step_over(st + 1ull, X.n_init, gridDim.x)) finish_step(P, S, X, k, st + 1ull, high_water);
+      }
+      ++n_items;
+      c_items += clock64() - c1;
     }
-    if (!grid_sync(S)) return;
-    // finish test (src/Util.cpp:239-243) and the record queue's high-water mark
-    const int nLo = ldcg_i(X.lo_n);
+    t_work += globaltimer() - g0;
+    ev_n += X.ev_n;
+    ev_c += X.ev_c;
+    // every warp of the block takes the same decision: an abort after a bounded wait, or
+    // the step's verdict (which stays until this block has entered the next step)
+    if (__syncthreads_or(ld_acquire_u32(&C->finished) == 0xffffffffu)) break;
+    const unsigned verdict = ld_acquire_u32(&C->verdict);
     if (tid == 0) {
-      C->step = k + 1;
-      const unsigned items = (unsigned)(__ldcg(&X.qc->state) >> 32) + (unsigned)X.n_init;
-      if ((int)items > C->max_items) C->max_items = (int)items;
+      depth_sum += __ldcg(&X.qc->depth);
+      for (int l = 0; l < 4; ++l) {
+        lvl_s[l] += __ldcg(&X.qc->lvl_start[l]);
+        lvl_e[l] += __ldcg(&X.qc->lvl_end[l]);
+      }
     }
-    if (X.t > P.end_time && nLo == 0) { if (tid == 0) C->done = 1; break; }
-    if (ldcg_i(S.rec_n) > high_water) { if (tid == 0) C->stop = 1; break; }
+    if (verdict & 3u) { ++k; break; }
   }
+  cp_async_wait_all();
+  flush_block(S, &bbuf, S.rec_n);
   if (lane == 0 && pairs) atomicAdd(S.pairs, pairs);
+  if (lane == 0) {
+    atomicAdd(&C->prof[2], n_items);
+    atomicAdd(&C->prof[3], c_items);
+    atomicAdd(&C->prof[4], c_wait);
+    atomicAdd(&C->prof[7], ev_n);
+    atomicAdd(&C->prof[8], ev_c);
+  }
+  if (tid == 0) {
+    atomicAdd(&C->prof[0], t_work);
+    atomicAdd(&C->prof[5], depth_sum);
+    atomicAdd(&C->prof[6], (unsigned long long)(k - k_begin));
+    for (int l = 0; l < 4; ++l) { atomicAdd(&C->prof[10 + l], lvl_s[l]); atomicAdd(&C->prof[14 + l], lvl_e[l]); }
+  }
 }
 
 // ------------------------------------------------------------------ NoTracking
@@ -744,14 +1140,21 @@ static cudaError_t launch_track_t(const DevProblem& P, const TrackState& S, cons
   int dev = 0, sms = 0, occ = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_track<PREC, SURF>, kTrackThreads, 0);
+  // stage whole lists up to the slot capacity, within 200 KB of shared memory for both buffers
+  int cap = std::min(w.slot_cap, (200 * 1024) / (2 * staged_bytes_per_node<PREC>()));
+  cap = std::max(8, cap & ~7);
+  const size_t smem = (size_t)2 * cap * staged_bytes_per_node<PREC>();
+  cudaError_t e = cudaFuncSetAttribute(k_track<PREC, SURF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_track<PREC, SURF>, kTrackThreads, smem);
   const int blocks = sms * (occ < 1 ? occ : 1);
   if (blocks <= 0) return cudaErrorInvalidConfiguration;
   DevProblem Pc = P;
   TrackState Sc = S;
   NodeWindow Wc = w;
-  void* args[] = {&Pc, &Sc, &Wc, &k_begin, &k_end, &hw};
-  return cudaLaunchCooperativeKernel((const void*)k_track<PREC, SURF>, dim3(blocks), dim3(kTrackThreads), args, 0, s);
+  void* args[] = {&Pc, &Sc, &Wc, &k_begin, &k_end, &hw, &cap};
+  return cudaLaunchCooperativeKernel((const void*)k_track<PREC, SURF>, dim3(blocks), dim3(kTrackThreads), args, smem,
+                                     s);
 }
 
 cudaError_t th_launch_track(const DevProblem& P, const TrackState& S, const NodeWindow& w, int k_begin, int k_end,

@@ -21,22 +21,36 @@ struct SolRec {
 // Per-step counters; one struct in device memory.  Lists rotate over three buffers by
 // step (k % 3: this step's liquid list, (k + 1) % 3: the next one, (k + 2) % 3: being
 // cleared), so no buffer is reset while another block may still read it.
-struct QueueCounters {
+//
+// The counters that every warp touches live on separate 128-byte lines: the ticket
+// counter, the published/completed word, and the finished-step stamp that idle warps poll,
+// so the polling never queues behind the atomics.
+struct alignas(128) QueueCounters {
   unsigned head;                 // tickets taken
-  unsigned unused;
+  unsigned depth;                // longest parent -> child chain of the step's items
+  unsigned lvl_start[4];         // latest start / end (ns after the step began) of the items of
+  unsigned lvl_end[4];           // chain depth 0, 1, 2, >= 3 (profile)
+  unsigned pad0[22];
   unsigned long long state;      // (dynamic items published << 32) | items completed; the
                                  // published count also hands out the items' queue slots
-  unsigned pad[4];
+  unsigned long long pad1[15];
 };
 
-struct TrackCounters {
-  int liq_n[3];     // liquid list lengths
-  int rec_n[2];     // solidification records queued in each of the two record buffers
+struct alignas(128) TrackCounters {
   int step;         // next step to run
   int done;         // finish test passed
   int stop;         // the loop stopped early (record queue high-water mark)
   int max_items;    // most work items in one step
   int diag[8];      // where a bounded wait gave up: kind, step, ticket, n_init, head, tail, published, completed
+  // loop profile: block 0's work-phase and barrier time (ns), items run, item and wait
+  // time summed over warps (SM clocks), summed per-step chain depth, steps profiled,
+  // point evaluations and their SM clocks summed over warps, then the per-step latest
+  // start and end of items of chain depth 0..3 (ns) summed over steps
+  unsigned long long prof[18];
+  alignas(128) int liq_n[3];     // liquid list lengths
+  alignas(128) int rec_n[2];     // solidification records queued in each of the two record buffers
+  alignas(128) unsigned finished;// k + 1 once step k is over (0xffffffff: aborted by a bounded wait)
+  unsigned verdict;              // (k + 1) << 2 | 1 finished run | 2 record high-water mark
   QueueCounters q[3];
 };
 
@@ -55,12 +69,13 @@ struct TrackState {
   double* depth_max;       // per column
   int* liq[3];
   int list_cap;
-  int4* queue;             // work items {tag, type, point, aux}
+  ulonglong2* queue;       // work items {stamp << 32 | point, stamp << 32 | type | depth << 8 | aux << 16}
   int queue_cap;
   SolRec* rec;             // the record buffer this launch appends to
   int* rec_n;              // and its length (one of TrackCounters::rec_n)
   int rec_cap;
   TrackCounters* C;
+  const float2* axis;      // grid coordinates as (hi, lo) floats: x[0, nx), y[nx, nx + ny), z after
   unsigned* bar;           // grid barrier: [0] arrivals, [1] generation
   int* err;
   unsigned long long* pairs;
@@ -74,7 +89,15 @@ struct NodeWindow {
   int* count;              // per slot
   const double* t;         // per slot
   int base;                // step of slot 1
+  // beam-trace candidates of each slot's step (Volume / Surface tracking): surface points
+  // the trace would test, before the claim; nseed[slot] may exceed seed_cap (overflow)
+  int* seeds;              // slot-major, seed_cap per slot
+  int* nseed;
+  int seed_cap;
 };
+
+// Error bits of a window build (with the node bits 1 = node capacity, 2 = walk limit).
+enum { ERR_SEED_CAPACITY = 4 };
 
 // Error bits written by the solidification kernels (besides the node bits).
 enum { ERR_BARRIER = 16, ERR_RECORDS = 32, ERR_LISTS = 64, ERR_QUEUE = 128 };

@@ -208,6 +208,18 @@ def run_solidification(args, th, torch, dev, path, deck, world):
               "ms_tracking": st["ms_track"], "ms_solidify": st["ms_solidify"], "records": int(st["records"]),
               "max_items_per_step": int(st["max_items"]), "wall_s_per_step": statistics.median(wall),
               "device_s_per_step": statistics.median(dev_s)}
+    if st.get("loop_steps"):
+        n = st["loop_steps"]
+        detail["loop_profile"] = {
+            "us_work_per_timestep": 1e3 * st["loop_ms_work"] / n, "us_barrier_per_timestep": 1e3 * st["loop_ms_barrier"] / n,
+            "items_per_timestep": st["loop_items"] / n,
+            "us_per_item": st["loop_item_clocks"] / max(1, st["loop_items"]) / clk_mhz,
+            "us_waiting_per_warp_timestep": st["loop_wait_clocks"] / n / clk_mhz / (SM_COUNT * 4),
+            "chain_depth_per_timestep": st["loop_depth_sum"] / n,
+            "evals_per_timestep": st["loop_evals"] / n,
+            "us_per_eval": st["loop_eval_clocks"] / max(1, st["loop_evals"]) / clk_mhz,
+            "us_latest_item_start_by_chain_depth": [1e3 * st[f"loop_ms_start{l}"] / n for l in range(4)],
+            "us_latest_item_end_by_chain_depth": [1e3 * st[f"loop_ms_end{l}"] / n for l in range(4)]}
     return {"value": value, "ms_per_step": 1e3 * total_s / args.steps, "e2e": e2e, "roofline": roof,
             "clocks": clk, "gpu_launches": launches * args.steps, "detail": detail}
 

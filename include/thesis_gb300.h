@@ -137,7 +137,13 @@ th_status th_run_reset(th_ctx* ctx);
  * node windows, ms in the tracking / NoTracking steps, ms solidifying records, windows,
  * records, most work items in one step (tracking), steps, node slots per step,
  * device-elapsed ms of th_solidify calls (host gaps included), point x node pairs of the
- * bulk solidification, all point x node pairs of the context. */
+ * bulk solidification, all point x node pairs of the context; then the tracking loop's
+ * profile: ms of block 0's work phases, ms of block 0's barrier waits, work items run,
+ * SM clocks spent in items and in waiting for items (summed over warps), the per-step
+ * longest parent -> child item chain summed over steps, steps profiled, point evaluations
+ * and their SM clocks summed over warps, then per chain depth 0, 1, 2, >= 3 the latest
+ * item start and the latest item end after the step began, in ms summed over steps
+ * (28 values). */
 th_status th_run_stats(th_ctx* ctx, double* out, int32_t n);
 
 /* Whole run as the reference CLI does it: the mode loop, then the CSV files under
