@@ -379,12 +379,14 @@ void th_make_dev_problem(const HostProblem& hp, const DevSeg* d_segs, DevProblem
     off += D.nseg;
   }
   dp.T0 = hp.T0; dp.TL = hp.TL; dp.a = hp.a; dp.a12 = 12.0 * hp.a;
-  {  // exact ceil((TL - T0) * 2^30): TL - T0 = s + e exactly (TwoSum), then ceil of (s + e) * 2^30
+  {  // TL - T0 = s + e exactly (TwoSum); s + e split into three floats
     const double s = hp.TL - hp.T0, bb = s - hp.TL;
     const double e = (hp.TL - (s - bb)) + (-hp.T0 - bb);
-    const double s30 = std::ldexp(s, 30), f = std::floor(s30);
-    const double r = (s30 - f) + std::ldexp(e, 30);
-    dp.tl_fix = (int64_t)f + (r > 1.0 ? 2 : (r > 0.0 ? 1 : 0));
+    const float f0 = (float)s;
+    const double r1 = (s - (double)f0) + e;
+    const float f1 = (float)r1;
+    const float f2 = (float)(r1 - (double)f1);
+    dp.tl_df[0] = f0; dp.tl_df[1] = f1; dp.tl_df[2] = f2;
   }
   dp.cetN0 = hp.cetN0; dp.cetn = hp.cetn; dp.ceta = hp.ceta;
   dp.nx = hp.nx; dp.ny = hp.ny; dp.nz = hp.nz;

@@ -37,7 +37,7 @@ struct DevProblem {
   DevBeam beam[TH_MAX_BEAMS];
   // material
   double T0, TL, a, a12;    // a12 = 12 * a
-  int64_t tl_fix;           // ceil((TL - T0) * 2^30): the liquidus in the FP32 tracking's fixed point
+  float tl_df[3];           // TL - T0 as three floats (hi + mid + lo), for the FP32 tracking's liquid test
   double cetN0, cetn, ceta;
   // domain
   int32_t nx, ny, nz;       // axis counts

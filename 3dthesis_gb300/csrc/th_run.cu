@@ -182,6 +182,7 @@ th_status init_run(th_ctx* ctx) {
                             "copy")) != TH_OK)
       return st;
     S.axis = r->d_axis;
+    S.t_fixed = (ctx->precision == TH_FP32_KAHAN && hp.tracking != TH_TRACK_NONE) ? 1 : 0;
   }
   S.pairs = ctx->d_pairs;
   S.rec = r->rec[0];

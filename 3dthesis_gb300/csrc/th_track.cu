@@ -43,69 +43,76 @@ __device__ __forceinline__ double warp_sum_d(double v) {
   return v;
 }
 
-// The current step's node list staged in shared memory (array-of-structures, one copy per
-// block): FP32 A = (xh, yh, zh, kx), B = (xl, yl, zl, ky), C = (kz, w); FP64 four double2
-// (x, y), (z, 1/phix), (1/phiy, 1/phiz), (dtau, amp).  Nodes at and beyond n_sm are read
-// from the window in global memory.
+// A step's node list staged in shared memory, one copy per block.  FP32: ten float arrays
+// of cap entries (xh, yh, zh, xl, yl, zl, kx, ky, kz, w), read two consecutive nodes at a
+// time; FP64: four double2 arrays (x, y), (z, 1/phix), (1/phiy, 1/phiz), (dtau, amp).
+// Nodes at and beyond n_sm are read from the window in global memory.
 struct Staged {
   const unsigned char* base;
   int n_sm;                // staged nodes
-  int cap;                 // nodes per staged array
+  int cap;                 // nodes per staged array (a multiple of 8)
 };
 
 template <int PREC>
 __host__ __device__ constexpr int staged_bytes_per_node() { return PREC == 0 ? 64 : 40; }
 
-__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
-               : "memory");
-}
 __device__ __forceinline__ void cp_async8(void* dst, const void* src) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
                : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-// Issues the block's asynchronous copies of the first m nodes of nb into buf (field-major
-// order, so consecutive threads read consecutive nodes of one field).
+// Issues the block's asynchronous copies of the first m nodes of nb into buf.  FP32 copies
+// whole 16-byte groups of four nodes (a slot's arrays start 128-byte aligned and hold a
+// multiple of 32 nodes, so the group that straddles m stays inside the slot).
 template <int PREC>
 __device__ __forceinline__ void stage_issue(const NodeBufView& nb, int m, unsigned char* buf, int cap) {
   if (PREC == 0) {
     const double* src[8] = {nb.x, nb.y, nb.z, nb.ipx, nb.ipy, nb.ipz, nb.dtau, nb.amp};
-    for (int i = threadIdx.x; i < 8 * m; i += blockDim.x) {
-      const int f = i / m, n = i - f * m;
-      double* dst = (double*)(buf + (size_t)(f >> 1) * cap * 16) + 2 * n + (f & 1);
-      cp_async8(dst, src[f] + n);
+#pragma unroll
+    for (int f = 0; f < 8; ++f) {
+      double* dst = (double*)(buf + (size_t)(f >> 1) * cap * 16) + (f & 1);
+      for (int n = threadIdx.x; n < m; n += blockDim.x) cp_async8(dst + 2 * n, src[f] + n);
     }
   } else {
-    const float* src[10] = {nb.xh, nb.yh, nb.zh, nb.kx, nb.xl, nb.yl, nb.zl, nb.ky, nb.kz, nb.w};
-    for (int i = threadIdx.x; i < 10 * m; i += blockDim.x) {
-      const int f = i / m, n = i - f * m;
-      float* dst = f < 8 ? (float*)(buf + (size_t)(f >> 2) * cap * 16) + 4 * n + (f & 3)
-                         : (float*)(buf + (size_t)cap * 32) + 2 * n + (f - 8);
-      cp_async4(dst, src[f] + n);
+    const float* src[10] = {nb.xh, nb.yh, nb.zh, nb.xl, nb.yl, nb.zl, nb.kx, nb.ky, nb.kz, nb.w};
+    const int groups = (m + 3) >> 2;
+#pragma unroll
+    for (int f = 0; f < 10; ++f) {
+      float* dst = (float*)(buf + (size_t)f * cap * 4);
+      for (int g = threadIdx.x; g < groups; g += blockDim.x) cp_async16(dst + 4 * g, src[f] + 4 * g);
     }
   }
   cp_async_commit();
 }
 
-// round(x * 2^30) as an integer, from the float's bits alone (no FP64 or conversion unit):
-// |x| below 2^32; values under 2^-31 give 0.
-__device__ __forceinline__ long long to_fix30(float x) {
-  const int b = __float_as_int(x);
-  const int e = (b >> 23) & 0xff;
-  const long long m = (long long)((b & 0x7fffff) | 0x800000);
-  const int sh = e - 120;                                // value = m * 2^(e - 150); times 2^30
-  long long v;
-  if (e == 0 || sh < -24) v = 0;
-  else if (sh >= 0) v = m << min(sh, 38);
-  else v = (m + (1ll << (-sh - 1))) >> -sh;
-  return b < 0 ? -v : v;
+// (hi, lo) += (bh, bl) in double-float: TwoSum of the heads, then the tails, renormalised
+// with Fast2Sum (Knuth; Dekker).  The result depends only on the two operands as a set
+// (TwoSum's error term is exact either way), so both lanes of a butterfly get the same bits.
+__device__ __forceinline__ void df_add(float& hi, float& lo, float bh, float bl) {
+  const float s = hi + bh;
+  const float v = s - hi;
+  float e = (hi - (s - v)) + (bh - v);
+  e += lo + bl;
+  hi = s + e;
+  lo = e - (hi - s);
 }
 
-// One evaluation's result: T, and T >= T_L decided exactly.
+// One evaluation's result: T as stored (a double in FP64 runs; in FP32 runs the sum T - T0
+// as a double-float pair (hi, lo) in the double's bits, decoded by t_decode), and T >= T_L.
 struct EvalT { double T; bool liquid; };
+
+// (hi, lo) packed for storage; a zero sum is stored with lo = -0 so that all-zero bits keep
+// meaning "never evaluated".
+__device__ __forceinline__ double pack_df(float hi, float lo) {
+  const unsigned l = (hi == 0.f && lo == 0.f) ? 0x80000000u : __float_as_uint(lo);
+  return __longlong_as_double((long long)(((unsigned long long)__float_as_uint(hi) << 32) | l));
+}
 
 // T at NP points from one node list, the 32 lanes of a warp splitting the nodes; every
 // lane returns the same values.  Each node is read once for all NP points, so a pass over
@@ -113,9 +120,10 @@ struct EvalT { double T; bool liquid; };
 //
 // FP32 form: the points' coordinates come as (hi, lo) float pairs from per-axis tables;
 // each lane sums its share with Kahan compensation; the lanes' results are reduced as
-// 64-bit fixed point (2^-30 K), which is exact and independent of the order, and the
-// liquid test is an integer comparison with ceil((T_L - T_0) 2^30).  No FP64 operation
-// sits on the evaluation's path; T itself is formed in FP64 once, for storing.
+// double-float pairs, and the liquid test compares that pair with T_L - T_0 split into
+// three floats.  No FP64 arithmetic or conversion sits on the evaluation's path: T is
+// stored as the pair and turned into a double only where fields and solidification times
+// are computed.
 template <int PREC, int NP>
 __device__ __forceinline__ void warp_T_n(const DevProblem& P, const TrackState& S, const NodeBufView& nb, int nn,
                                          const int (&pts)[NP], const Staged& st, EvalT (&out)[NP]) {
@@ -158,60 +166,108 @@ __device__ __forceinline__ void warp_T_n(const DevProblem& P, const TrackState& 
       out[q].liquid = out[q].T >= P.TL;
     }
   } else {
-    float2 X[NP], Y[NP], Z[NP];
-    float s[2][NP], c[2][NP];                    // two independent Kahan sums per point
+    // points as (v, v) pairs; per point one packed Kahan sum over node pairs (even nodes in
+    // the low half, odd in the high) and one scalar sum for the odd node and global tail
+    unsigned long long Xh[NP], Xl[NP], Yh[NP], Yl[NP], Zh[NP], Zl[NP], s2[NP], c2[NP];
+    float xh1[NP], xl1[NP], yh1[NP], yl1[NP], zh1[NP], zl1[NP], s1[NP], c1[NP];
 #pragma unroll
     for (int q = 0; q < NP; ++q) {
-      X[q] = __ldg(S.axis + pi[q]);
-      Y[q] = __ldg(S.axis + P.nx + pj[q]);
-      Z[q] = __ldg(S.axis + P.nx + P.ny + pk[q]);
-      s[0][q] = s[1][q] = 0.f;
-      c[0][q] = c[1][q] = 0.f;
+      const float2 X = __ldg(S.axis + pi[q]), Y = __ldg(S.axis + P.nx + pj[q]),
+                   Z = __ldg(S.axis + P.nx + P.ny + pk[q]);
+      xh1[q] = X.x; xl1[q] = X.y; yh1[q] = Y.x; yl1[q] = Y.y; zh1[q] = Z.x; zl1[q] = Z.y;
+      Xh[q] = pk2(X.x, X.x); Xl[q] = pk2(X.y, X.y);
+      Yh[q] = pk2(Y.x, Y.x); Yl[q] = pk2(Y.y, Y.y);
+      Zh[q] = pk2(Z.x, Z.x); Zl[q] = pk2(Z.y, Z.y);
+      s2[q] = c2[q] = 0ull;
+      s1[q] = c1[q] = 0.f;
     }
-    auto acc = [&](int h, float4 a, float4 b, float2 cc) {
+    auto acc1 = [&](float xh, float yh, float zh, float xl, float yl, float zl, float kx, float ky, float kz,
+                    float w) {
 #pragma unroll
       for (int q = 0; q < NP; ++q) {
-        const float dx = (X[q].x - a.x) + (X[q].y - b.x);
-        const float dy = (Y[q].x - a.y) + (Y[q].y - b.y);
-        const float dz = (Z[q].x - a.z) + (Z[q].y - b.z);
-        const float e = fmaf(dz * dz, cc.x, fmaf(dy * dy, b.w, dx * dx * a.w));
-        const float v = ex2_approx(e) * cc.y;
-        const float yy = v - c[h][q];
-        const float tt = s[h][q] + yy;
-        c[h][q] = (tt - s[h][q]) - yy;
-        s[h][q] = tt;
+        const float dx = (xh1[q] - xh) + (xl1[q] - xl);
+        const float dy = (yh1[q] - yh) + (yl1[q] - yl);
+        const float dz = (zh1[q] - zh) + (zl1[q] - zl);
+        const float e = fmaf(dz * dz, kz, fmaf(dy * dy, ky, dx * dx * kx));
+        const float v = ex2_approx(e) * w;
+        const float yy = v - c1[q];
+        const float tt = s1[q] + yy;
+        c1[q] = (tt - s1[q]) - yy;
+        s1[q] = tt;
       }
     };
-    const float4* A = (const float4*)st.base;
-    const float4* B = A + st.cap;
-    const float2* C = (const float2*)(B + st.cap);
-    int n = lane;
-    for (; n + 32 < n_sm; n += 64) {              // two nodes per round, one per sum
-      const float4 a0 = A[n], b0 = B[n], a1 = A[n + 32], b1 = B[n + 32];
-      const float2 c0 = C[n], c1 = C[n + 32];
-      acc(0, a0, b0, c0);
-      acc(1, a1, b1, c1);
-    }
-    for (; n < n_sm; n += 32) acc(0, A[n], B[n], C[n]);
-    for (; n < nn; n += 32)
-      acc(0, make_float4(__ldg(nb.xh + n), __ldg(nb.yh + n), __ldg(nb.zh + n), __ldg(nb.kx + n)),
-          make_float4(__ldg(nb.xl + n), __ldg(nb.yl + n), __ldg(nb.zl + n), __ldg(nb.ky + n)),
-          make_float2(__ldg(nb.kz + n), __ldg(nb.w + n)));
-    long long f[NP];
+    const int cap2 = st.cap >> 1;
+    const unsigned long long* F = (const unsigned long long*)st.base;   // field f, node pair j: F[f * cap2 + j]
+    const int npair = n_sm >> 1;
+    for (int j = lane; j < npair; j += 32) {
+      const unsigned long long xh = F[j], yh = F[cap2 + j], zh = F[2 * cap2 + j], xl = F[3 * cap2 + j],
+                               yl = F[4 * cap2 + j], zl = F[5 * cap2 + j], kx = F[6 * cap2 + j],
+                               ky = F[7 * cap2 + j], kz = F[8 * cap2 + j], w = F[9 * cap2 + j];
 #pragma unroll
-    for (int q = 0; q < NP; ++q)
-      f[q] = (to_fix30(s[0][q]) - to_fix30(c[0][q])) + (to_fix30(s[1][q]) - to_fix30(c[1][q]));
+      for (int q = 0; q < NP; ++q) {
+        const unsigned long long dx = add2(sub2(Xh[q], xh), sub2(Xl[q], xl));
+        const unsigned long long dy = add2(sub2(Yh[q], yh), sub2(Yl[q], yl));
+        const unsigned long long dz = add2(sub2(Zh[q], zh), sub2(Zl[q], zl));
+        const unsigned long long e = fma2(mul2(dz, dz), kz, fma2(mul2(dy, dy), ky, mul2(mul2(dx, dx), kx)));
+        float e0, e1;
+        upk2(e, e0, e1);
+        const unsigned long long v = mul2(pk2(ex2_approx(e0), ex2_approx(e1)), w);
+        const unsigned long long y = sub2(v, c2[q]);
+        const unsigned long long t = add2(s2[q], y);
+        c2[q] = sub2(sub2(t, s2[q]), y);
+        s2[q] = t;
+      }
+    }
+    const float* F1 = (const float*)st.base;
+    if ((n_sm & 1) && lane == 0) {                 // the odd staged node
+      const int n = n_sm - 1, c = st.cap;
+      acc1(F1[n], F1[c + n], F1[2 * c + n], F1[3 * c + n], F1[4 * c + n], F1[5 * c + n], F1[6 * c + n],
+           F1[7 * c + n], F1[8 * c + n], F1[9 * c + n]);
+    }
+    for (int n = n_sm + lane; n < nn; n += 32)     // nodes past the staged copy
+      acc1(__ldg(nb.xh + n), __ldg(nb.yh + n), __ldg(nb.zh + n), __ldg(nb.xl + n), __ldg(nb.yl + n),
+           __ldg(nb.zl + n), __ldg(nb.kx + n), __ldg(nb.ky + n), __ldg(nb.kz + n), __ldg(nb.w + n));
+    float hi[NP], lo[NP];
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+      float sl, sh, cl, ch;
+      upk2(s2[q], sl, sh);
+      upk2(c2[q], cl, ch);
+      hi[q] = sl;
+      lo[q] = -cl;
+      df_add(hi[q], lo[q], sh, -ch);
+      df_add(hi[q], lo[q], s1[q], -c1[q]);
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
 #pragma unroll
-      for (int q = 0; q < NP; ++q) f[q] += __shfl_xor_sync(0xffffffffu, f[q], o);
+      for (int q = 0; q < NP; ++q) {
+        const float bh = __shfl_xor_sync(0xffffffffu, hi[q], o), bl = __shfl_xor_sync(0xffffffffu, lo[q], o);
+        df_add(hi[q], lo[q], bh, bl);
+      }
     }
 #pragma unroll
     for (int q = 0; q < NP; ++q) {
-      out[q].liquid = f[q] >= P.tl_fix;
-      out[q].T = fma((double)f[q], 0x1p-30, P.T0);
+      // sign of (hi + lo) - (T_L - T_0): the head difference is exact near the threshold
+      const float d = ((hi[q] - P.tl_df[0]) + (lo[q] - P.tl_df[1])) - P.tl_df[2];
+      out[q].liquid = d >= 0.f;
+      out[q].T = pack_df(hi[q], lo[q]);
     }
   }
+}
+
+// a[i] of a four-entry register array without local-memory indexing.
+__device__ __forceinline__ EvalT pick4(const EvalT (&a)[4], int i) {
+  return i == 0 ? a[0] : (i == 1 ? a[1] : (i == 2 ? a[2] : a[3]));
+}
+
+// T from its stored form (see EvalT); 0 is a point never evaluated (the reference's
+// zero-initialised grid).
+__device__ __forceinline__ double t_decode(const TrackState& S, const DevProblem& P, double raw) {
+  if (!S.t_fixed) return raw;
+  const unsigned long long b = (unsigned long long)__double_as_longlong(raw);
+  if (b == 0ull) return 0.0;
+  return P.T0 + ((double)__uint_as_float((unsigned)(b >> 32)) + (double)__uint_as_float((unsigned)b));
 }
 
 __device__ __forceinline__ int ldcg_i(const int* p) { return __ldcg(p); }
@@ -269,10 +325,8 @@ __device__ __forceinline__ unsigned long long globaltimer() {
 // ------------------------------------------------------------------ step work queue
 enum { IT_RETEST = 0, IT_VISIT = 2, IT_COLUMN = 3 };
 
-__device__ constexpr Staged kNoStage = {nullptr, 0, 0};
-
 struct StepCtx {
-  Staged st;               // this step's node list in shared memory
+  Staged st, stl;          // this step's and the previous step's node lists in shared memory
   BlockBuf* bb;            // this block's buffered records
   mutable unsigned long long ev_n, ev_c;  // point evaluations and their SM clocks (profile)
   int depth;               // chain depth of the item being run (its children get depth + 1)
@@ -282,8 +336,8 @@ struct StepCtx {
   NodeBufView nb, nbl;
   int nn, nnl;
   int nL, n_init;
-  const int* L;
-  int* Lo;
+  const int2* L;
+  int2* Lo;
   int* lo_n;
   QueueCounters* qc;
 };
@@ -292,6 +346,11 @@ __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long
   unsigned long long v;
   asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
+}
+__device__ __forceinline__ unsigned long long atom_add_release(unsigned long long* p, unsigned long long v) {
+  unsigned long long old;
+  asm volatile("atom.add.release.gpu.global.u64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
+  return old;
 }
 __device__ __forceinline__ void st_relaxed_v2(ulonglong2* p, unsigned long long a, unsigned long long b) {
   asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(p), "l"(a), "l"(b) : "memory");
@@ -322,13 +381,13 @@ __device__ __forceinline__ EvalT eval_T(const DevProblem& P, const TrackState& S
   return T[0];
 }
 
-// Four points of this step's list in one pass (entries the caller does not need may repeat
+// NP points of this step's list in one pass (entries the caller does not need may repeat
 // a valid point).
-template <int PREC>
-__device__ __forceinline__ void eval_T4(const DevProblem& P, const TrackState& S, const StepCtx& X,
-                                        const int (&pts)[4], EvalT (&T)[4]) {
+template <int PREC, int NP>
+__device__ __forceinline__ void eval_Tn(const DevProblem& P, const TrackState& S, const StepCtx& X,
+                                        const int (&pts)[NP], EvalT (&T)[NP]) {
   const long long c0 = clock64();
-  warp_T_n<PREC, 4>(P, S, X.nb, X.nn, pts, X.st, T);
+  warp_T_n<PREC, NP>(P, S, X.nb, X.nn, pts, X.st, T);
   X.ev_c += clock64() - c0;
   X.ev_n += 1;
 }
@@ -379,10 +438,12 @@ __device__ __forceinline__ void expand(const DevProblem& P, const TrackState& S,
   emit(S, X, got, IT_VISIT, q, 0, nchild);
 }
 
-__device__ __forceinline__ void push_liquid(const TrackState& S, const StepCtx& X, int p) {
+// A liquid point joins the next step's list with its column's depth (the next re-test
+// needs both).  The slot is reserved as soon as the point is known to be liquid and filled
+// when the item ends, so the reservation's round trip overlaps the item's other work.
+__device__ __forceinline__ void push_liquid(const TrackState& S, const StepCtx& X, int i, int p, int depth) {
   atomicMax(S.stamp + p, X.stamp + 1u);   // already claimed for the next step's re-test
-  const int i = atomicAdd(X.lo_n, 1);
-  if (i < S.list_cap) X.Lo[i] = p; else atomicOr(S.err, ERR_LISTS);
+  if (i < S.list_cap) X.Lo[i] = make_int2(p, depth); else atomicOr(S.err, ERR_LISTS);
 }
 
 __device__ __forceinline__ bool step_over(unsigned long long v, int n_init, unsigned blocks) {
@@ -587,19 +648,19 @@ __global__ void __launch_bounds__(kGenThreads) k_nodes_window(DevProblem P, Node
 // Depth walk under a liquid surface point and the running depth maximum
 // (src/Melt.cpp:271-357): walk down while liquid, else walk up solidifying.  The walk is
 // sequential in the reference; here the layers it is likely to visit are evaluated four
-// at a time ahead of it - the caller's first pass already holds D + 1, D + 2 (down) and
-// D (up) - and only the layers the walk reaches are committed.  T at a layer does not
-// depend on the walk.
+// at a time ahead of it - the caller's first pass already holds D + 1 (down) and D (up) -
+// and only the layers the walk reaches are committed.  T at a layer does not depend on the
+// walk.
 template <int PREC>
-__device__ void depth_walk(const DevProblem& P, const TrackState& S, const StepCtx& X, int p, int D,
-                           const EvalT (&first)[4], unsigned long long& pairs) {
+__device__ int depth_walk(const DevProblem& P, const TrackState& S, const StepCtx& X, int p, int D,
+                          const EvalT& first_down, const EvalT& first_up, unsigned long long& pairs) {
   const int lane = threadIdx.x & 31;
   const int col = p / P.nz;
   const int top = col * P.nz + (P.nz - 1);            // layer d of the column is point top - d
   EvalT Tc[4], Tu[4];
-  int cb = D + 1, cn = (D + 1 <= P.nz - 1) ? ((D + 2 <= P.nz - 1) ? 2 : 1) : 0;   // down: cb..cb+cn-1
-  int ub = D, un = D >= 1 ? 1 : 0;                                                   // up: ub..ub-un+1
-  Tc[0] = first[1]; Tc[1] = first[2]; Tu[0] = first[3];
+  int cb = D + 1, cn = (D + 1 <= P.nz - 1) ? 1 : 0;   // down: cb..cb+cn-1
+  int ub = D, un = D >= 1 ? 1 : 0;                    // up: ub..ub-un+1
+  Tc[0] = first_down; Tu[0] = first_up;
   int d = D;
   bool none_deeper = true;
   while (true) {
@@ -615,18 +676,19 @@ __device__ void depth_walk(const DevProblem& P, const TrackState& S, const StepC
         cn += ok ? 1 : 0;
       }
       cb = d;
-      eval_T4<PREC>(P, S, X, pts, Tc);
+      eval_Tn<PREC, 4>(P, S, X, pts, Tc);
     }
-    const EvalT T = Tc[d - cb];
+    const EvalT T = pick4(Tc, d - cb);
     pairs += X.nn;
     if (lane == 0) set_T(S, top - d, T, X.k);
     if (!T.liquid) break;
     none_deeper = false;
   }
+  EvalT Tl4[4];                                       // the up layers' T at t - dt (below D)
   while (true) {
     --d;
     if (d == 0 || !none_deeper) break;
-    if (!(d <= ub && d > ub - un)) {                  // next four layers up
+    if (!(d <= ub && d > ub - un)) {                  // next four layers up, at t and at t - dt
       int pts[4];
       un = 0;
 #pragma unroll
@@ -636,16 +698,20 @@ __device__ void depth_walk(const DevProblem& P, const TrackState& S, const StepC
         un += ok ? 1 : 0;
       }
       ub = d;
-      eval_T4<PREC>(P, S, X, pts, Tu);
+      eval_Tn<PREC, 4>(P, S, X, pts, Tu);
+      const long long c0 = clock64();
+      warp_T_n<PREC, 4>(P, S, X.nbl, X.nnl, pts, X.stl, Tl4);
+      X.ev_c += clock64() - c0;
+      X.ev_n += 1;
     }
     const int q = top - d;
     const double Told = ldcg_d(S.T + q);
-    const EvalT T = Tu[ub - d];
+    const EvalT T = pick4(Tu, ub - d);
     pairs += X.nn;
     if (lane == 0) set_T(S, q, T, X.k);
     if (!T.liquid) {
       double Tl = Told;                                   // T of the previous step
-      if (d != D) { Tl = eval_T<PREC>(P, S, X, X.nbl, X.nnl, q, kNoStage).T; pairs += X.nnl; }
+      if (d != D) { Tl = pick4(Tl4, ub - d).T; pairs += X.nnl; }
       if (lane == 0) push_rec(S, X, q, T.T, Tl);
     } else {
       break;
@@ -658,8 +724,8 @@ __device__ void depth_walk(const DevProblem& P, const TrackState& S, const StepC
       double dep;
       if (d == P.nz - 1) dep = d;
       else {
-        const double Tl = ldcg_d(S.T + col * P.nz + (P.nz - 1 - d));
-        const double Ts = ldcg_d(S.T + col * P.nz + (P.nz - 1 - (d + 1)));
+        const double Tl = t_decode(S, P, ldcg_d(S.T + col * P.nz + (P.nz - 1 - d)));
+        const double Ts = t_decode(S, P, ldcg_d(S.T + col * P.nz + (P.nz - 1 - (d + 1))));
         dep = rn_add((double)d, rn_div(rn_sub(P.TL, Tl), rn_sub(Ts, Tl)));
       }
       if (dep > S.depth_max[col]) {
@@ -668,12 +734,17 @@ __device__ void depth_walk(const DevProblem& P, const TrackState& S, const StepC
       }
     }
   }
+  return d;
 }
 
 // One work item; returns the number of child items it published (already counted).
+// A beam-trace candidate arrives with its claim still in flight (the lane-0 result of the
+// atomic, `got`): the point is evaluated meanwhile and the item stops before any effect if
+// another item took the point.
+// A re-test brings its column's depth from the liquid list (Dk); other items read it.
 template <int PREC, bool SURF>
 __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx& X, int type, int p, int aux,
-                        unsigned long long& pairs) {
+                        int Dk, bool seed, bool got, unsigned long long& pairs) {
   const int lane = threadIdx.x & 31;
   int nchild = 0;
   const double Told = ldcg_d(S.T + p);
@@ -682,33 +753,44 @@ __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx&
     pairs += X.nn;
     if (lane == 0) set_T(S, p, T, X.k);
     double Tl = Told;
-    if (aux) { Tl = eval_T<PREC>(P, S, X, X.nbl, X.nnl, p, kNoStage).T; pairs += X.nnl; }
+    if (aux) { Tl = eval_T<PREC>(P, S, X, X.nbl, X.nnl, p, X.stl).T; pairs += X.nnl; }
     if (lane == 0) push_rec(S, X, p, T.T, Tl);
     return 0;
   }
   // Surface re-tests expand whatever their temperature (src/Run.cpp:655): claim first, so
   // the neighbours' items start while this point is evaluated.
   if (SURF && type == IT_RETEST) expand<SURF>(P, S, X, p, nchild);
-  EvalT T4[4];
+  EvalT T3[3];
   int D = 0;
   if (SURF) {                              // the point and the layers its depth walk starts with
     const int col = p / P.nz, top = col * P.nz + (P.nz - 1);
-    D = ldcg_i(S.depths + col);
-    const int pts[4] = {p, D + 1 <= P.nz - 1 ? top - (D + 1) : p, D + 2 <= P.nz - 1 ? top - (D + 2) : p,
-                        D >= 1 ? top - D : p};
-    eval_T4<PREC>(P, S, X, pts, T4);
+    D = type == IT_RETEST ? Dk : ldcg_i(S.depths + col);
+    const int down = D + 1 <= P.nz - 1 ? top - (D + 1) : p;
+    if (D >= 1) {
+      const int pts[3] = {p, down, top - D};
+      eval_Tn<PREC, 3>(P, S, X, pts, T3);
+    } else {
+      const int pts[2] = {p, down};
+      EvalT T2[2];
+      eval_Tn<PREC, 2>(P, S, X, pts, T2);
+      T3[0] = T2[0]; T3[1] = T2[1]; T3[2] = T2[1];
+    }
   } else {
-    T4[0] = eval_T<PREC>(P, S, X, X.nb, X.nn, p, X.st);
+    T3[0] = eval_T<PREC>(P, S, X, X.nb, X.nn, p, X.st);
   }
-  const EvalT T = T4[0];
+  if (seed && !__shfl_sync(0xffffffffu, got, 0)) return 0;
+  const EvalT T = T3[0];
   pairs += X.nn;
   if (lane == 0) set_T(S, p, T, X.k);
   if (T.liquid) {
+    int slot = 0;
+    if (lane == 0) slot = atomicAdd(X.lo_n, 1);
     // Volume expands the liquid points; Surface the liquid visits (re-tests did above)
     if (!(SURF && type == IT_RETEST)) expand<SURF>(P, S, X, p, nchild);
     // the depth walk under a liquid surface point needs nothing else from this step
-    if (SURF) depth_walk<PREC>(P, S, X, p, D, T4, pairs);
-    if (lane == 0) push_liquid(S, X, p);
+    int Dn = 0;
+    if (SURF) Dn = depth_walk<PREC>(P, S, X, p, D, T3[1], T3[2], pairs);
+    if (lane == 0) push_liquid(S, X, slot, p, Dn);
   } else if (type == IT_RETEST) {          // cooled below T_L since the last step
     if (lane == 0) push_rec(S, X, p, T.T, Told);
     if (SURF) {
@@ -741,20 +823,28 @@ __global__ void __launch_bounds__(kTrackThreads, 1) k_track(DevProblem P, TrackS
   TrackCounters* C = S.C;
   unsigned long long pairs = 0;
   const size_t buf_bytes = (size_t)stage_cap * staged_bytes_per_node<PREC>();
+  __shared__ int s_flush[2];
   if (threadIdx.x == 0) bbuf.nrec = 0;
-  if (k_begin < k_end) {                    // the first step's list; later ones are prefetched
+  // Three staged lists rotate by step: k % 3 holds step k's, (k - 1) % 3 the previous
+  // step's (for T at t - dt), (k + 1) % 3 receives the next step's while step k runs.
+  auto buf_of = [&](int kk) { return stage_mem + (size_t)(((kk % 3) + 3) % 3) * buf_bytes; };
+  if (k_begin < k_end) {
     const int slot = k_begin - W.base + 1;
-    stage_issue<PREC>(slot_view(W, slot), min(W.count[slot], stage_cap), stage_mem + (k_begin & 1) * buf_bytes,
-                      stage_cap);
+    stage_issue<PREC>(slot_view(W, slot), min(W.count[slot], stage_cap), buf_of(k_begin), stage_cap);
+    if (k_begin > 0) stage_issue<PREC>(slot_view(W, slot - 1), min(W.count[slot - 1], stage_cap), buf_of(k_begin - 1),
+                                       stage_cap);
   }
+  cp_async_wait_all();
+  __syncthreads();
   unsigned long long t_work = 0, n_items = 0, c_items = 0, c_wait = 0, depth_sum = 0;
   unsigned long long ev_n = 0, ev_c = 0, lvl_s[4] = {0, 0, 0, 0}, lvl_e[4] = {0, 0, 0, 0};
+  // step k's live-list length and this warp's first re-test entry, read when step k - 1
+  // ended (for the first step, from memory)
+  int nL_next = k_begin < k_end ? ldcg_i(&C->liq_n[k_begin % 3]) : 0;
+  int2 first_next = make_int2(0, 0);
+  if (k_begin < k_end && (tid >> 5) < S.list_cap) first_next = __ldcg(S.liq[k_begin % 3] + (tid >> 5));
   int k = k_begin;
   for (; k < k_end; ++k) {
-    // this step's list has landed in every thread's share; the block's warps have all left
-    // the previous step
-    cp_async_wait_all();
-    if (__syncthreads_or(threadIdx.x == 0 && bbuf.nrec >= kBlkRec / 2)) flush_block(S, &bbuf, S.rec_n);
     StepCtx X;
     X.ev_n = 0;
     X.ev_c = 0;
@@ -764,7 +854,8 @@ __global__ void __launch_bounds__(kTrackThreads, 1) k_track(DevProblem P, TrackS
     const int b0 = k % 3, b1 = (k + 1) % 3;
     X.qc = &C->q[b0];
     X.stamp = (unsigned)k + 1u;
-    X.nL = ldcg_i(&C->liq_n[b0]);
+    X.nL = nL_next;
+    const int2 first_entry = first_next;
     // the beam trace runs for k > 0 while t < end + dt (src/Run.cpp:661)
     X.t = W.t[slot];
     const bool seeds = k > 0 && X.t < P.end_time + P.dt;
@@ -772,12 +863,14 @@ __global__ void __launch_bounds__(kTrackThreads, 1) k_track(DevProblem P, TrackS
     const int* seed = W.seeds + (size_t)slot * W.seed_cap;
     X.n_init = X.nL + n_seed;
     if (k + 1 < k_end)                      // next step's list, copied while this step runs
-      stage_issue<PREC>(slot_view(W, slot + 1), min(W.count[slot + 1], stage_cap),
-                        stage_mem + ((k + 1) & 1) * buf_bytes, stage_cap);
+      stage_issue<PREC>(slot_view(W, slot + 1), min(W.count[slot + 1], stage_cap), buf_of(k + 1), stage_cap);
     X.bb = &bbuf;
-    X.st.base = stage_mem + (k & 1) * buf_bytes;
+    X.st.base = buf_of(k);
     X.st.cap = stage_cap;
     X.st.n_sm = min(W.count[slot], stage_cap);
+    X.stl.base = buf_of(k - 1);
+    X.stl.cap = stage_cap;
+    X.stl.n_sm = k == 0 ? 0 : min(W.count[slot - 1], stage_cap);
     X.k = k;
     X.nb = slot_view(W, slot);
     X.nbl = slot_view(W, slot - 1);
@@ -786,10 +879,9 @@ __global__ void __launch_bounds__(kTrackThreads, 1) k_track(DevProblem P, TrackS
     X.L = S.liq[b0];
     X.Lo = S.liq[b1];
     X.lo_n = &C->liq_n[b1];
-    if (threadIdx.x == 0) {                 // this block has entered the step
-      const unsigned long long st = atomicAdd(&X.qc->state, kArrive);
-      if (step_over(st + kArrive, X.n_init, gridDim.x)) finish_step(P, S, X, k, st + kArrive, high_water);
-    }
+    unsigned long long arrival = 0;         // this block enters the step (thread 0)
+    bool arrival_pending = threadIdx.x == 0;
+    if (arrival_pending) arrival = atomicAdd(&X.qc->state, kArrive);
     // The work loop.  The step's initial items - re-tests of the previous liquid points,
     // then the beam trace's candidates - are dealt to the warps in order (warp w takes
     // w, w + warps, ...), so they all start at once; items published during the step are
@@ -801,23 +893,28 @@ __global__ void __launch_bounds__(kTrackThreads, 1) k_track(DevProblem P, TrackS
     long long idle = 0;
     while (true) {
       const long long c0 = clock64();
-      int type, p = 0, aux = 0;
-      bool run = true;
+      int type, p = 0, aux = 0, Dk = 0;
+      bool is_seed = false, got = false;
       if (next_init < X.n_init) {
         const int t = next_init;
         next_init += n_warps;
         X.depth = 0;
         if (t < X.nL) {
           type = IT_RETEST;
-          p = __ldcg(X.L + t);
+          const int2 e = (t == (tid >> 5)) ? first_entry : __ldcg(X.L + t);
+          p = e.x;
+          Dk = e.y;
         } else {                            // a trace candidate: visited if this claim takes it
           type = IT_VISIT;
           p = __ldg(seed + (t - X.nL));
-          bool got = false;
+          is_seed = true;
           if (lane == 0) got = claim(S, p, X.stamp);
-          run = __shfl_sync(0xffffffffu, got, 0);
         }
       } else {
+        if (arrival_pending) {              // this block's entry, checked once its result is back
+          arrival_pending = false;
+          if (step_over(arrival + kArrive, X.n_init, gridDim.x)) finish_step(P, S, X, k, arrival + kArrive, high_water);
+        }
         unsigned ticket = 0;
         if (lane == 0) ticket = atomicAdd(&X.qc->head, 1u);
         ticket = __shfl_sync(0xffffffffu, ticket, 0);
@@ -866,15 +963,14 @@ __global__ void __launch_bounds__(kTrackThreads, 1) k_track(DevProblem P, TrackS
         if (lane == 0) atomicMax(&X.qc->depth, (unsigned)max_depth);
       }
       const unsigned long long g_item = globaltimer();
-      if (run) run_item<PREC, SURF>(P, S, X, type, p, aux, pairs);
+      run_item<PREC, SURF>(P, S, X, type, p, aux, Dk, is_seed, got, pairs);
       if (lane == 0) {
         const int l = min(X.depth, 3);
         atomicMax(&X.qc->lvl_start[l], (unsigned)(g_item - g0));
         atomicMax(&X.qc->lvl_end[l], (unsigned)(globaltimer() - g0));
       }
-      __threadfence();
-      if (lane == 0) {                                           // completed
-        const unsigned long long st = atomicAdd(&X.qc->state, 1ull);
+      if (lane == 0) {                                           // completed, after the item's writes
+        const unsigned long long st = atom_add_release(&X.qc->state, 1ull);
         if (step_over(st + 1ull, X.n_init, gridDim.x)) finish_step(P, S, X, k, st + 1ull, high_water);
       }
       ++n_items;
@@ -883,10 +979,16 @@ __global__ void __launch_bounds__(kTrackThreads, 1) k_track(DevProblem P, TrackS
     t_work += globaltimer() - g0;
     ev_n += X.ev_n;
     ev_c += X.ev_c;
-    // every warp of the block takes the same decision: an abort after a bounded wait, or
-    // the step's verdict (which stays until this block has entered the next step)
-    if (__syncthreads_or(ld_acquire_u32(&C->finished) == 0xffffffffu)) break;
+    // The step is over: the next step's live-list length and this step's verdict are final
+    // (the verdict stays until this block has entered the next step).  Every warp of the
+    // block takes the same decisions; the block barrier also completes the next list's
+    // copies.
     const unsigned verdict = ld_acquire_u32(&C->verdict);
+    nL_next = ldcg_i(X.lo_n);
+    if ((tid >> 5) < S.list_cap) first_next = __ldcg(X.Lo + (tid >> 5));
+    cp_async_wait_all();
+    if (threadIdx.x == 0) s_flush[k & 1] = bbuf.nrec >= kBlkRec / 2;
+    if (__syncthreads_or(ld_acquire_u32(&C->finished) == 0xffffffffu)) break;
     if (tid == 0) {
       depth_sum += __ldcg(&X.qc->depth);
       for (int l = 0; l < 4; ++l) {
@@ -895,6 +997,7 @@ __global__ void __launch_bounds__(kTrackThreads, 1) k_track(DevProblem P, TrackS
       }
     }
     if (verdict & 3u) { ++k; break; }
+    if (s_flush[k & 1]) flush_block(S, &bbuf, S.rec_n);
   }
   cp_async_wait_all();
   flush_block(S, &bbuf, S.rec_n);
@@ -1070,7 +1173,7 @@ __global__ void __launch_bounds__(128) k_solidify(DevProblem P, TrackState S, co
   point_xyz(P, r.p, x, y, z);
   unsigned long long pairs = 0;
   int err = 0;
-  double T2 = r.T, T1 = r.Tl, t2 = r.t, t1 = rn_sub(r.t, P.dt), tsol = 0.0;
+  double T2 = t_decode(S, P, r.T), T1 = t_decode(S, P, r.Tl), t2 = r.t, t1 = rn_sub(r.t, P.dt), tsol = 0.0;
   PointSums ps;
   for (int it = 1;; ++it) {
     const double m = rn_div(rn_sub(T2, T1), rn_sub(t2, t1));
@@ -1110,7 +1213,7 @@ __global__ void k_final_field(DevProblem P, TrackState S, int f, double* out) {
   const bool liquid_last = S.last_liq[p] > S.sol_step[p];
   double v = 0.0;
   switch (f) {
-    case F_T: v = S.T[p]; break;
+    case F_T: v = t_decode(S, P, S.T[p]); break;
     case F_TSOL: v = S.tSol ? S.tSol[p] : 0.0; break;
     case F_G: v = liquid_last ? DBL_MIN : (S.G ? S.G[p] : 0.0); break;
     case F_V: v = liquid_last ? DBL_MIN : (S.V ? S.V[p] : 0.0); break;
@@ -1140,11 +1243,16 @@ static cudaError_t launch_track_t(const DevProblem& P, const TrackState& S, cons
   int dev = 0, sms = 0, occ = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  // stage whole lists up to the slot capacity, within 200 KB of shared memory for both buffers
-  int cap = std::min(w.slot_cap, (200 * 1024) / (2 * staged_bytes_per_node<PREC>()));
+  // stage whole lists up to the slot capacity, within 200 KB of shared memory for the three buffers
+  int cap = std::min(w.slot_cap, (200 * 1024) / (3 * staged_bytes_per_node<PREC>()));
   cap = std::max(8, cap & ~7);
-  const size_t smem = (size_t)2 * cap * staged_bytes_per_node<PREC>();
+  const size_t smem = (size_t)3 * cap * staged_bytes_per_node<PREC>();
   cudaError_t e = cudaFuncSetAttribute(k_track<PREC, SURF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  // leave the rest of the SM's 256 KB to the L1 cache (the kernel's loads of node windows,
+  // axis tables and local arrays hit there)
+  const int carve = std::min(100, (int)((smem + 16 * 1024) * 100 / (228 * 1024)) + 1);
+  e = cudaFuncSetAttribute(k_track<PREC, SURF>, cudaFuncAttributePreferredSharedMemoryCarveout, carve);
   if (e != cudaSuccess) return e;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_track<PREC, SURF>, kTrackThreads, smem);
   const int blocks = sms * (occ < 1 ? occ : 1);

@@ -67,7 +67,7 @@ struct TrackState {
   double* depth;           // per point (Surface with depth output), may be null
   int* depths;             // per (i, j) column: deepest liquid layer
   double* depth_max;       // per column
-  int* liq[3];
+  int2* liq[3];             // liquid surface points (point, column depth), rotating by step
   int list_cap;
   ulonglong2* queue;       // work items {stamp << 32 | point, stamp << 32 | type | depth << 8 | aux << 16}
   int queue_cap;
@@ -76,6 +76,7 @@ struct TrackState {
   int rec_cap;
   TrackCounters* C;
   const float2* axis;      // grid coordinates as (hi, lo) floats: x[0, nx), y[nx, nx + ny), z after
+  int t_fixed;             // T and the records' T, T_last hold FP32 tracking's fixed point (see t_decode)
   unsigned* bar;           // grid barrier: [0] arrivals, [1] generation
   int* err;
   unsigned long long* pairs;
