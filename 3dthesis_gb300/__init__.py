@@ -42,7 +42,9 @@ EXPORTED = ("th_ctx_create_from_deck", "th_ctx_destroy", "th_last_error", "th_ge
             "th_simulate", "th_pairs", "th_set_tile_shape", "th_last_kernel_ms", "th_sync",
             "th_calc_T_noalloc", "th_run_stats", "th_run_reset", "th_autotune",
             "th_batch_create", "th_batch_destroy", "th_batch_last_error", "th_batch_points", "th_batch_snapshot",
-            "th_batch_snapshot_device", "th_batch_set_tile_shape", "th_batch_autotune", "th_batch_pairs")
+            "th_batch_snapshot_device", "th_batch_set_tile_shape", "th_batch_autotune", "th_batch_pairs",
+            "th_adj_create", "th_adj_destroy", "th_adj_last_error", "th_adj_num_params", "th_adj_params",
+            "th_adj_host_nodes", "th_adj_forward", "th_adj_backward")
 
 
 class ThesisError(RuntimeError):
@@ -109,6 +111,16 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.th_batch_set_tile_shape.argtypes = [vp, c_int, c_int]
     L.th_batch_autotune.argtypes = [vp, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int)]
     L.th_batch_pairs.argtypes = [vp, ctypes.POINTER(c_i64)]
+    L.th_adj_create.argtypes = [ctypes.c_char_p, c_int, vp, c_int, vp, c_int, ctypes.POINTER(vp)]
+    L.th_adj_destroy.argtypes = [vp]
+    L.th_adj_destroy.restype = None
+    L.th_adj_last_error.argtypes = [vp]
+    L.th_adj_last_error.restype = ctypes.c_char_p
+    L.th_adj_num_params.argtypes = [vp]
+    L.th_adj_params.argtypes = [vp, vp]
+    L.th_adj_host_nodes.argtypes = [vp, vp, c_int, vp, c_int, vp, ctypes.POINTER(c_int)]
+    L.th_adj_forward.argtypes = [vp, vp, vp]
+    L.th_adj_backward.argtypes = [vp, vp, vp]
     _lib = L
     return L
 
@@ -324,3 +336,92 @@ class Batch:
         v = ctypes.c_int64()
         self._check(self._lib.th_batch_pairs(self._b, ctypes.byref(v)))
         return v.value
+
+
+PARAM_NAMES = ("P", "eta", "Width_X", "Width_Y", "Depth_Z", "alpha")
+
+
+class Adjoint:
+    """Probe temperatures of a single-beam deck as a differentiable function of
+    theta = (P, efficiency, Width_X, Width_Y, Depth_Z, alpha, x1, y1, x2, y2, ...) - the path
+    vertices after the origin, in metres - and their gradient (``backward``)."""
+
+    def __init__(self, param_input: str, probes: np.ndarray, times: Sequence[float], precision="fp32"):
+        self._lib = load_library()
+        self._a = ctypes.c_void_p()
+        self.probes = np.ascontiguousarray(probes, dtype=np.int64)
+        self.times = np.ascontiguousarray(times, dtype=np.float64)
+        st = self._lib.th_adj_create(os.fspath(param_input).encode(), _PRECISIONS[precision], _ptr(self.probes),
+                                     self.probes.size, _ptr(self.times), self.times.size, ctypes.byref(self._a))
+        if st != 0:
+            raise ThesisError(st, self._lib.th_adj_last_error(None).decode())
+        self.num_params = int(self._lib.th_adj_num_params(self._a))
+
+    def _check(self, st: int):
+        if st != 0:
+            raise ThesisError(st, self._lib.th_adj_last_error(self._a).decode())
+
+    def close(self):
+        if self._a:
+            self._lib.th_adj_destroy(self._a)
+            self._a = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self) -> np.ndarray:
+        th = np.empty(self.num_params)
+        self._check(self._lib.th_adj_params(self._a, _ptr(th)))
+        return th
+
+    def host_nodes(self, theta: np.ndarray, time_idx: int, tangents: bool = False):
+        """(values[8, n], tangents[8, n, num_params] or None) of the node list at times[time_idx]."""
+        theta = np.ascontiguousarray(theta, dtype=np.float64)
+        n = ctypes.c_int32()
+        self._check(self._lib.th_adj_host_nodes(self._a, _ptr(theta), int(time_idx), None, 0, None, ctypes.byref(n)))
+        cap = max(1, n.value)
+        vals = np.zeros((8, cap))
+        tan = np.zeros((8, cap, self.num_params)) if tangents else None
+        self._check(self._lib.th_adj_host_nodes(self._a, _ptr(theta), int(time_idx), _ptr(vals), cap,
+                                                _ptr(tan) if tangents else None, ctypes.byref(n)))
+        return vals[:, :n.value], (tan[:, :n.value] if tangents else None)
+
+    def forward(self, theta: np.ndarray) -> np.ndarray:
+        theta = np.ascontiguousarray(theta, dtype=np.float64)
+        out = np.empty((self.times.size, self.probes.size))
+        self._check(self._lib.th_adj_forward(self._a, _ptr(theta), _ptr(out)))
+        return out
+
+    def backward(self, dL_dT: np.ndarray) -> np.ndarray:
+        g = np.ascontiguousarray(dL_dT, dtype=np.float64).reshape(self.times.size, self.probes.size)
+        out = np.empty(self.num_params)
+        self._check(self._lib.th_adj_backward(self._a, _ptr(g), _ptr(out)))
+        return out
+
+
+def probe_temperatures(adj: "Adjoint", theta):
+    """torch.autograd entry: T[times, probes] = f(theta) with the gradient from the adjoint
+    kernel.  theta is a float64 torch tensor of adj.num_params entries."""
+    import torch
+
+    class _ProbeT(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, th):
+            T = adj.forward(th.detach().cpu().numpy())
+            return torch.from_numpy(T).to(th.device)
+
+        @staticmethod
+        def backward(ctx, grad_T):
+            g = adj.backward(grad_T.detach().cpu().numpy())
+            return torch.from_numpy(g).to(grad_T.device)
+
+    return _ProbeT.apply(theta)

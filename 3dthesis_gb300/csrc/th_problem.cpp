@@ -199,9 +199,9 @@ bool th_load_deck(const std::string& param_input, HostProblem& hp, std::string& 
       HostBeam B;
       B.ax = b.num("Shape", "Width_X", 10.0e-6); B.ay = b.num("Shape", "Width_Y", 10.0e-6);
       B.az = b.num("Shape", "Depth_Z", 1.0e-6);
-      B.q = b.num("Intensity", "Power", 1200); B.eff = b.num("Intensity", "Efficiency", 1.0);
+      B.power = b.num("Intensity", "Power", 1200); B.eff = b.num("Intensity", "Efficiency", 1.0);
       if (B.eff == DBL_MAX) B.eff = 1.0;
-      B.q = B.q * B.eff * 2.0;
+      B.q = B.power * B.eff * 2.0;
       if (!(B.ax > 0.0 && B.ay > 0.0 && B.az > 0.0)) { err = "beam widths must be positive in " + f; return false; }
       hp.beams.push_back(B);
     }

@@ -61,7 +61,7 @@ struct DevProblem {
   double gl_loc[30], gl_w[30];
 };
 
-struct HostBeam { double ax, ay, az, eff, q, nond; };
+struct HostBeam { double ax, ay, az, eff, q, nond, power; };
 
 struct HostProblem {
   std::string dir, name;

@@ -367,3 +367,40 @@ def small_sweep(n: int = 10, seed: int = 3) -> List[Deck]:
                   AxisSpec(-(nz - 1) * 1e-5, 0.0, num=nz)),
             scan_fracs=[50, 100], tracking="None", bcs=bcs))
     return decks
+
+
+def adjoint_calibration(grid: Tuple[int, int, int] = (300, 300, 60), tracks: int = 50,
+                        length_mm: float = 5.0) -> Deck:
+    """The Surface-serpentine path and material (50 x 5 mm tracks, hatch 80 um, 0.8 m/s,
+    200 W) as a Snapshots deck on a 300x300x60 grid at 10 um; the calibration's probe points
+    and times are chosen by the caller (``adjoint_probes``)."""
+    nx, ny, nz = grid
+    d = surface_serpentine(tracks=tracks, length_mm=length_mm)
+    d.name = "adjoint_calibration"
+    d.mode = "Snapshots"
+    d.tracking = "None"
+    d.timestep = None
+    d.outputs = {"T": 1}
+    d.axes = (AxisSpec(0.0, (nx - 1) * 1e-5, num=nx), AxisSpec(-0.5e-3, -0.5e-3 + (ny - 1) * 1e-5, num=ny),
+              AxisSpec(-(nz - 1) * 1e-5, 0.0, num=nz))
+    d.scan_fracs = [100]
+    return d
+
+
+def adjoint_probes(deck: Deck, n: int = 4096, seed: int = 0, times: Sequence[float] = (0.05, 0.15, 0.30)):
+    """Seeded probe points (flat ids) in the top quarter of the grid, and the snapshot
+    times (s) of the calibration loss."""
+    rng = random.Random(seed)
+    nx, ny, nz = (ax.num for ax in deck.axes)
+    pts = []
+    for _ in range(n):
+        i, j, k = rng.randrange(nx), rng.randrange(ny), rng.randrange(max(0, nz - nz // 4), nz)
+        pts.append((i * ny + j) * nz + k)
+    return pts, list(times)
+
+
+def small_adjoint() -> Deck:
+    d = adjoint_calibration(grid=(40, 30, 10), tracks=3, length_mm=0.4)
+    d.name = "small_adjoint"
+    d.axes = (AxisSpec(-0.05e-3, 0.34e-3, num=40), AxisSpec(-0.1e-3, 0.19e-3, num=30), AxisSpec(-0.09e-3, 0.0, num=10))
+    return d

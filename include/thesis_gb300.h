@@ -192,6 +192,36 @@ th_status th_batch_autotune(th_batch* b, int32_t idx, int32_t* kp_out, int32_t* 
 /* Point x node pairs evaluated by the batch so far. */
 th_status th_batch_pairs(th_batch* b, int64_t* out);
 
+/* ---- Adjoint (calibration gradients) -----------------------------------------------
+ * Temperatures of a single-beam deck at probe points and times, as a function of the
+ * parameter vector theta = (P, efficiency, Width_X, Width_Y, Depth_Z, alpha, then x, y of
+ * every path vertex after the origin, in metres), and the gradient of a loss through them.
+ * alpha is the diffusivity k / (rho c).  The node list is re-walked for theta on the host in
+ * FP64 dual numbers (values identical to the device walk); the device recomputes each
+ * probe x node term for the per-node adjoint sums.  The walk's discrete choices (interval
+ * counts, Gauss orders, r_max cut-off) are held at theta's.  No reference counterpart: the
+ * reference has no gradients (its forward is src/Calc.cpp:67-211 + src/Grid.cpp:275-314). */
+typedef struct th_adj th_adj;
+
+/* probes: flat grid point ids (k fastest); times: seconds.  No device work until forward. */
+th_status th_adj_create(const char* param_input, int32_t precision, const int64_t* probes, int32_t nprobe,
+                        const double* times, int32_t ntimes, th_adj** out);
+void th_adj_destroy(th_adj* a);
+const char* th_adj_last_error(const th_adj* a);
+/* 6 + 2 x (path segments after the origin). */
+int32_t th_adj_num_params(const th_adj* a);
+/* The deck's own parameter values. */
+th_status th_adj_params(th_adj* a, double* theta);
+/* Host node list at times[time_idx] for theta (8 arrays of cap: x y z 1/phix 1/phiy 1/phiz
+ * dtau amp) and, when tangents is not NULL, d(node field)/d(theta) laid out
+ * [field][node][param] with cap nodes per field; *n_out = node count.  CPU only. */
+th_status th_adj_host_nodes(th_adj* a, const double* theta, int32_t time_idx, double* out, int32_t cap,
+                            double* tangents, int32_t* n_out);
+/* T at every probe and time for theta: T_out[t * nprobe + p].  Remembers theta. */
+th_status th_adj_forward(th_adj* a, const double* theta, double* T_out);
+/* dL/dtheta from dL/dT (same layout as T_out) at the theta of the last forward. */
+th_status th_adj_backward(th_adj* a, const double* dL_dT, double* dL_dtheta);
+
 #ifdef __cplusplus
 }
 #endif
