@@ -657,26 +657,32 @@ __device__ int depth_walk(const DevProblem& P, const TrackState& S, const StepCt
   const int lane = threadIdx.x & 31;
   const int col = p / P.nz;
   const int top = col * P.nz + (P.nz - 1);            // layer d of the column is point top - d
+  // FP64 runs walk one layer at a time: their passes are FP64-throughput bound, so layers
+  // the walk may not reach are not evaluated ahead
+  constexpr int NB = PREC == 0 ? 1 : 4;
   EvalT Tc[4], Tu[4];
-  int cb = D + 1, cn = (D + 1 <= P.nz - 1) ? 1 : 0;   // down: cb..cb+cn-1
-  int ub = D, un = D >= 1 ? 1 : 0;                    // up: ub..ub-un+1
+  int cb = D + 1, cn = (PREC != 0 && D + 1 <= P.nz - 1) ? 1 : 0;   // down: cb..cb+cn-1
+  int ub = D, un = (PREC != 0 && D >= 1) ? 1 : 0;                  // up: ub..ub-un+1
   Tc[0] = first_down; Tu[0] = first_up;
   int d = D;
   bool none_deeper = true;
   while (true) {
     ++d;
     if (d == P.nz) break;
-    if (d >= cb + cn) {                               // next four layers down
-      int pts[4];
+    if (d >= cb + cn) {                               // next NB layers down
+      int pts[NB];
       cn = 0;
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
+      for (int q = 0; q < NB; ++q) {
         const bool ok = d + q <= P.nz - 1;
         pts[q] = ok ? top - (d + q) : p;
         cn += ok ? 1 : 0;
       }
       cb = d;
-      eval_Tn<PREC, 4>(P, S, X, pts, Tc);
+      EvalT tmp[NB];
+      eval_Tn<PREC, NB>(P, S, X, pts, tmp);
+#pragma unroll
+      for (int q = 0; q < NB; ++q) Tc[q] = tmp[q];
     }
     const EvalT T = pick4(Tc, d - cb);
     pairs += X.nn;
@@ -688,21 +694,27 @@ __device__ int depth_walk(const DevProblem& P, const TrackState& S, const StepCt
   while (true) {
     --d;
     if (d == 0 || !none_deeper) break;
-    if (!(d <= ub && d > ub - un)) {                  // next four layers up, at t and at t - dt
-      int pts[4];
+    if (!(d <= ub && d > ub - un)) {                  // next NB layers up, at t and at t - dt
+      int pts[NB];
       un = 0;
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
+      for (int q = 0; q < NB; ++q) {
         const bool ok = d - q >= 1;
         pts[q] = ok ? top - (d - q) : p;
         un += ok ? 1 : 0;
       }
       ub = d;
-      eval_Tn<PREC, 4>(P, S, X, pts, Tu);
-      const long long c0 = clock64();
-      warp_T_n<PREC, 4>(P, S, X.nbl, X.nnl, pts, X.stl, Tl4);
-      X.ev_c += clock64() - c0;
-      X.ev_n += 1;
+      EvalT tmp[NB], tmpl[NB];
+      eval_Tn<PREC, NB>(P, S, X, pts, tmp);
+      // T at t - dt is needed only below D (the layer at D has it stored)
+      if (d != D) {
+        const long long c0 = clock64();
+        warp_T_n<PREC, NB>(P, S, X.nbl, X.nnl, pts, X.stl, tmpl);
+        X.ev_c += clock64() - c0;
+        X.ev_n += 1;
+      }
+#pragma unroll
+      for (int q = 0; q < NB; ++q) { Tu[q] = tmp[q]; Tl4[q] = tmpl[q]; }
     }
     const int q = top - d;
     const double Told = ldcg_d(S.T + q);
@@ -762,7 +774,7 @@ __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx&
   if (SURF && type == IT_RETEST) expand<SURF>(P, S, X, p, nchild);
   EvalT T3[3];
   int D = 0;
-  if (SURF) {                              // the point and the layers its depth walk starts with
+  if (SURF && PREC != 0) {                 // the point and the layers its depth walk starts with
     const int col = p / P.nz, top = col * P.nz + (P.nz - 1);
     D = type == IT_RETEST ? Dk : ldcg_i(S.depths + col);
     const int down = D + 1 <= P.nz - 1 ? top - (D + 1) : p;
@@ -776,6 +788,7 @@ __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx&
       T3[0] = T2[0]; T3[1] = T2[1]; T3[2] = T2[1];
     }
   } else {
+    if (SURF) D = type == IT_RETEST ? Dk : ldcg_i(S.depths + p / P.nz);
     T3[0] = eval_T<PREC>(P, S, X, X.nb, X.nn, p, X.st);
   }
   if (seed && !__shfl_sync(0xffffffffu, got, 0)) return 0;

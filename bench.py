@@ -39,6 +39,8 @@ import tempfile
 import threading
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -46,7 +48,10 @@ METRIC = "point-node pairs/s"
 SM_COUNT = 152
 FP32_LANES = 128            # FP32 lanes per SM per clock
 MUFU_LANES = 16             # MUFU.EX2 results per SM per clock
-FP32_OPS_KAHAN = 14         # FP32-pipe instructions of one compensated pair (survey estimate)
+# FP32 lane-operations the tiled kernel issues per compensated pair: per node and thread
+# 6 scalar ops shared by its 4 points, per packed pair of points 8 f32x2 ops (2 lanes each)
+# -> (6 + 2 x 16) / 4 = 9.5
+FP32_OPS_KAHAN = 9.5
 OPS_PER_PAIR = 16           # algorithmic work of a pair: 15 floating-point operations + 1 exp
 
 DECK_TEXT = {
@@ -57,6 +62,10 @@ DECK_TEXT = {
     "snapshot_sweep": "256 independent Snapshots decks (seed 0): P~U(100,400) W, v~U(0.5,2) m/s, "
                       "width~U(40,120) um, U{1..30} x 2 mm tracks, grids U{50..400}^2 x U{10..60} at 10 um, "
                       "snapshot at 100 %",
+    "adjoint_calibration": "serpentine path and material of the Surface deck on a 300x300x60 grid; loss = sum "
+                           "(T - T_target)^2 over 4096 seeded probes x 3 times (0.05/0.15/0.30 s), target from "
+                           "P x 1.1, Width_X x 0.9, alpha x 1.05; one step = forward + adjoint over all 208 "
+                           "parameters",
 }
 
 
@@ -198,7 +207,7 @@ def run_solidification(args, th, torch, dev, path, deck, world):
     achieved = track_pairs / (st["ms_track"] / 1e3)
     roof = {"bound": "latency", "kernel": "k_track (persistent Surface loop)",
             "achieved": achieved / 1e9, "peak": peak_pairs / 1e9, "unit": "Gpairs/s", "frac": achieved / peak_pairs,
-            "peak_basis": f"{SM_COUNT} SMs x {clk_mhz:.0f} MHz x min({FP32_LANES}/{FP32_OPS_KAHAN} FP32 issue, "
+            "peak_basis": f"{SM_COUNT} SMs x {clk_mhz:.0f} MHz x min({FP32_LANES}/{FP32_OPS_KAHAN} FP32 lane-ops, "
                           f"{MUFU_LANES} MUFU) pairs/clk",
             "note": "each timestep evaluates ~1e3 points x ~300 nodes in a work queue closed by one grid barrier; "
                     "the loop is bound by per-step latency, not by FP32/MUFU issue or HBM",
@@ -299,7 +308,7 @@ def run_snapshot(args, th, torch, dev, path, deck, world):
     roof = {"bound": "fp32_issue", "kernel": "k_grid_fp32" if args.precision == "fp32" else "k_grid_fp64",
             "achieved": achieved / 1e9, "peak": peak_pairs / 1e9, "unit": "Gpairs/s", "frac": achieved / peak_pairs,
             "achieved_tops": achieved * OPS_PER_PAIR / 1e12, "kernel_ms": kernel_ms, "pairs_per_launch": pairs_last,
-            "peak_basis": f"{SM_COUNT} SMs x {clk_mhz:.0f} MHz x min({FP32_LANES}/{FP32_OPS_KAHAN} FP32 issue, "
+            "peak_basis": f"{SM_COUNT} SMs x {clk_mhz:.0f} MHz x min({FP32_LANES}/{FP32_OPS_KAHAN} FP32 lane-ops, "
                           f"{MUFU_LANES} MUFU) pairs/clk",
             "hbm": {"algorithmic_bytes": int(8 * pnum + counts[-1] * 104), "peak_gbs": pk.get("hbm_gbs"),
                     "achieved_gbs": (8 * pnum + counts[-1] * 104) / (kernel_ms / 1e3) / 1e9, "peak_source": src},
@@ -375,7 +384,7 @@ def run_sweep(args, th, torch, dev, paths, deck, world):
             "achieved": achieved / 1e9, "peak": peak_pairs / 1e9, "unit": "Gpairs/s", "frac": achieved / peak_pairs,
             "achieved_tops": achieved * OPS_PER_PAIR / 1e12, "kernel_ms": kernel_ms,
             "pairs_per_launch": pairs_per_step,
-            "peak_basis": f"{SM_COUNT} SMs x {clk_mhz:.0f} MHz x min({FP32_LANES}/{FP32_OPS_KAHAN} FP32 issue, "
+            "peak_basis": f"{SM_COUNT} SMs x {clk_mhz:.0f} MHz x min({FP32_LANES}/{FP32_OPS_KAHAN} FP32 lane-ops, "
                           f"{MUFU_LANES} MUFU) pairs/clk",
             "hbm": {"algorithmic_bytes": int(8 * pnum), "peak_gbs": pk.get("hbm_gbs"),
                     "achieved_gbs": 8 * pnum / (kernel_ms / 1e3) / 1e9, "peak_source": src},
@@ -386,6 +395,58 @@ def run_sweep(args, th, torch, dev, paths, deck, world):
             "detail": {"pairs_per_step": pairs_per_step, "points": pnum, "decks": len(paths)}}
 
 
+# ------------------------------------------------------------------ adjoint workload
+def run_adjoint(args, th, torch, dev, path, deck, world):
+    """One step = forward temperatures at the probes + the adjoint gradient (host dual walk
+    with tangents, device per-node adjoint sums), through the public API."""
+    decks = importlib.import_module("3dthesis_gb300.decks")
+    probes, times = decks.adjoint_probes(deck)
+    adj = th.Adjoint(path, np.asarray(probes, dtype=np.int64), times, args.precision)
+    theta = adj.params()
+    tt = theta.copy()
+    tt[0] *= 1.1
+    tt[2] *= 0.9
+    tt[5] *= 1.05
+    target = adj.forward(tt)
+    nodes = [adj.host_nodes(theta, i)[0].shape[1] for i in range(len(times))]
+    pairs_per_step = 2 * sum(nodes) * len(probes)          # forward sums + adjoint sums
+
+    def step():
+        T = adj.forward(theta)
+        return adj.backward(2.0 * (T - target))
+
+    for _ in range(args.warmup):
+        step()
+    barrier(world)
+    clocks = ClockSampler(dev.index or 0)
+    clocks.start()
+    wall = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        step()
+        wall.append(time.perf_counter() - t0)
+    clk = clocks.stop()
+    barrier(world)
+    total_s = allreduce_max(sum(wall), world)
+    value = pairs_per_step * args.steps * world / total_s
+    # the host walk alone (tangents over every parameter), for the split of the step
+    t0 = time.perf_counter()
+    for i in range(len(times)):
+        adj.host_nodes(theta, i, tangents=True)
+    host_s = time.perf_counter() - t0
+    e2e = {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": int(8 * 8 * sum(nodes) * 2 + 8 * len(probes) * 3),
+           "d2h_bytes_per_step": int(8 * len(probes) * len(times) + 7 * 8 * sum(nodes)), "ms_per_step": 1e3 * total_s / args.steps,
+           "includes": "host node walks (values, then tangents), node uploads, forward and adjoint kernels, D2H"}
+    roof = {"bound": "host walk", "note": "the dual-number node walk (tangents over every parameter) runs on the "
+            "host; host_walk_ms_per_step is its share of the step", "host_walk_ms_per_step": 1e3 * host_s,
+            "achieved": value / 1e9, "unit": "Gpairs/s", "peak": None, "frac": None, "traffic": None}
+    adj.close()
+    return {"value": value, "ms_per_step": 1e3 * total_s / args.steps, "e2e": e2e, "roofline": roof,
+            "clocks": clk, "gpu_launches": 2 * len(times) * args.steps * 2,
+            "detail": {"pairs_per_step": pairs_per_step, "nodes_per_time": nodes, "params": int(theta.size)}}
+
+
 # ------------------------------------------------------------------ CPU oracle legs
 def cpu_sample(path, workload, threads, budget_s):
     """The CPU oracle on the same deck: solidification runs a prefix of the timesteps,
@@ -393,6 +454,20 @@ def cpu_sample(path, workload, threads, budget_s):
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_lib
     oracle_lib.load()
+    if workload == "adjoint_calibration":
+        decks = importlib.import_module("3dthesis_gb300.decks")
+        deck = decks.adjoint_calibration()
+        probes, times = decks.adjoint_probes(deck)
+        o = oracle_lib.Oracle(path)
+        pts = np.asarray(probes, dtype=np.int64)
+        pairs, used, n = 0, 0.0, 0
+        while used < budget_s and n < 60:
+            p0, t0 = o.pairs, time.perf_counter()
+            o.calc_T(times[n % len(times)], pts, threads=threads)
+            used += time.perf_counter() - t0
+            pairs += o.pairs - p0
+            n += 1
+        return pairs / used, f"{n} probe-temperature evaluations (4096 probes) on the oracle ({used:.1f} s)"
     if workload == "snapshot_sweep":
         pairs, used, n = 0, 0.0, 0
         while used < budget_s and n < len(path):
@@ -478,7 +553,7 @@ def main():
     tmp = tempfile.mkdtemp(prefix="thesis_bench_")
     deck, path = make_deck(args.workload, tmp)
     runner = {"surface_serpentine": run_solidification, "snapshot_raster": run_snapshot,
-              "snapshot_sweep": run_sweep}[args.workload]
+              "snapshot_sweep": run_sweep, "adjoint_calibration": run_adjoint}[args.workload]
     r = runner(args, th, torch, dev, path, deck, world)
     line = {"metric": METRIC, "value": r["value"], "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
