@@ -53,6 +53,9 @@ MUFU_LANES = 16             # MUFU.EX2 results per SM per clock
 # -> (6 + 2 x 16) / 4 = 9.5
 FP32_OPS_KAHAN = 9.5
 OPS_PER_PAIR = 16           # algorithmic work of a pair: 15 floating-point operations + 1 exp
+# DRAM bytes (read + write) of one launch of the dominant kernel, from one ncu capture of
+# that kernel on that deck (dram__bytes_read.sum + dram__bytes_write.sum)
+NCU_TRAFFIC = {"snapshot_raster": 21248}
 
 DECK_TEXT = {
     "surface_serpentine": "Solidification/Surface; 50 tracks x 5 mm serpentine, hatch 80 um, 0.8 m/s, P=200 W, "
@@ -312,7 +315,7 @@ def run_snapshot(args, th, torch, dev, path, deck, world):
                           f"{MUFU_LANES} MUFU) pairs/clk",
             "hbm": {"algorithmic_bytes": int(8 * pnum + counts[-1] * 104), "peak_gbs": pk.get("hbm_gbs"),
                     "achieved_gbs": (8 * pnum + counts[-1] * 104) / (kernel_ms / 1e3) / 1e9, "peak_source": src},
-            "traffic": None}
+            "traffic": NCU_TRAFFIC.get(args.workload) if args.precision == "fp32" else None}
     sim.close()
     return {"value": value, "ms_per_step": 1e3 * total_s / args.steps, "e2e": e2e, "roofline": roof,
             "clocks": clk, "gpu_launches": 2 * len(times) * args.steps,
