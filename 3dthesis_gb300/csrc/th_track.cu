@@ -1161,6 +1161,87 @@ __device__ void point_sums(const DevProblem& P, double x, double y, double z, do
   }
 }
 
+// The same sums in the FP32 form: the walk and each node's time, t - t', position and
+// offset from the point stay FP64; the inverse widths, amplitude, exponential and the six
+// sums (Kahan-compensated) are FP32.  The line position uses the segment's reciprocal
+// duration, formed once per interval.
+template <bool GRAD>
+__device__ void point_sums_f32(const DevProblem& P, double x, double y, double z, double t, bool is_sol,
+                               PointSums& o, unsigned long long& pairs, int& err) {
+  float s[6] = {0, 0, 0, 0, 0, 0}, c[6] = {0, 0, 0, 0, 0, 0};
+  auto kahan = [&](int j, float v) {
+    const float yy = v - c[j], tt = s[j] + yy;
+    c[j] = (tt - s[j]) - yy;
+    s[j] = tt;
+  };
+  auto add = [&](double nx0, double ny0, double nz0, double ct, double qb, double dtau, const DevBeam& B) {
+    const float fx = (float)(B.ax2 + ct), fy = (float)(B.ay2 + ct), fz = (float)(B.az2 + ct);
+    const float ipx = __frcp_rn(fx), ipy = __frcp_rn(fy), ipz = __frcp_rn(fz);
+    const float amp = (float)qb * __frsqrt_rn(fx * fy * fz);
+    const float fdt = (float)dtau;
+    for (int im = 0; im < P.n_images; ++im) {
+      double nx = nx0, ny = ny0, nz = nz0;
+      if (im) {
+        nx = image_coord(P.img[im][0], P.bcx0, P.bcx1, nx0);
+        ny = image_coord(P.img[im][1], P.bcy0, P.bcy1, ny0);
+        nz = image_coord(P.img[im][2], P.bcz0, P.bcz1, nz0);
+      }
+      const float dx = (float)(x - nx), dy = (float)(y - ny), dz = (float)(z - nz);
+      const float e = (float)kNeg3Log2e * ((dx * dx * ipx + dy * dy * ipy) + dz * dz * ipz);
+      const float phi = amp * ex2_approx(e);
+      const float seg = fdt * phi;
+      kahan(0, seg);
+      if (GRAD) {
+        const float ddx = -6.f * ipx, ddy = -6.f * ipy, ddz = -6.f * ipz;
+        const float dpx = ddx * dx, dpy = ddy * dy, dpz = ddz * dz;
+        kahan(1, seg * dpx); kahan(2, seg * dpy); kahan(3, seg * dpz);
+        kahan(4, seg * (((dpx * dpx + dpy * dpy) + dpz * dpz) + ((ddx + ddy) + ddz)));
+        if (dtau == 0) kahan(5, phi);
+      }
+      ++pairs;
+    }
+  };
+  for (int b = 0; b < P.nbeams; ++b) {
+    const DevBeam B = P.beam[b];
+    const DevSeg* path = P.segs + B.seg_off;
+    Walk W;
+    walk_begin(B, path, t, is_sol, W);
+    {
+      const BeamLoc L = beam_loc(P, path, W.t, W.s);
+      const double qb = L.q * B.beta;
+      if (W.t <= B.tlast && qb > 0.0) add(L.x, L.y, L.z, 0.0, qb, 0.0, B);
+    }
+    int steps = 0;
+    while (W.more) {
+      if (++steps > kMaxWalkSteps) { err |= ERR_WALK_LIMIT; break; }
+      walk_interval(B, path, W);
+      const DevSeg cur = path[W.s], prv = path[W.s - 1];
+      const double inv = cur.mode ? 0.0 : 1.0 / (cur.tend - prv.tend);
+      const double h = W.t2 - W.t1;
+      const int base = W.order - 2;
+      for (int kk = base + W.order - 1; kk >= base; --kk) {
+        const double tp = 0.5 * (h * P.gl_loc[kk] + (W.t2 + W.t1));
+        double lx = cur.x, ly = cur.y, lz = cur.z;
+        if (!cur.mode) {
+          const double r = (tp - prv.tend) * inv;
+          lx = prv.x + r * (cur.x - prv.x); ly = prv.y + r * (cur.y - prv.y); lz = prv.z + r * (cur.z - prv.z);
+        }
+        const bool out = (lx > P.rx1) || (lx < P.rx0) || (ly > P.ry1) || (ly < P.ry0);
+        const double qb = (out ? 0.0 : cur.q) * B.beta;
+        const double dtau = 0.5 * h * P.gl_w[kk];
+        if (qb > 0.0 && dtau > 0.0) add(lx, ly, lz, P.a12 * (W.t - tp), qb, dtau, B);
+      }
+      walk_advance(W);
+    }
+  }
+  o.T = (double)s[0] - (double)c[0];
+  o.gx = (double)s[1] - (double)c[1];
+  o.gy = (double)s[2] - (double)c[2];
+  o.gz = (double)s[3] - (double)c[3];
+  o.lap = (double)s[4] - (double)c[4];
+  o.dtt = (double)s[5] - (double)c[5];
+}
+
 // C int abs() applied to a double (the reference's int abs on doubles, src/Grid.cpp:381,535),
 // with the x86-64 conversion result INT_MIN for values outside int.
 __device__ __forceinline__ double int_abs(double x) {
@@ -1177,6 +1258,7 @@ __global__ void k_sol_latest(TrackState S, const SolRec* rec, int nrec) {
 
 // Solidification time by the reference's secant step, then gradient, Laplacian and source
 // sums at that time with the refined schedule, and the derived fields (src/Grid.cpp:316-548).
+template <int PREC>
 __global__ void __launch_bounds__(128) k_solidify(DevProblem P, TrackState S, const SolRec* rec, int nrec) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nrec) return;
@@ -1191,13 +1273,15 @@ __global__ void __launch_bounds__(128) k_solidify(DevProblem P, TrackState S, co
   for (int it = 1;; ++it) {
     const double m = rn_div(rn_sub(T2, T1), rn_sub(t2, t1));
     tsol = rn_add(t1, rn_div(rn_sub(P.TL, T1), m));
-    point_sums<false>(P, x, y, z, tsol, false, ps, pairs, err);
+    if (PREC == 0) point_sums<false>(P, x, y, z, tsol, false, ps, pairs, err);
+    else point_sums_f32<false>(P, x, y, z, tsol, false, ps, pairs, err);
     const double Tt = P.T0 + ps.T;
     const double e = int_abs(rn_sub(1.0, rn_div(Tt, P.TL)));
     if ((e < P.sol_tol) || (it >= P.sol_iter)) break;
     if (Tt > P.TL) { t1 = tsol; T1 = Tt; } else { t2 = tsol; T2 = Tt; }
   }
-  point_sums<true>(P, x, y, z, tsol, true, ps, pairs, err);
+  if (PREC == 0) point_sums<true>(P, x, y, z, tsol, true, ps, pairs, err);
+  else point_sums_f32<true>(P, x, y, z, tsol, true, ps, pairs, err);
   const double G = sqrt(ps.gx * ps.gx + ps.gy * ps.gy + ps.gz * ps.gz);
   const double dTdt = int_abs(rn_add(rn_mul(P.a, ps.lap), ps.dtt));
   const double V = dTdt / G;
@@ -1297,10 +1381,11 @@ void th_launch_notrack_step(const DevProblem& P, const TrackState& S, const Node
 
 void th_launch_solidify(const DevProblem& P, const TrackState& S, const SolRec* rec, int nrec, int precision,
                         bool do_sol, cudaStream_t s) {
-  (void)precision;
   if (nrec <= 0) return;
   k_sol_latest<<<(nrec + 255) / 256, 256, 0, s>>>(S, rec, nrec);
-  if (do_sol) k_solidify<<<(nrec + 127) / 128, 128, 0, s>>>(P, S, rec, nrec);
+  if (!do_sol) return;
+  if (precision == 0) k_solidify<0><<<(nrec + 127) / 128, 128, 0, s>>>(P, S, rec, nrec);
+  else k_solidify<1><<<(nrec + 127) / 128, 128, 0, s>>>(P, S, rec, nrec);
 }
 
 void th_launch_final_field(const DevProblem& P, const TrackState& S, int field, double* out, cudaStream_t s) {

@@ -95,7 +95,9 @@ def test_gradients_at_gpu_solidification_time(runs, oracle, tmp_path, tag, prec)
 
     The quadrature schedule is a discontinuous function of t (a step boundary can land on a
     segment end or the doubling threshold), so the reference's own G can jump by ~1e-3 when
-    t_sol moves by one ulp; comparing at the GPU's own t_sol isolates the gradient sums."""
+    t_sol moves by one ulp; comparing at the GPU's own t_sol isolates the gradient sums.
+    FP64 runs agree to 1e-10; FP32 runs (FP32 exponentials and compensated FP32 sums over
+    FP64 node times and offsets) to 1e-4 relative."""
     deck, ref, gpu = runs[tag]
     g = gpu[prec]
     if "tSol" not in g:
@@ -105,15 +107,18 @@ def test_gradients_at_gpu_solidification_time(runs, oracle, tmp_path, tag, prec)
     rng = np.random.default_rng(5)
     for p in rng.choice(solid, min(400, solid.size), replace=False):
         want = o.solid_fields(p, g["tSol"][p])
+        rel = 1e-10 if prec == "fp64" else 1e-4
         for f in SOL:
             if f not in g:
                 continue
-            if f == "dTdt":
-                assert abs(g[f][p] - want[f]) <= 1.0 + 1e-12 * abs(want[f]), (p, f)
+            if f == "dTdt":       # an integer (the reference's int abs): one unit of truncation
+                assert abs(g[f][p] - want[f]) <= 1.0 + max(1e-12, rel) * abs(want[f]), (p, f)
             elif f in ("Gx", "Gy", "Gz"):
-                assert abs(g[f][p] - want[f]) <= 1e-10, (p, f)
+                assert abs(g[f][p] - want[f]) <= rel, (p, f)
+            elif f == "eqFrac":
+                assert abs(g[f][p] - want[f]) <= rel * max(abs(want[f]), 1e-6), (p, f, g[f][p], want[f])
             else:
-                assert abs(g[f][p] - want[f]) <= 1e-10 * abs(want[f]) + 1e-300, (p, f, g[f][p], want[f])
+                assert abs(g[f][p] - want[f]) <= rel * abs(want[f]) + 1e-300, (p, f, g[f][p], want[f])
 
 
 @pytest.mark.parametrize("tag", sorted(CASES))
