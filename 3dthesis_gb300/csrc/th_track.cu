@@ -856,12 +856,24 @@ __global__ void __launch_bounds__(kTrackThreads, 1) k_track(DevProblem P, TrackS
   int nL_next = k_begin < k_end ? ldcg_i(&C->liq_n[k_begin % 3]) : 0;
   int2 first_next = make_int2(0, 0);
   if (k_begin < k_end && (tid >> 5) < S.list_cap) first_next = __ldcg(S.liq[k_begin % 3] + (tid >> 5));
+  // the window's per-step scalars, read one step ahead
+  double t_next = 0.0;
+  int cnt_next = 0, cntl_next = 0, nseed_next = 0;
+  if (k_begin < k_end) {
+    const int slot = k_begin - W.base + 1;
+    t_next = W.t[slot]; cnt_next = W.count[slot]; cntl_next = W.count[slot - 1]; nseed_next = W.nseed[slot];
+  }
   int k = k_begin;
   for (; k < k_end; ++k) {
     StepCtx X;
     X.ev_n = 0;
     X.ev_c = 0;
     const int slot = k - W.base + 1;
+    const double t_k = t_next;
+    const int cnt_k = cnt_next, cntl_k = cntl_next, nseed_k = nseed_next;
+    if (k + 1 < k_end) {
+      t_next = W.t[slot + 1]; cnt_next = W.count[slot + 1]; cntl_next = cnt_k; nseed_next = W.nseed[slot + 1];
+    }
     const unsigned long long g0 = globaltimer();
     int max_depth = 0;
     const int b0 = k % 3, b1 = (k + 1) % 3;
@@ -870,25 +882,26 @@ __global__ void __launch_bounds__(kTrackThreads, 1) k_track(DevProblem P, TrackS
     X.nL = nL_next;
     const int2 first_entry = first_next;
     // the beam trace runs for k > 0 while t < end + dt (src/Run.cpp:661)
-    X.t = W.t[slot];
+    X.t = t_k;
     const bool seeds = k > 0 && X.t < P.end_time + P.dt;
-    const int n_seed = seeds ? min(W.nseed[slot], W.seed_cap) : 0;
+    const int n_seed = seeds ? min(nseed_k, W.seed_cap) : 0;
     const int* seed = W.seeds + (size_t)slot * W.seed_cap;
     X.n_init = X.nL + n_seed;
-    if (k + 1 < k_end)                      // next step's list, copied while this step runs
-      stage_issue<PREC>(slot_view(W, slot + 1), min(W.count[slot + 1], stage_cap), buf_of(k + 1), stage_cap);
+    // the next step's list is copied while this step runs, issued by each warp when it
+    // first runs out of initial items
+    bool staged = !(k + 1 < k_end);
     X.bb = &bbuf;
     X.st.base = buf_of(k);
     X.st.cap = stage_cap;
-    X.st.n_sm = min(W.count[slot], stage_cap);
+    X.st.n_sm = min(cnt_k, stage_cap);
     X.stl.base = buf_of(k - 1);
     X.stl.cap = stage_cap;
-    X.stl.n_sm = k == 0 ? 0 : min(W.count[slot - 1], stage_cap);
+    X.stl.n_sm = k == 0 ? 0 : min(cntl_k, stage_cap);
     X.k = k;
     X.nb = slot_view(W, slot);
     X.nbl = slot_view(W, slot - 1);
-    X.nn = min(W.count[slot], W.slot_cap);
-    X.nnl = (k == 0) ? 0 : min(W.count[slot - 1], W.slot_cap);
+    X.nn = min(cnt_k, W.slot_cap);
+    X.nnl = (k == 0) ? 0 : min(cntl_k, W.slot_cap);
     X.L = S.liq[b0];
     X.Lo = S.liq[b1];
     X.lo_n = &C->liq_n[b1];
@@ -924,6 +937,10 @@ __global__ void __launch_bounds__(kTrackThreads, 1) k_track(DevProblem P, TrackS
           if (lane == 0) got = claim(S, p, X.stamp);
         }
       } else {
+        if (!staged) {
+          stage_issue<PREC>(slot_view(W, slot + 1), min(cnt_next, stage_cap), buf_of(k + 1), stage_cap);
+          staged = true;
+        }
         if (arrival_pending) {              // this block's entry, checked once its result is back
           arrival_pending = false;
           if (step_over(arrival + kArrive, X.n_init, gridDim.x)) finish_step(P, S, X, k, arrival + kArrive, high_water);
