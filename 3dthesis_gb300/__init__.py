@@ -44,7 +44,7 @@ EXPORTED = ("th_ctx_create_from_deck", "th_ctx_destroy", "th_last_error", "th_ge
             "th_batch_create", "th_batch_destroy", "th_batch_last_error", "th_batch_points", "th_batch_snapshot",
             "th_batch_snapshot_device", "th_batch_set_tile_shape", "th_batch_autotune", "th_batch_pairs",
             "th_adj_create", "th_adj_destroy", "th_adj_last_error", "th_adj_num_params", "th_adj_params",
-            "th_adj_host_nodes", "th_adj_forward", "th_adj_backward")
+            "th_adj_host_nodes", "th_adj_forward", "th_adj_backward", "th_calc_T_times_device")
 
 
 class ThesisError(RuntimeError):
@@ -89,6 +89,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.th_calc_T.argtypes = [vp, c_d, vp, c_i64, vp]
     L.th_calc_T_device.argtypes = [vp, c_d, vp, c_i64, vp, vp]
     L.th_sync.argtypes = [vp, vp]
+    L.th_calc_T_times_device.argtypes = [vp, vp, c_int, vp, c_i64, vp, vp]
     L.th_calc_T_noalloc.argtypes = [vp, c_d, vp, c_i64, vp, vp]
     L.th_run_stats.argtypes = [vp, vp, c_int]
     L.th_run_reset.argtypes = [vp]
@@ -211,6 +212,12 @@ class Simulation:
         instead of memory the context allocates; never allocates device memory."""
         self._check(self._lib.th_calc_T_noalloc(self._ctx, float(t), ctypes.c_void_p(d_pts or None), int(n),
                                                 ctypes.c_void_p(d_T), ctypes.c_void_p(stream or None)))
+
+    def calc_T_times_device(self, times, d_pts: int, n: int, d_T: int, stream: int = 0):
+        """T at every time of ``times`` into device memory d_T (len(times) x n doubles)."""
+        t = np.ascontiguousarray(times, dtype=np.float64)
+        self._check(self._lib.th_calc_T_times_device(self._ctx, _ptr(t), t.size, ctypes.c_void_p(d_pts or None),
+                                                     int(n), ctypes.c_void_p(d_T), ctypes.c_void_p(stream or None)))
 
     def sync(self, stream: int = 0):
         self._check(self._lib.th_sync(self._ctx, ctypes.c_void_p(stream or None)))

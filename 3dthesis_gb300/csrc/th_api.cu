@@ -12,6 +12,7 @@
 #include "th_ctx.h"
 #include "th_kernels.h"
 #include "th_nodes.cuh"
+#include "th_track.h"
 
 static thread_local std::string g_create_error;
 
@@ -156,6 +157,9 @@ void th_ctx_destroy(th_ctx* ctx) {
   cudaFree(ctx->d_pts);
   cudaFree(ctx->d_Tlist);
   cudaFree(ctx->d_export);
+  cudaFree(ctx->multi_mem);
+  cudaFree(ctx->d_multi_t);
+  cudaFree(ctx->d_multi_count);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -262,6 +266,60 @@ th_status th_calc_T_device(th_ctx* ctx, double t, const int64_t* d_pts, int64_t 
   th_launch_nodes(ctx->dp, t, false, ctx->nb, ctx->d_small, ctx->d_small + 1, s);
   if (d_pts) th_launch_list_sum(ctx->dp, ctx->nb, ctx->d_small, d_pts, n, d_T, ctx->precision, ctx->d_pairs, s);
   else th_launch_grid_sum(ctx->dp, ctx->nb, ctx->d_small, d_T, ctx->precision, ctx->shape, ctx->d_pairs, s);
+  TH_CUDA(ctx, cudaGetLastError());
+  return TH_OK;
+}
+
+// Node lists of ntimes times in one launch (a block per time, as Integrate_Parallel
+// precomputes several future lists, src/Calc.cpp:21-46), then each time's sum into
+// d_T + i * n.  Enqueued on the stream without host synchronisation; node-list errors are
+// latched for th_sync.
+th_status th_calc_T_times_device(th_ctx* ctx, const double* times, int32_t ntimes, const int64_t* d_pts, int64_t n,
+                                 double* d_T, void* stream) {
+  if (!ctx || !times || ntimes <= 0 || !d_T || n < 0) return th_fail(ctx, TH_ERR_INVALID, "bad argument");
+  if (!d_pts && n != ctx->hp.pnum) return th_fail(ctx, TH_ERR_INVALID, "d_pts == NULL needs n == pnum");
+  TH_CUDA(ctx, cudaSetDevice(ctx->device));
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+  if (ctx->multi_slots < ntimes || ctx->multi_cap != ctx->nb.cap) {
+    TH_CUDA(ctx, cudaStreamSynchronize(s));          // the old buffers may still be read
+    cudaFree(ctx->multi_mem); cudaFree(ctx->d_multi_t); cudaFree(ctx->d_multi_count);
+    ctx->multi_mem = nullptr; ctx->d_multi_t = nullptr; ctx->d_multi_count = nullptr;
+    const int slots = std::max(ntimes, ctx->multi_slots), cap = ctx->nb.cap;
+    TH_CUDA(ctx, cudaMalloc(&ctx->multi_mem, (size_t)slots * cap * (8 * sizeof(double) + 10 * sizeof(float))));
+    TH_CUDA(ctx, cudaMalloc(&ctx->d_multi_t, slots * sizeof(double)));
+    TH_CUDA(ctx, cudaMalloc(&ctx->d_multi_count, slots * sizeof(int)));
+    ctx->multi_slots = slots;
+    ctx->multi_cap = cap;
+  }
+  const size_t cap = (size_t)ctx->multi_slots * ctx->multi_cap;
+  double* d = (double*)ctx->multi_mem;
+  float* f = (float*)(d + 8 * cap);
+  NodeWindow w{};
+  NodeBufView& nb = w.nb;
+  nb.cap = (int)cap;
+  nb.x = d; nb.y = d + cap; nb.z = d + 2 * cap; nb.ipx = d + 3 * cap; nb.ipy = d + 4 * cap; nb.ipz = d + 5 * cap;
+  nb.dtau = d + 6 * cap; nb.amp = d + 7 * cap;
+  nb.kx = f; nb.ky = f + cap; nb.kz = f + 2 * cap; nb.w = f + 3 * cap; nb.xh = f + 4 * cap; nb.xl = f + 5 * cap;
+  nb.yh = f + 6 * cap; nb.yl = f + 7 * cap; nb.zh = f + 8 * cap; nb.zl = f + 9 * cap;
+  w.slot_cap = ctx->multi_cap;
+  w.nslots = ctx->multi_slots;
+  w.count = ctx->d_multi_count;
+  w.t = ctx->d_multi_t;
+  // from pageable memory the copy is staged before the call returns; in stream order it
+  // lands after the previous call's kernels have read the times
+  TH_CUDA(ctx, cudaMemcpyAsync(ctx->d_multi_t, times, ntimes * sizeof(double), cudaMemcpyHostToDevice, s));
+  th_launch_nodes_window(ctx->dp, w, 0, ntimes, false, ctx->d_small + 1, s);
+  for (int i = 0; i < ntimes; ++i) {
+    NodeBufView v = nb;
+    const size_t off = (size_t)i * ctx->multi_cap;
+    v.x += off; v.y += off; v.z += off; v.ipx += off; v.ipy += off; v.ipz += off; v.dtau += off; v.amp += off;
+    v.kx += off; v.ky += off; v.kz += off; v.w += off; v.xh += off; v.xl += off; v.yh += off; v.yl += off;
+    v.zh += off; v.zl += off;
+    v.cap = ctx->multi_cap;
+    double* out = d_T + (size_t)i * n;
+    if (d_pts) th_launch_list_sum(ctx->dp, v, ctx->d_multi_count + i, d_pts, n, out, ctx->precision, ctx->d_pairs, s);
+    else th_launch_grid_sum(ctx->dp, v, ctx->d_multi_count + i, out, ctx->precision, ctx->shape, ctx->d_pairs, s);
+  }
   TH_CUDA(ctx, cudaGetLastError());
   return TH_OK;
 }

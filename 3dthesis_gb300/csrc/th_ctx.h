@@ -34,6 +34,10 @@ struct th_ctx {
   double* d_export = nullptr;  size_t export_bytes = 0;
 
   RunState* run = nullptr;
+
+  // several node lists at once (th_calc_T_times_device): slot-major buffers of nb.cap nodes
+  void* multi_mem = nullptr;   int multi_slots = 0;   int multi_cap = 0;
+  double* d_multi_t = nullptr; int* d_multi_count = nullptr;
 };
 
 th_status th_fail(th_ctx* ctx, th_status code, const std::string& msg);

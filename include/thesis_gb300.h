@@ -116,6 +116,13 @@ th_status th_calc_T_noalloc(th_ctx* ctx, double t, const int64_t* d_pts, int64_t
  * error latched since the last check. */
 th_status th_sync(th_ctx* ctx, void* stream);
 
+/* T at ntimes times into d_T + i * n (device memory): the node lists of all times in one
+ * launch, one block per time (Calc::Integrate_Parallel, src/Calc.cpp:21-46, precomputes
+ * future lists the same way), then one sum per time.  Same stream semantics and latched
+ * errors as th_calc_T_device; successive calls must use one stream. */
+th_status th_calc_T_times_device(th_ctx* ctx, const double* times, int32_t ntimes, const int64_t* d_pts, int64_t n,
+                                 double* d_T, void* stream);
+
 /* Snapshot idx of a Snapshots deck over the whole grid: T for every point (host buffer,
  * pnum doubles).  T_out == NULL leaves the result in the context's device buffer. */
 th_status th_snapshot(th_ctx* ctx, int32_t idx, double* T_out);

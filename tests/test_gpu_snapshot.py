@@ -108,3 +108,17 @@ def test_pair_count(lib, deck_dir, oracle):
         sim.snapshot(0)
         n = sim.integrate(sim.snapshot_times[0])["xb"].size
         assert sim.pairs == n * sim.pnum == 205 * 800000
+
+
+def test_times_in_one_launch_match_single_snapshots(lib, deck_dir):
+    """th_calc_T_times_device (all node lists in one launch) gives every snapshot's T bit
+    for bit as the one-time path."""
+    torch = pytest.importorskip("torch")
+    with lib.Simulation(deck_dir("snapshot_raster"), "fp32") as sim:
+        times = sim.snapshot_times
+        out = torch.empty(len(times) * sim.pnum, dtype=torch.float64, device="cuda")
+        sim.calc_T_times_device(times, 0, sim.pnum, out.data_ptr())
+        sim.sync()
+        got = out.cpu().numpy().reshape(len(times), sim.pnum)
+        for i in range(len(times)):
+            assert np.array_equal(got[i], sim.snapshot(i)), i
