@@ -5,14 +5,14 @@
 // The node list is a function of the parameters through the quadrature walk: node times,
 // weights and positions move with the widths, the diffusivity and the segment end times
 // (which follow the vertices through the segment lengths).  The host re-walks the path in
-// forward-mode dual numbers - the same FP64 operations in the same order as the device walk
-// (src/Calc.cpp:67-211, src/Util.cpp:192-237), so the values are the device's node list
-// bit for bit - and carries each node quantity's derivative with respect to every
-// parameter.  The device kernel recomputes every probe x node term (no pair storage) and
-// sums, per node, the loss gradient with respect to the node's position, inverse widths and
-// weight; the host contracts those with the node tangents.  Discrete choices of the walk
-// (interval counts, Gauss orders, the r_max cut-off) are held fixed, as a finite difference
-// that does not cross one of them sees.
+// FP64 with the same operations in the same order as the device walk (src/Calc.cpp:67-211,
+// src/Util.cpp:192-237), so the values are the device's node list bit for bit, while
+// recording the walk for differentiation.  The device kernel recomputes every probe x node
+// term (no pair storage) and sums, per node, the loss gradient with respect to the node's
+// position, inverse widths and weight; a reverse sweep over the recorded walk carries those
+// to every parameter at once.  (A forward-mode walk in dual numbers gives the node tangents
+// themselves, for inspection.)  Discrete choices of the walk (interval counts, Gauss orders,
+// the r_max cut-off) are held fixed, as a finite difference that does not cross one sees.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -30,7 +30,7 @@ using namespace thdev;
 
 namespace {
 
-// ------------------------------------------------------------------ dual numbers
+// ------------------------------------------------------------------ forward mode
 // Value and gradient over the parameter vector; an empty gradient is a constant.
 struct Dual {
   double v = 0.0;
@@ -38,13 +38,6 @@ struct Dual {
   Dual() = default;
   Dual(double x) : v(x) {}
 };
-
-Dual variable(double x, int i, int np) {
-  Dual r(x);
-  r.d.assign(np, 0.0);
-  r.d[i] = 1.0;
-  return r;
-}
 
 // r.d = a * x.d + b * y.d, treating an empty gradient as zero
 void combine(Dual& r, double a, const Dual& x, double b, const Dual& y) {
@@ -71,30 +64,54 @@ Dual dsqrt(const Dual& x) {
   return r;
 }
 
-// ------------------------------------------------------------------ the walk in duals
-struct DSeg { Dual x, y, z, tend, rt0; double q, prm; int mode; };
-struct DBeam { Dual az, ax2, ay2, az2, nond, beta, tlast, a12; int nseg; };
+// ------------------------------------------------------------------ reverse mode
+// A value recorded on the tape: entry i has up to two parents with their partial
+// derivatives; the first np entries are the parameters.  i < 0 is a constant.
+struct TapeEntry { int a, b; double da, db; };
+thread_local std::vector<TapeEntry>* g_tape = nullptr;
 
-struct DNode { Dual x, y, z, ipx, ipy, ipz, dtau, amp; };
-
-struct DWalk {
-  double t;
-  Dual t1, t2, tpp, stepmax, step0;
-  int s, order;
-  bool more, sw;
+struct Rev {
+  double v = 0.0;
+  int i = -1;
+  Rev() = default;
+  Rev(double x) : v(x) {}
 };
 
+Rev record(double v, const Rev& x, double dx, const Rev& y, double dy) {
+  Rev r(v);
+  if (x.i < 0 && y.i < 0) return r;
+  r.i = (int)g_tape->size();
+  g_tape->push_back({x.i, y.i, dx, dy});
+  return r;
+}
+Rev operator+(const Rev& x, const Rev& y) { return record(x.v + y.v, x, 1.0, y, 1.0); }
+Rev operator-(const Rev& x, const Rev& y) { return record(x.v - y.v, x, 1.0, y, -1.0); }
+Rev operator*(const Rev& x, const Rev& y) { return record(x.v * y.v, x, y.v, y, x.v); }
+Rev operator/(const Rev& x, const Rev& y) { return record(x.v / y.v, x, 1.0 / y.v, y, -(x.v / y.v) / y.v); }
+Rev dsqrt(const Rev& x) {
+  const double s = std::sqrt(x.v);
+  return record(s, x, s > 0.0 ? 0.5 / s : 0.0, Rev(), 0.0);
+}
+
+// ------------------------------------------------------------------ the walk, on either
+template <class N> struct DSeg { N x, y, z, tend, rt0; double q, prm; int mode; };
+template <class N> struct DBeam { N az, ax2, ay2, az2, nond, beta, tlast, a12; int nseg; };
+template <class N> struct DNode { N x, y, z, ipx, ipy, ipz, dtau, amp; };
+template <class N> struct DLoc { N x, y, z; double q; };
+
 // src/Util.cpp:192-209
-Dual ref_time(const DBeam& B, const std::vector<DSeg>& path, const Dual& tpp, int s) {
-  Dual spp = tpp / B.nond;
-  if (spp.v < 0.0) spp = Dual(0.0);
-  if (path[s].mode == 0) return path[s].rt0 * dsqrt(Dual(12.0) * spp + Dual(1.0));
-  Dual r = path[s].tend - path[s - 1].tend;
-  if (r.v == 0) r = Dual(1.0e-9);
+template <class N>
+N ref_time(const DBeam<N>& B, const std::vector<DSeg<N>>& path, const N& tpp, int s) {
+  N spp = tpp / B.nond;
+  if (spp.v < 0.0) spp = N(0.0);
+  if (path[s].mode == 0) return path[s].rt0 * dsqrt(N(12.0) * spp + N(1.0));
+  N r = path[s].tend - path[s - 1].tend;
+  if (r.v == 0) r = N(1.0e-9);
   return r;
 }
 
-int find_seg(const std::vector<DSeg>& path, double t) {
+template <class N>
+int find_seg(const std::vector<DSeg<N>>& path, double t) {
   int lo = 1, hi = (int)path.size() - 1;
   while (lo < hi) {
     const int mid = (lo + hi) >> 1;
@@ -103,17 +120,16 @@ int find_seg(const std::vector<DSeg>& path, double t) {
   return lo;
 }
 
-struct DLoc { Dual x, y, z; double q; };
-
 // src/Util.cpp:211-237 with the r_max cut-off of src/Util.cpp:168-172
-DLoc beam_loc(const DevProblem& P, const std::vector<DSeg>& path, const Dual& t, int s) {
-  const DSeg& cur = path[s];
-  DLoc L;
+template <class N>
+DLoc<N> beam_loc(const DevProblem& P, const std::vector<DSeg<N>>& path, const N& t, int s) {
+  const DSeg<N>& cur = path[s];
+  DLoc<N> L;
   if (cur.mode) {
     L.x = cur.x; L.y = cur.y; L.z = cur.z;
   } else {
-    const DSeg& prv = path[s - 1];
-    const Dual r = (t - prv.tend) / (cur.tend - prv.tend);
+    const DSeg<N>& prv = path[s - 1];
+    const N r = (t - prv.tend) / (cur.tend - prv.tend);
     L.x = prv.x + r * (cur.x - prv.x);
     L.y = prv.y + r * (cur.y - prv.y);
     L.z = prv.z + r * (cur.z - prv.z);
@@ -123,11 +139,12 @@ DLoc beam_loc(const DevProblem& P, const std::vector<DSeg>& path, const Dual& t,
   return L;
 }
 
-DNode finish_node(const DBeam& B, const Dual& ct, const Dual& qb, const Dual& dtau, const DLoc& L) {
-  const Dual phx = B.ax2 + ct, phy = B.ay2 + ct, phz = B.az2 + ct;
-  DNode v;
+template <class N>
+DNode<N> finish_node(const DBeam<N>& B, const N& ct, const N& qb, const N& dtau, const DLoc<N>& L) {
+  const N phx = B.ax2 + ct, phy = B.ay2 + ct, phz = B.az2 + ct;
+  DNode<N> v;
   v.x = L.x; v.y = L.y; v.z = L.z;
-  v.ipx = Dual(1.0) / phx; v.ipy = Dual(1.0) / phy; v.ipz = Dual(1.0) / phz;
+  v.ipx = N(1.0) / phx; v.ipy = N(1.0) / phy; v.ipz = N(1.0) / phz;
   v.dtau = dtau;
   v.amp = qb / dsqrt((phx * phy) * phz);
   return v;
@@ -135,56 +152,54 @@ DNode finish_node(const DBeam& B, const Dual& ct, const Dual& qb, const Dual& dt
 
 // The node list at t in the device's order (zero-weight node, then each interval's Gauss
 // points from the late end); returns false when the walk exceeds its step limit.
-bool walk_nodes(const DevProblem& P, const DBeam& B, const std::vector<DSeg>& path, double t, bool is_sol,
-                std::vector<DNode>& out) {
-  DWalk W;
-  W.t = t;
-  W.s = find_seg(path, t);
-  W.step0 = is_sol ? B.nond * B.az : B.nond;
-  W.stepmax = W.step0;
-  W.order = 16;
-  W.t2 = Dual(t); W.t1 = Dual(t); W.tpp = Dual(0.0);
-  if (t > B.tlast.v) { W.tpp = W.tpp + (Dual(t) - B.tlast); W.t2 = B.tlast; }
+template <class N>
+bool walk_nodes(const DevProblem& P, const DBeam<N>& B, const std::vector<DSeg<N>>& path, double t, bool is_sol,
+                std::vector<DNode<N>>& out) {
+  N t1, t2, tpp, stepmax, step0;
+  int s = find_seg(path, t), order = 16;
+  step0 = is_sol ? B.nond * B.az : B.nond;
+  stepmax = step0;
+  t2 = N(t); t1 = N(t); tpp = N(0.0);
+  if (t > B.tlast.v) { tpp = tpp + (N(t) - B.tlast); t2 = B.tlast; }
   int guard = 0;
-  while (W.tpp.v >= (Dual(2.0) * W.stepmax - W.step0).v && guard++ < 4096) {
-    W.stepmax = W.stepmax * Dual(2.0);
-    if (W.order != 2) W.order /= 2;
+  while (tpp.v >= (N(2.0) * stepmax - step0).v && guard++ < 4096) {
+    stepmax = stepmax * N(2.0);
+    if (order != 2) order /= 2;
   }
-  W.more = true;
-  W.sw = false;
+  bool more = true, sw = false;
   {  // src/Calc.cpp:124-132
-    const DLoc L = beam_loc(P, path, Dual(t), W.s);
-    if (t <= B.tlast.v && L.q * B.beta.v > 0.0) out.push_back(finish_node(B, Dual(0.0), Dual(L.q) * B.beta, Dual(0.0), L));
+    const DLoc<N> L = beam_loc(P, path, N(t), s);
+    if (t <= B.tlast.v && L.q * B.beta.v > 0.0) out.push_back(finish_node(B, N(0.0), N(L.q) * B.beta, N(0.0), L));
   }
   int steps = 0;
-  while (W.more) {
+  while (more) {
     if (++steps > kMaxWalkSteps) return false;
-    const Dual rt = ref_time(B, path, W.tpp, W.s);
-    const Dual use = (rt.v < W.stepmax.v) ? rt : W.stepmax;
-    W.t1 = W.t2 - use;
-    const Dual next = path[W.s - 1].tend;
-    W.sw = false;
-    if (W.t1.v <= next.v) {
-      W.t1 = next;
-      if (next.v > 0.0) W.sw = true; else W.more = false;
+    const N rt = ref_time(B, path, tpp, s);
+    const N use = (rt.v < stepmax.v) ? rt : stepmax;
+    t1 = t2 - use;
+    const N next = path[s - 1].tend;
+    sw = false;
+    if (t1.v <= next.v) {
+      t1 = next;
+      if (next.v > 0.0) sw = true; else more = false;
     }
-    const int base = W.order - 2;
-    for (int k = base + W.order - 1; k >= base; --k) {       // src/Calc.cpp:176-190
-      const Dual h = W.t2 - W.t1;
-      const Dual tp = Dual(0.5) * ((h * Dual(P.gl_loc[k])) + (W.t2 + W.t1));
-      const Dual ct = B.a12 * (Dual(t) - tp);
-      const DLoc L = beam_loc(P, path, tp, W.s);
-      const Dual qb = Dual(L.q) * B.beta;
-      const Dual dtau = (Dual(0.5) * h) * Dual(P.gl_w[k]);
+    const int base = order - 2;
+    for (int k = base + order - 1; k >= base; --k) {         // src/Calc.cpp:176-190
+      const N h = t2 - t1;
+      const N tp = N(0.5) * ((h * N(P.gl_loc[k])) + (t2 + t1));
+      const N ct = B.a12 * (N(t) - tp);
+      const DLoc<N> L = beam_loc(P, path, tp, s);
+      const N qb = N(L.q) * B.beta;
+      const N dtau = (N(0.5) * h) * N(P.gl_w[k]);
       if (!(qb.v > 0.0 && dtau.v > 0.0)) continue;
       out.push_back(finish_node(B, ct, qb, dtau, L));
     }
-    if (W.sw) W.s--;                                           // src/Calc.cpp:192-207
-    W.tpp = W.tpp + (W.t2 - W.t1);
-    W.t2 = W.t1;
-    if (W.tpp.v >= (Dual(2.0) * W.stepmax - W.step0).v) {
-      W.stepmax = W.stepmax * Dual(2.0);
-      if (W.order != 2) W.order /= 2;
+    if (sw) s--;                                              // src/Calc.cpp:192-207
+    tpp = tpp + (t2 - t1);
+    t2 = t1;
+    if (tpp.v >= (N(2.0) * stepmax - step0).v) {
+      stepmax = stepmax * N(2.0);
+      if (order != 2) order /= 2;
     }
   }
   return true;
@@ -287,6 +302,7 @@ struct th_adj {
   std::vector<double> theta;        // parameters of the last forward
   int nvert = 0;                    // path segments after the origin (vertices)
   std::string err;
+  std::vector<TapeEntry> tape;      // the recorded walk of the last backward
   // device (allocated at the first forward)
   int device = -1;
   cudaStream_t stream = nullptr;
@@ -316,43 +332,42 @@ th_status afail(th_adj* a, th_status st, const std::string& m) {
     if (e_ != cudaSuccess) return afail((a), TH_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
   } while (0)
 
-// The dual problem for parameters theta (gradients only when np > 0).
-void build_dual(const th_adj& A, const double* th, int np, DBeam& B, std::vector<DSeg>& path) {
-  auto var = [&](double x, int i) { return np ? variable(x, i, np) : Dual(x); };
-  const Dual P = var(th[0], 0), eta = var(th[1], 1), ax = var(th[2], 2), ay = var(th[3], 3), az = var(th[4], 4),
-             a = var(th[5], 5);
-  const Dual q = (P * eta) * Dual(2.0);                           // src/Init.cpp:862-865
+// The walk's inputs for parameters theta; var(x, i) makes parameter i.
+template <class N, class Var>
+void build_problem(const th_adj& A, const double* th, Var var, DBeam<N>& B, std::vector<DSeg<N>>& path) {
+  const N P = var(th[0], 0), eta = var(th[1], 1), ax = var(th[2], 2), ay = var(th[3], 3), az = var(th[4], 4),
+          a = var(th[5], 5);
+  const N q = (P * eta) * N(2.0);                                // src/Init.cpp:862-865
   B.az = az;
   B.ax2 = ax * ax; B.ay2 = ay * ay; B.az2 = az * az;
   B.nond = (ax * ax) / a;
-  B.beta = (Dual(std::pow(3.0 / 3.14159265358979323846, 1.5)) * q) / Dual(A.hp.rho * A.hp.cps);
-  B.a12 = Dual(12.0) * a;
+  B.beta = (N(std::pow(3.0 / 3.14159265358979323846, 1.5)) * q) / N(A.hp.rho * A.hp.cps);
+  B.a12 = N(12.0) * a;
   const std::vector<DevSeg>& hpath = A.hp.paths[0];
-  path.assign(hpath.size(), DSeg());
+  path.assign(hpath.size(), DSeg<N>());
   for (size_t k = 0; k < hpath.size(); ++k) {
-    DSeg& s = path[k];
+    DSeg<N>& s = path[k];
     s.mode = hpath[k].mode; s.q = hpath[k].q; s.prm = hpath[k].prm;
-    if (k == 0) { s.x = Dual(hpath[0].x); s.y = Dual(hpath[0].y); s.z = Dual(hpath[0].z); s.tend = Dual(0.0); continue; }
+    if (k == 0) { s.x = N(hpath[0].x); s.y = N(hpath[0].y); s.z = N(hpath[0].z); s.tend = N(0.0); continue; }
     s.x = var(th[6 + 2 * (k - 1)], 6 + 2 * (int)(k - 1));
     s.y = var(th[7 + 2 * (k - 1)], 7 + 2 * (int)(k - 1));
-    s.z = Dual(hpath[k].z);
-    if (s.mode) s.tend = path[k - 1].tend + Dual(s.prm);
+    s.z = N(hpath[k].z);
+    if (s.mode) s.tend = path[k - 1].tend + N(s.prm);         // src/Init.cpp path times
     else {
-      const Dual dx = s.x - path[k - 1].x, dy = s.y - path[k - 1].y, dz = s.z - path[k - 1].z;
-      s.tend = path[k - 1].tend + dsqrt((dx * dx + dy * dy) + dz * dz) / Dual(s.prm);
+      const N dx = s.x - path[k - 1].x, dy = s.y - path[k - 1].y, dz = s.z - path[k - 1].z;
+      s.tend = path[k - 1].tend + dsqrt((dx * dx + dy * dy) + dz * dz) / N(s.prm);
     }
-    s.rt0 = s.mode == 0 ? (Dual(0.58870501125) * ax) / Dual(s.prm) : Dual(0.0);
+    s.rt0 = s.mode == 0 ? (N(0.58870501125) * ax) / N(s.prm) : N(0.0);
   }
   B.tlast = path.back().tend;
   B.nseg = (int)path.size();
 }
 
-th_status node_lists(th_adj* A, const double* th, int np, std::vector<std::vector<DNode>>& lists) {
-  DBeam B;
-  std::vector<DSeg> path;
-  build_dual(*A, th, np, B, path);
-  // the walk's DevProblem fields that do not follow the parameters: Gauss tables, r_max box,
-  // Depth_Z of the solidification schedule
+template <class N, class Var>
+th_status node_lists(th_adj* A, const double* th, Var var, std::vector<std::vector<DNode<N>>>& lists) {
+  DBeam<N> B;
+  std::vector<DSeg<N>> path;
+  build_problem<N>(*A, th, var, B, path);
   lists.assign(A->times.size(), {});
   for (size_t i = 0; i < A->times.size(); ++i)
     if (!walk_nodes(A->dp, B, path, A->times[i], false, lists[i]))
@@ -397,11 +412,12 @@ th_status ensure_device(th_adj* A, int nmax) {
 }
 
 // Uploads one node list's values and derives the float fields (enqueued on the stream).
-th_status upload_nodes(th_adj* A, const std::vector<DNode>& L) {
+template <class N>
+th_status upload_nodes(th_adj* A, const std::vector<DNode<N>>& L) {
   const int n = (int)L.size();
   std::vector<double> h((size_t)8 * n);
   for (int i = 0; i < n; ++i) {
-    const DNode& v = L[i];
+    const DNode<N>& v = L[i];
     const double f[8] = {v.x.v, v.y.v, v.z.v, v.ipx.v, v.ipy.v, v.ipz.v, v.dtau.v, v.amp.v};
     for (int j = 0; j < 8; ++j) h[(size_t)j * n + i] = f[j];
   }
@@ -413,6 +429,8 @@ th_status upload_nodes(th_adj* A, const std::vector<DNode>& L) {
   ACUDA(A, cudaStreamSynchronize(A->stream));      // h and n leave scope
   return TH_OK;
 }
+
+auto constant_var = [](double x, int) { return Rev(x); };
 
 }  // namespace
 
@@ -474,13 +492,18 @@ th_status th_adj_host_nodes(th_adj* A, const double* theta, int32_t time_idx, do
   if (!A || !theta || !n_out || time_idx < 0 || time_idx >= (int)A->times.size())
     return afail(A, TH_ERR_INVALID, "bad argument");
   const int np = tangents ? th_adj_num_params(A) : 0;
-  std::vector<std::vector<DNode>> lists;
+  auto var = [np](double x, int i) {
+    Dual r(x);
+    if (np) { r.d.assign(np, 0.0); r.d[i] = 1.0; }
+    return r;
+  };
+  std::vector<std::vector<DNode<Dual>>> lists;
   const std::vector<double> keep = A->times;
   A->times.assign(1, keep[time_idx]);
-  th_status st = node_lists(A, theta, np, lists);
+  th_status st = node_lists<Dual>(A, theta, var, lists);
   A->times = keep;
   if (st != TH_OK) return st;
-  const std::vector<DNode>& L = lists[0];
+  const std::vector<DNode<Dual>>& L = lists[0];
   *n_out = (int)L.size();
   const int n = std::min<int>((int)L.size(), cap);
   for (int i = 0; i < n; ++i) {
@@ -497,8 +520,8 @@ th_status th_adj_host_nodes(th_adj* A, const double* theta, int32_t time_idx, do
 
 th_status th_adj_forward(th_adj* A, const double* theta, double* T_out) {
   if (!A || !theta || !T_out) return afail(A, TH_ERR_INVALID, "null argument");
-  std::vector<std::vector<DNode>> lists;
-  th_status st = node_lists(A, theta, 0, lists);
+  std::vector<std::vector<DNode<Rev>>> lists;
+  th_status st = node_lists<Rev>(A, theta, constant_var, lists);   // values only: nothing recorded
   if (st != TH_OK) return st;
   A->theta.assign(theta, theta + th_adj_num_params(A));
   int nmax = 1;
@@ -518,17 +541,26 @@ th_status th_adj_forward(th_adj* A, const double* theta, double* T_out) {
 th_status th_adj_backward(th_adj* A, const double* dL_dT, double* dL_dtheta) {
   if (!A || !dL_dT || !dL_dtheta) return afail(A, TH_ERR_INVALID, "null argument");
   const int npar = th_adj_num_params(A);
-  std::vector<std::vector<DNode>> lists;
-  th_status st = node_lists(A, A->theta.data(), npar, lists);   // recomputed with tangents
+  // re-walk at the last forward's theta, recording every operation; the parameters are the
+  // tape's first npar entries
+  A->tape.clear();
+  A->tape.reserve(1 << 20);
+  for (int j = 0; j < npar; ++j) A->tape.push_back({-1, -1, 0.0, 0.0});
+  g_tape = &A->tape;
+  auto var = [](double x, int i) { Rev r(x); r.i = i; return r; };
+  std::vector<std::vector<DNode<Rev>>> lists;
+  th_status st = node_lists<Rev>(A, A->theta.data(), var, lists);
+  g_tape = nullptr;
   if (st != TH_OK) return st;
   int nmax = 1;
   for (const auto& L : lists) nmax = std::max<int>(nmax, (int)L.size());
   if ((st = ensure_device(A, nmax)) != TH_OK) return st;
-  std::fill(dL_dtheta, dL_dtheta + npar, 0.0);
+  std::vector<double> adj(A->tape.size(), 0.0);
+  auto seed = [&](const Rev& q, double g) { if (q.i >= 0) adj[q.i] += g; };
   const int np = (int)A->probes.size();
   std::vector<double> G;
   for (size_t i = 0; i < lists.size(); ++i) {
-    const std::vector<DNode>& L = lists[i];
+    const std::vector<DNode<Rev>>& L = lists[i];
     const int n = (int)L.size();
     if (n == 0) continue;
     if ((st = upload_nodes(A, L)) != TH_OK) return st;
@@ -543,24 +575,29 @@ th_status th_adj_backward(th_adj* A, const double* dL_dT, double* dL_dtheta) {
     G.resize((size_t)7 * n);
     ACUDA(A, cudaMemcpyAsync(G.data(), A->d_G, (size_t)7 * n * sizeof(double), cudaMemcpyDeviceToHost, A->stream));
     ACUDA(A, cudaStreamSynchronize(A->stream));
-    // chain: dL/dtheta += sum_n G . d(node)/dtheta, with w = dtau * amp
+    // the loss gradient with respect to each node quantity (w = dtau * amp)
     for (int k = 0; k < n; ++k) {
-      const DNode& v = L[k];
+      const DNode<Rev>& v = L[k];
       const double gw = G[(size_t)0 * n + k];
-      auto add = [&](double coef, const Dual& q) {
-        if (coef == 0.0 || q.d.empty()) return;
-        for (int j = 0; j < npar; ++j) dL_dtheta[j] += coef * q.d[j];
-      };
-      add(gw * v.amp.v, v.dtau);
-      add(gw * v.dtau.v, v.amp);
-      add(G[(size_t)1 * n + k], v.x);
-      add(G[(size_t)2 * n + k], v.y);
-      add(G[(size_t)3 * n + k], v.z);
-      add(G[(size_t)4 * n + k], v.ipx);
-      add(G[(size_t)5 * n + k], v.ipy);
-      add(G[(size_t)6 * n + k], v.ipz);
+      seed(v.dtau, gw * v.amp.v);
+      seed(v.amp, gw * v.dtau.v);
+      seed(v.x, G[(size_t)1 * n + k]);
+      seed(v.y, G[(size_t)2 * n + k]);
+      seed(v.z, G[(size_t)3 * n + k]);
+      seed(v.ipx, G[(size_t)4 * n + k]);
+      seed(v.ipy, G[(size_t)5 * n + k]);
+      seed(v.ipz, G[(size_t)6 * n + k]);
     }
   }
+  // reverse sweep over the recorded walk
+  for (size_t i = A->tape.size(); i-- > (size_t)npar;) {
+    const double g = adj[i];
+    if (g == 0.0) continue;
+    const TapeEntry& e = A->tape[i];
+    if (e.a >= 0) adj[e.a] += e.da * g;
+    if (e.b >= 0) adj[e.b] += e.db * g;
+  }
+  for (int j = 0; j < npar; ++j) dL_dtheta[j] = adj[j];
   return TH_OK;
 }
 
