@@ -144,11 +144,13 @@ def barrier(world):
 
 
 def allreduce_max(x, world):
+    """The slowest rank's time (every rank gets it); NCCL reduces on the GPU, gloo on the CPU."""
     if world <= 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
