@@ -184,6 +184,10 @@ __device__ __forceinline__ void gen_list_block(const DevProblem& P, double t, bo
     }
     n = n0 * P.n_images;
   }
+  // zero-weight nodes up to a multiple of four (they add exactly nothing), so that FP32
+  // passes read whole groups of four nodes
+  if (n <= nb.cap)
+    for (int s = n + tid; s < ((n + 3) & ~3) && s < nb.cap; s += kGenThreads) store_node(nb, s, NodeVal{});
   __syncthreads();
   if (tid == 0) {
     int e = sh.err;

@@ -152,6 +152,17 @@ void axis(int& num, double& vmin, double& vmax, double& res, bool guard_is_one) 
   else res = DBL_MAX;
 }
 
+// Division by an invariant divisor d >= 1 for dividends x < 2^31 (Granlund and Montgomery,
+// "Division by invariant integers using multiplication", 1994): with l = ceil(log2 d),
+// s = 31 + l and m = ceil(2^s / d), m < 2^32 and floor(x / d) = floor(x * m / 2^s), because
+// the excess x * (m d - 2^s) / (d 2^s) stays below x / 2^s < 1 / d (m d - 2^s < d <= 2^l).
+void udiv_magic(uint32_t d, uint32_t& m, int32_t& s) {
+  int l = 0;
+  while ((1ull << l) < d) ++l;
+  s = 31 + l;
+  m = (uint32_t)(((1ull << s) + d - 1) / d);
+}
+
 }  // namespace
 
 void th_gauss_tables(double loc[30], double w[30]) {
@@ -390,6 +401,8 @@ void th_make_dev_problem(const HostProblem& hp, const DevSeg* d_segs, DevProblem
   }
   dp.cetN0 = hp.cetN0; dp.cetn = hp.cetn; dp.ceta = hp.ceta;
   dp.nx = hp.nx; dp.ny = hp.ny; dp.nz = hp.nz;
+  udiv_magic((uint32_t)std::max(1, hp.nz), dp.div_nz_m, dp.div_nz_s);
+  udiv_magic((uint32_t)std::max(1, hp.ny), dp.div_ny_m, dp.div_ny_s);
   dp.gx = (uint16_t)hp.nx; dp.gy = (uint16_t)hp.ny; dp.gz = (uint16_t)hp.nz;
   dp.pnum = hp.pnum;
   dp.xmin = hp.xmin; dp.xmax = hp.xmax; dp.ymin = hp.ymin; dp.ymax = hp.ymax; dp.zmin = hp.zmin; dp.zmax = hp.zmax;

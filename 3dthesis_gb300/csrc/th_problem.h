@@ -41,6 +41,9 @@ struct DevProblem {
   double cetN0, cetn, ceta;
   // domain
   int32_t nx, ny, nz;       // axis counts
+  // floor(x / nz) and floor(x / ny) as (x * m) >> s for 0 <= x < 2^31 (point and column ids)
+  uint32_t div_nz_m, div_ny_m;
+  int32_t div_nz_s, div_ny_s;
   int32_t gx, gy, gz;       // the same truncated to uint16_t (the reference grid's width)
   int64_t pnum;
   double xmin, xmax, ymin, ymax, zmin, zmax;

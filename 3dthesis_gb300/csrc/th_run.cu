@@ -579,14 +579,15 @@ th_status th_run_stats(th_ctx* ctx, double* out, int32_t n) {
     st = th_cuda_check(ctx, cudaMemcpy(prof, r->S.C->prof, sizeof(prof), cudaMemcpyDeviceToHost), "cudaMemcpy");
     if (st != TH_OK) return st;
   }
-  const double v[28] = {r ? r->ms_nodes : 0, r ? r->ms_track : 0, r ? r->ms_solid : 0, r ? (double)r->windows : 0,
+  const double v[29] = {r ? r->ms_nodes : 0, r ? r->ms_track : 0, r ? r->ms_solid : 0, r ? (double)r->windows : 0,
                         r ? (double)r->records : 0, r ? (double)r->max_items : 0, r ? (double)r->k : 0,
                         r ? (double)r->slot_cap : 0, r ? r->ms_device : 0, (double)pairs[1],
                         (double)pairs[0], prof[0] * 1e-6, prof[1] * 1e-6, (double)prof[2], (double)prof[3],
                         (double)prof[4], (double)prof[5], (double)prof[6], (double)prof[7], (double)prof[8],
                         prof[10] * 1e-6, prof[11] * 1e-6, prof[12] * 1e-6, prof[13] * 1e-6,
-                        prof[14] * 1e-6, prof[15] * 1e-6, prof[16] * 1e-6, prof[17] * 1e-6};
-  for (int i = 0; i < n && i < 28; ++i) out[i] = v[i];
+                        prof[14] * 1e-6, prof[15] * 1e-6, prof[16] * 1e-6, prof[17] * 1e-6,
+                        (double)prof[9]};
+  for (int i = 0; i < n && i < 29; ++i) out[i] = v[i];
   return TH_OK;
 }
 

@@ -114,36 +114,49 @@ __device__ __forceinline__ double pack_df(float hi, float lo) {
   return __longlong_as_double((long long)(((unsigned long long)__float_as_uint(hi) << 32) | l));
 }
 
-// T at NP points from one node list, the 32 lanes of a warp splitting the nodes; every
-// lane returns the same values.  Each node is read once for all NP points, so a pass over
-// four points costs little more than a pass over one.
+__device__ __forceinline__ unsigned udiv(unsigned x, unsigned m, int sh) {
+  return (unsigned)(((unsigned long long)x * m) >> sh);
+}
+
+// (hi, lo) += (bh, bl) without the final renormalisation: TwoSum of the heads, the error
+// and both tails summed into lo.  Chained in the lane butterfly, with one Fast2Sum at the end.
+__device__ __forceinline__ void df_add_lazy(float& hi, float& lo, float bh, float bl) {
+  const float s = hi + bh;
+  const float v = s - hi;
+  lo = ((hi - (s - v)) + (bh - v)) + (lo + bl);
+  hi = s;
+}
+
+// T at NP points of one grid column (the same i, j; the callers' passes - a point and the
+// layers under it, or a run of layers of a depth walk - always are) from one node list,
+// the 32 lanes of a warp splitting the nodes; every lane returns the same values.  Each node
+// is read once for all NP points, so a pass over four points costs little more than a pass
+// over one.
 //
-// FP32 form: the points' coordinates come as (hi, lo) float pairs from per-axis tables;
-// each lane sums its share with Kahan compensation; the lanes' results are reduced as
+// FP32 form: the points' coordinates come as (hi, lo) float pairs from per-axis tables
+// (`ax`, in shared memory when it fits); each lane takes groups of four staged nodes (the
+// lists are padded with zero-weight nodes to a multiple of four) as two packed pairs, forms
+// the x, y part of the exponent once per node and the z part per point, adds the two
+// pairs' terms and folds them into a packed Kahan sum.  The lanes' results are reduced as
 // double-float pairs, and the liquid test compares that pair with T_L - T_0 split into
 // three floats.  No FP64 arithmetic or conversion sits on the evaluation's path: T is
 // stored as the pair and turned into a double only where fields and solidification times
 // are computed.
 template <int PREC, int NP>
-__device__ __forceinline__ void warp_T_n(const DevProblem& P, const TrackState& S, const NodeBufView& nb, int nn,
-                                         const int (&pts)[NP], const Staged& st, EvalT (&out)[NP]) {
+__device__ __forceinline__ void warp_T_n(const DevProblem& P, const TrackState& S, const float2* ax,
+                                         const NodeBufView& nb, int nn, const int (&pts)[NP], const Staged& st,
+                                         EvalT (&out)[NP]) {
   const int lane = threadIdx.x & 31;
   const int n_sm = min(st.n_sm, nn);
-  unsigned pi[NP], pj[NP], pk[NP];
-#pragma unroll
-  for (int q = 0; q < NP; ++q) {
-    const unsigned pu = (unsigned)pts[q], col = pu / (unsigned)P.nz;
-    pk[q] = pu - col * (unsigned)P.nz;
-    pi[q] = col / (unsigned)P.ny;
-    pj[q] = col - pi[q] * (unsigned)P.ny;
-  }
   if constexpr (PREC == 0) {
     double x[NP], y[NP], z[NP], s[NP];
 #pragma unroll
     for (int q = 0; q < NP; ++q) {
-      x[q] = coord(P.gx, P.xmin, P.xmax, P.hx, (int)pi[q]);
-      y[q] = coord(P.gy, P.ymin, P.ymax, P.hy, (int)pj[q]);
-      z[q] = coord(P.gz, P.zmin, P.zmax, P.hz, (int)pk[q]);
+      const unsigned pu = (unsigned)pts[q], col = pu / (unsigned)P.nz;
+      const unsigned pk = pu - col * (unsigned)P.nz, pi = col / (unsigned)P.ny, pj = col - pi * (unsigned)P.ny;
+      x[q] = coord(P.gx, P.xmin, P.xmax, P.hx, (int)pi);
+      y[q] = coord(P.gy, P.ymin, P.ymax, P.hy, (int)pj);
+      z[q] = coord(P.gz, P.zmin, P.zmax, P.hz, (int)pk);
       s[q] = 0.0;
     }
     const double2* D = (const double2*)st.base;
@@ -166,67 +179,49 @@ __device__ __forceinline__ void warp_T_n(const DevProblem& P, const TrackState& 
       out[q].liquid = out[q].T >= P.TL;
     }
   } else {
-    // points as (v, v) pairs; per point one packed Kahan sum over node pairs (even nodes in
-    // the low half, odd in the high) and one scalar sum for the odd node and global tail
-    unsigned long long Xh[NP], Xl[NP], Yh[NP], Yl[NP], Zh[NP], Zl[NP], s2[NP], c2[NP];
-    float xh1[NP], xl1[NP], yh1[NP], yl1[NP], zh1[NP], zl1[NP], s1[NP], c1[NP];
+    const unsigned col = udiv((unsigned)pts[0], P.div_nz_m, P.div_nz_s);
+    const unsigned pi = udiv(col, P.div_ny_m, P.div_ny_s), pj = col - pi * (unsigned)P.ny;
+    const float2 X = ax[pi], Y = ax[P.nx + pj];
+    const unsigned long long Xh = pk2(X.x, X.x), Xl = pk2(X.y, X.y), Yh = pk2(Y.x, Y.x), Yl = pk2(Y.y, Y.y);
+    // per point its z as (v, v) pairs and one packed Kahan sum (s2, c2) over node pairs (the
+    // pairs' even nodes in the low half, odd in the high)
+    unsigned long long Zh[NP], Zl[NP], s2[NP], c2[NP];
+    float zh1[NP], zl1[NP];
 #pragma unroll
     for (int q = 0; q < NP; ++q) {
-      const float2 X = __ldg(S.axis + pi[q]), Y = __ldg(S.axis + P.nx + pj[q]),
-                   Z = __ldg(S.axis + P.nx + P.ny + pk[q]);
-      xh1[q] = X.x; xl1[q] = X.y; yh1[q] = Y.x; yl1[q] = Y.y; zh1[q] = Z.x; zl1[q] = Z.y;
-      Xh[q] = pk2(X.x, X.x); Xl[q] = pk2(X.y, X.y);
-      Yh[q] = pk2(Y.x, Y.x); Yl[q] = pk2(Y.y, Y.y);
+      const unsigned pk = min((unsigned)pts[q] - col * (unsigned)P.nz, (unsigned)P.nz - 1u);
+      const float2 Z = ax[P.nx + P.ny + pk];
+      zh1[q] = Z.x; zl1[q] = Z.y;
       Zh[q] = pk2(Z.x, Z.x); Zl[q] = pk2(Z.y, Z.y);
       s2[q] = c2[q] = 0ull;
-      s1[q] = c1[q] = 0.f;
     }
-    auto acc1 = [&](float xh, float yh, float zh, float xl, float yl, float zl, float kx, float ky, float kz,
-                    float w) {
+    const int cap4 = st.cap >> 2;
+    const ulonglong2* F = (const ulonglong2*)st.base;   // field f, group g of four nodes: F[f * cap4 + g]
+    const int ng = (n_sm + 3) >> 2;
+    for (int g = lane; g < ng; g += 32) {
+      const ulonglong2 xh = F[g], yh = F[cap4 + g], zh = F[2 * cap4 + g], xl = F[3 * cap4 + g],
+                       yl = F[4 * cap4 + g], zl = F[5 * cap4 + g], kx = F[6 * cap4 + g], ky = F[7 * cap4 + g],
+                       kz = F[8 * cap4 + g], w = F[9 * cap4 + g];
+      const unsigned long long dxa = add2(sub2(Xh, xh.x), sub2(Xl, xl.x)), dxb = add2(sub2(Xh, xh.y), sub2(Xl, xl.y));
+      const unsigned long long dya = add2(sub2(Yh, yh.x), sub2(Yl, yl.x)), dyb = add2(sub2(Yh, yh.y), sub2(Yl, yl.y));
+      const unsigned long long ea = fma2(mul2(dya, dya), ky.x, mul2(mul2(dxa, dxa), kx.x));
+      const unsigned long long eb = fma2(mul2(dyb, dyb), ky.y, mul2(mul2(dxb, dxb), kx.y));
 #pragma unroll
       for (int q = 0; q < NP; ++q) {
-        const float dx = (xh1[q] - xh) + (xl1[q] - xl);
-        const float dy = (yh1[q] - yh) + (yl1[q] - yl);
-        const float dz = (zh1[q] - zh) + (zl1[q] - zl);
-        const float e = fmaf(dz * dz, kz, fmaf(dy * dy, ky, dx * dx * kx));
-        const float v = ex2_approx(e) * w;
-        const float yy = v - c1[q];
-        const float tt = s1[q] + yy;
-        c1[q] = (tt - s1[q]) - yy;
-        s1[q] = tt;
-      }
-    };
-    const int cap2 = st.cap >> 1;
-    const unsigned long long* F = (const unsigned long long*)st.base;   // field f, node pair j: F[f * cap2 + j]
-    const int npair = n_sm >> 1;
-    for (int j = lane; j < npair; j += 32) {
-      const unsigned long long xh = F[j], yh = F[cap2 + j], zh = F[2 * cap2 + j], xl = F[3 * cap2 + j],
-                               yl = F[4 * cap2 + j], zl = F[5 * cap2 + j], kx = F[6 * cap2 + j],
-                               ky = F[7 * cap2 + j], kz = F[8 * cap2 + j], w = F[9 * cap2 + j];
-#pragma unroll
-      for (int q = 0; q < NP; ++q) {
-        const unsigned long long dx = add2(sub2(Xh[q], xh), sub2(Xl[q], xl));
-        const unsigned long long dy = add2(sub2(Yh[q], yh), sub2(Yl[q], yl));
-        const unsigned long long dz = add2(sub2(Zh[q], zh), sub2(Zl[q], zl));
-        const unsigned long long e = fma2(mul2(dz, dz), kz, fma2(mul2(dy, dy), ky, mul2(mul2(dx, dx), kx)));
-        float e0, e1;
-        upk2(e, e0, e1);
-        const unsigned long long v = mul2(pk2(ex2_approx(e0), ex2_approx(e1)), w);
-        const unsigned long long y = sub2(v, c2[q]);
+        const unsigned long long dza = add2(sub2(Zh[q], zh.x), sub2(Zl[q], zl.x));
+        const unsigned long long dzb = add2(sub2(Zh[q], zh.y), sub2(Zl[q], zl.y));
+        const unsigned long long fa = fma2(mul2(dza, dza), kz.x, ea), fb = fma2(mul2(dzb, dzb), kz.y, eb);
+        float a0, a1, b0, b1;
+        upk2(fa, a0, a1);
+        upk2(fb, b0, b1);
+        const unsigned long long va = mul2(pk2(ex2_approx(a0), ex2_approx(a1)), w.x);
+        const unsigned long long vb = mul2(pk2(ex2_approx(b0), ex2_approx(b1)), w.y);
+        const unsigned long long y = sub2(add2(va, vb), c2[q]);
         const unsigned long long t = add2(s2[q], y);
         c2[q] = sub2(sub2(t, s2[q]), y);
         s2[q] = t;
       }
     }
-    const float* F1 = (const float*)st.base;
-    if ((n_sm & 1) && lane == 0) {                 // the odd staged node
-      const int n = n_sm - 1, c = st.cap;
-      acc1(F1[n], F1[c + n], F1[2 * c + n], F1[3 * c + n], F1[4 * c + n], F1[5 * c + n], F1[6 * c + n],
-           F1[7 * c + n], F1[8 * c + n], F1[9 * c + n]);
-    }
-    for (int n = n_sm + lane; n < nn; n += 32)     // nodes past the staged copy
-      acc1(__ldg(nb.xh + n), __ldg(nb.yh + n), __ldg(nb.zh + n), __ldg(nb.xl + n), __ldg(nb.yl + n),
-           __ldg(nb.zl + n), __ldg(nb.kx + n), __ldg(nb.ky + n), __ldg(nb.kz + n), __ldg(nb.w + n));
     float hi[NP], lo[NP];
 #pragma unroll
     for (int q = 0; q < NP; ++q) {
@@ -235,19 +230,44 @@ __device__ __forceinline__ void warp_T_n(const DevProblem& P, const TrackState& 
       upk2(c2[q], cl, ch);
       hi[q] = sl;
       lo[q] = -cl;
-      df_add(hi[q], lo[q], sh, -ch);
-      df_add(hi[q], lo[q], s1[q], -c1[q]);
+      df_add_lazy(hi[q], lo[q], sh, -ch);
+    }
+    if (n_sm < nn) {                               // nodes past the staged copy, one per lane
+      float s1[NP], c1[NP];
+#pragma unroll
+      for (int q = 0; q < NP; ++q) s1[q] = c1[q] = 0.f;
+      for (int n = n_sm + lane; n < nn; n += 32) {
+        const float xh = __ldg(nb.xh + n), yh = __ldg(nb.yh + n), zh = __ldg(nb.zh + n), xl = __ldg(nb.xl + n),
+                    yl = __ldg(nb.yl + n), zl = __ldg(nb.zl + n), kx = __ldg(nb.kx + n), ky = __ldg(nb.ky + n),
+                    kz = __ldg(nb.kz + n), w = __ldg(nb.w + n);
+        const float dx = (X.x - xh) + (X.y - xl), dy = (Y.x - yh) + (Y.y - yl);
+        const float exy = fmaf(dy * dy, ky, dx * dx * kx);
+#pragma unroll
+        for (int q = 0; q < NP; ++q) {
+          const float dz = (zh1[q] - zh) + (zl1[q] - zl);
+          const float v = ex2_approx(fmaf(dz * dz, kz, exy)) * w;
+          const float yy = v - c1[q];
+          const float tt = s1[q] + yy;
+          c1[q] = (tt - s1[q]) - yy;
+          s1[q] = tt;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < NP; ++q) df_add_lazy(hi[q], lo[q], s1[q], -c1[q]);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
 #pragma unroll
       for (int q = 0; q < NP; ++q) {
         const float bh = __shfl_xor_sync(0xffffffffu, hi[q], o), bl = __shfl_xor_sync(0xffffffffu, lo[q], o);
-        df_add(hi[q], lo[q], bh, bl);
+        df_add_lazy(hi[q], lo[q], bh, bl);
       }
     }
 #pragma unroll
     for (int q = 0; q < NP; ++q) {
+      const float sh = hi[q];                      // Fast2Sum: |lo| is far below |hi|
+      hi[q] = sh + lo[q];
+      lo[q] = lo[q] - (hi[q] - sh);
       // sign of (hi + lo) - (T_L - T_0): the head difference is exact near the threshold
       const float d = ((hi[q] - P.tl_df[0]) + (lo[q] - P.tl_df[1])) - P.tl_df[2];
       out[q].liquid = d >= 0.f;
@@ -328,7 +348,7 @@ enum { IT_RETEST = 0, IT_VISIT = 2, IT_COLUMN = 3 };
 struct StepCtx {
   Staged st, stl;          // this step's and the previous step's node lists in shared memory
   BlockBuf* bb;            // this block's buffered records
-  mutable unsigned long long ev_n, ev_c;  // point evaluations and their SM clocks (profile)
+  mutable unsigned long long ev_n, ev_c, ev_nodes;  // evaluation passes, their SM clocks and nodes (profile)
   int depth;               // chain depth of the item being run (its children get depth + 1)
   int k;                   // step
   unsigned stamp;          // k + 1
@@ -340,6 +360,7 @@ struct StepCtx {
   int2* Lo;
   int* lo_n;
   QueueCounters* qc;
+  const float2* ax;        // grid axis table (hi, lo) (shared memory when it fits)
 };
 
 __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
@@ -375,9 +396,10 @@ __device__ __forceinline__ EvalT eval_T(const DevProblem& P, const TrackState& S
   const long long c0 = clock64();
   const int pts[1] = {(int)p};
   EvalT T[1];
-  warp_T_n<PREC, 1>(P, S, nb, nn, pts, st, T);
+  warp_T_n<PREC, 1>(P, S, X.ax, nb, nn, pts, st, T);
   X.ev_c += clock64() - c0;
   X.ev_n += 1;
+  X.ev_nodes += nn;
   return T[0];
 }
 
@@ -387,9 +409,10 @@ template <int PREC, int NP>
 __device__ __forceinline__ void eval_Tn(const DevProblem& P, const TrackState& S, const StepCtx& X,
                                         const int (&pts)[NP], EvalT (&T)[NP]) {
   const long long c0 = clock64();
-  warp_T_n<PREC, NP>(P, S, X.nb, X.nn, pts, X.st, T);
+  warp_T_n<PREC, NP>(P, S, X.ax, X.nb, X.nn, pts, X.st, T);
   X.ev_c += clock64() - c0;
   X.ev_n += 1;
+  X.ev_nodes += X.nn;
 }
 
 // Publishes one child item per lane that has one (warp-uniform call).  The children are
@@ -709,9 +732,10 @@ __device__ int depth_walk(const DevProblem& P, const TrackState& S, const StepCt
       // T at t - dt is needed only below D (the layer at D has it stored)
       if (d != D) {
         const long long c0 = clock64();
-        warp_T_n<PREC, NB>(P, S, X.nbl, X.nnl, pts, X.stl, tmpl);
+        warp_T_n<PREC, NB>(P, S, X.ax, X.nbl, X.nnl, pts, X.stl, tmpl);
         X.ev_c += clock64() - c0;
         X.ev_n += 1;
+        X.ev_nodes += X.nnl;
       }
 #pragma unroll
       for (int q = 0; q < NB; ++q) { Tu[q] = tmp[q]; Tl4[q] = tmpl[q]; }
@@ -825,6 +849,14 @@ constexpr int kTrackThreads = 128;   // four warps per block, one block per SM
 // trace seeds the new ones, and every claimed point, column and depth walk becomes a work
 // item that any warp may take; a packed (published << 32 | completed) counter tells the
 // warps when the step has no work left, and one grid barrier ends the step.
+// FP32 tracking keeps the grid's axis table (8 bytes per axis point) in shared memory
+// behind the staged lists when the axes have at most kAxisSmem points in all.
+constexpr int kAxisSmem = 2048;
+template <int PREC>
+__host__ __device__ __forceinline__ bool axis_in_smem(const DevProblem& P) {
+  return PREC != 0 && P.nx + P.ny + P.nz <= kAxisSmem;
+}
+
 template <int PREC, bool SURF>
 __global__ void __launch_bounds__(kTrackThreads, 1) k_track(DevProblem P, TrackState S, NodeWindow W, int k_begin,
                                                             int k_end, int high_water, int stage_cap) {
@@ -847,10 +879,17 @@ __global__ void __launch_bounds__(kTrackThreads, 1) k_track(DevProblem P, TrackS
     if (k_begin > 0) stage_issue<PREC>(slot_view(W, slot - 1), min(W.count[slot - 1], stage_cap), buf_of(k_begin - 1),
                                        stage_cap);
   }
+  // the axis table after the three lists, when it fits
+  const float2* ax = S.axis;
+  if (axis_in_smem<PREC>(P)) {
+    float2* sax = (float2*)(stage_mem + 3 * buf_bytes);
+    for (int i = threadIdx.x; i < P.nx + P.ny + P.nz; i += blockDim.x) sax[i] = __ldg(S.axis + i);
+    ax = sax;
+  }
   cp_async_wait_all();
   __syncthreads();
   unsigned long long t_work = 0, n_items = 0, c_items = 0, c_wait = 0, depth_sum = 0;
-  unsigned long long ev_n = 0, ev_c = 0, lvl_s[4] = {0, 0, 0, 0}, lvl_e[4] = {0, 0, 0, 0};
+  unsigned long long ev_n = 0, ev_c = 0, ev_nodes = 0, lvl_s[4] = {0, 0, 0, 0}, lvl_e[4] = {0, 0, 0, 0};
   // step k's live-list length and this warp's first re-test entry, read when step k - 1
   // ended (for the first step, from memory)
   int nL_next = k_begin < k_end ? ldcg_i(&C->liq_n[k_begin % 3]) : 0;
@@ -868,6 +907,7 @@ __global__ void __launch_bounds__(kTrackThreads, 1) k_track(DevProblem P, TrackS
     StepCtx X;
     X.ev_n = 0;
     X.ev_c = 0;
+    X.ev_nodes = 0;
     const int slot = k - W.base + 1;
     const double t_k = t_next;
     const int cnt_k = cnt_next, cntl_k = cntl_next, nseed_k = nseed_next;
@@ -905,6 +945,7 @@ __global__ void __launch_bounds__(kTrackThreads, 1) k_track(DevProblem P, TrackS
     X.L = S.liq[b0];
     X.Lo = S.liq[b1];
     X.lo_n = &C->liq_n[b1];
+    X.ax = ax;
     unsigned long long arrival = 0;         // this block enters the step (thread 0)
     bool arrival_pending = threadIdx.x == 0;
     if (arrival_pending) arrival = atomicAdd(&X.qc->state, kArrive);
@@ -1009,6 +1050,7 @@ __global__ void __launch_bounds__(kTrackThreads, 1) k_track(DevProblem P, TrackS
     t_work += globaltimer() - g0;
     ev_n += X.ev_n;
     ev_c += X.ev_c;
+    ev_nodes += X.ev_nodes;
     // The step is over: the next step's live-list length and this step's verdict are final
     // (the verdict stays until this block has entered the next step).  Every warp of the
     // block takes the same decisions; the block barrier also completes the next list's
@@ -1038,6 +1080,7 @@ __global__ void __launch_bounds__(kTrackThreads, 1) k_track(DevProblem P, TrackS
     atomicAdd(&C->prof[4], c_wait);
     atomicAdd(&C->prof[7], ev_n);
     atomicAdd(&C->prof[8], ev_c);
+    atomicAdd(&C->prof[9], ev_nodes);
   }
   if (tid == 0) {
     atomicAdd(&C->prof[0], t_work);
@@ -1360,7 +1403,8 @@ static cudaError_t launch_track_t(const DevProblem& P, const TrackState& S, cons
   // stage whole lists up to the slot capacity, within 200 KB of shared memory for the three buffers
   int cap = std::min(w.slot_cap, (200 * 1024) / (3 * staged_bytes_per_node<PREC>()));
   cap = std::max(8, cap & ~7);
-  const size_t smem = (size_t)3 * cap * staged_bytes_per_node<PREC>();
+  const size_t smem = (size_t)3 * cap * staged_bytes_per_node<PREC>() +
+                      (axis_in_smem<PREC>(P) ? (size_t)(P.nx + P.ny + P.nz) * sizeof(float2) : 0);
   cudaError_t e = cudaFuncSetAttribute(k_track<PREC, SURF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   // leave the rest of the SM's 256 KB to the L1 cache (the kernel's loads of node windows,

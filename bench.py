@@ -232,6 +232,7 @@ def run_solidification(args, th, torch, dev, path, deck, world):
             "chain_depth_per_timestep": st["loop_depth_sum"] / n,
             "evals_per_timestep": st["loop_evals"] / n,
             "us_per_eval": st["loop_eval_clocks"] / max(1, st["loop_evals"]) / clk_mhz,
+            "nodes_per_eval": st["loop_eval_nodes"] / max(1, st["loop_evals"]),
             "us_latest_item_start_by_chain_depth": [1e3 * st[f"loop_ms_start{l}"] / n for l in range(4)],
             "us_latest_item_end_by_chain_depth": [1e3 * st[f"loop_ms_end{l}"] / n for l in range(4)]}
     return {"value": value, "ms_per_step": 1e3 * total_s / args.steps, "e2e": e2e, "roofline": roof,
