@@ -36,6 +36,26 @@ __device__ __forceinline__ NodeBufView slot_view(const NodeWindow& w, int slot) 
   return v;
 }
 
+// One slot's node arrays as two base pointers: a window keeps each of its eight double
+// fields (x, y, z, ipx, ipy, ipz, dtau, amp) and ten float fields (kx, ky, kz, w, xh, xl, yh,
+// yl, zh, zl) in one array of `stride` entries, those arrays `stride` apart, slots one after
+// another (window_layout_ok checks this before a launch).  The tracking loop carries two of
+// these instead of two full views.
+struct SlotRef {
+  const double* d;
+  const float* f;
+  int stride;
+  __device__ __forceinline__ double dv(int field, int n) const { return __ldg(d + (size_t)field * stride + n); }
+  __device__ __forceinline__ float fv(int field, int n) const { return __ldg(f + (size_t)field * stride + n); }
+};
+enum { ND_X, ND_Y, ND_Z, ND_IPX, ND_IPY, ND_IPZ, ND_DTAU, ND_AMP };
+enum { NF_KX, NF_KY, NF_KZ, NF_W, NF_XH, NF_XL, NF_YH, NF_YL, NF_ZH, NF_ZL };
+
+__device__ __forceinline__ SlotRef slot_ref(const NodeWindow& w, int slot) {
+  const size_t off = (size_t)slot * w.slot_cap;
+  return SlotRef{w.nb.x + off, w.nb.kx + off, w.nb.cap};
+}
+
 // ------------------------------------------------------------------ warp evaluation
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
@@ -144,7 +164,7 @@ __device__ __forceinline__ void df_add_lazy(float& hi, float& lo, float bh, floa
 // are computed.
 template <int PREC, int NP>
 __device__ __forceinline__ void warp_T_n(const DevProblem& P, const TrackState& S, const float2* ax,
-                                         const NodeBufView& nb, int nn, const int (&pts)[NP], const Staged& st,
+                                         const SlotRef& nb, int nn, const int (&pts)[NP], const Staged& st,
                                          EvalT (&out)[NP]) {
   const int lane = threadIdx.x & 31;
   const int n_sm = min(st.n_sm, nn);
@@ -171,8 +191,8 @@ __device__ __forceinline__ void warp_T_n(const DevProblem& P, const TrackState& 
     int n = lane;
     for (; n < n_sm; n += 32) acc(D[n], D[st.cap + n], D[2 * st.cap + n], D[3 * st.cap + n]);
     for (; n < nn; n += 32)
-      acc(make_double2(__ldg(nb.x + n), __ldg(nb.y + n)), make_double2(__ldg(nb.z + n), __ldg(nb.ipx + n)),
-          make_double2(__ldg(nb.ipy + n), __ldg(nb.ipz + n)), make_double2(__ldg(nb.dtau + n), __ldg(nb.amp + n)));
+      acc(make_double2(nb.dv(ND_X, n), nb.dv(ND_Y, n)), make_double2(nb.dv(ND_Z, n), nb.dv(ND_IPX, n)),
+          make_double2(nb.dv(ND_IPY, n), nb.dv(ND_IPZ, n)), make_double2(nb.dv(ND_DTAU, n), nb.dv(ND_AMP, n)));
 #pragma unroll
     for (int q = 0; q < NP; ++q) {
       out[q].T = P.T0 + warp_sum_d(s[q]);
@@ -237,9 +257,9 @@ __device__ __forceinline__ void warp_T_n(const DevProblem& P, const TrackState& 
 #pragma unroll
       for (int q = 0; q < NP; ++q) s1[q] = c1[q] = 0.f;
       for (int n = n_sm + lane; n < nn; n += 32) {
-        const float xh = __ldg(nb.xh + n), yh = __ldg(nb.yh + n), zh = __ldg(nb.zh + n), xl = __ldg(nb.xl + n),
-                    yl = __ldg(nb.yl + n), zl = __ldg(nb.zl + n), kx = __ldg(nb.kx + n), ky = __ldg(nb.ky + n),
-                    kz = __ldg(nb.kz + n), w = __ldg(nb.w + n);
+        const float xh = nb.fv(NF_XH, n), yh = nb.fv(NF_YH, n), zh = nb.fv(NF_ZH, n), xl = nb.fv(NF_XL, n),
+                    yl = nb.fv(NF_YL, n), zl = nb.fv(NF_ZL, n), kx = nb.fv(NF_KX, n), ky = nb.fv(NF_KY, n),
+                    kz = nb.fv(NF_KZ, n), w = nb.fv(NF_W, n);
         const float dx = (X.x - xh) + (X.y - xl), dy = (Y.x - yh) + (Y.y - yl);
         const float exy = fmaf(dy * dy, ky, dx * dx * kx);
 #pragma unroll
@@ -353,7 +373,7 @@ struct StepCtx {
   int k;                   // step
   unsigned stamp;          // k + 1
   double t;
-  NodeBufView nb, nbl;
+  SlotRef nb, nbl;
   int nn, nnl;
   int nL, n_init;
   const int2* L;
@@ -389,10 +409,18 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
 __device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
 
 template <int PREC>
 __device__ __forceinline__ EvalT eval_T(const DevProblem& P, const TrackState& S, const StepCtx& X,
-                                        const NodeBufView& nb, int nn, int64_t p, const Staged& st) {
+                                        const SlotRef& nb, int nn, int64_t p, const Staged& st) {
   const long long c0 = clock64();
   const int pts[1] = {(int)p};
   EvalT T[1];
@@ -442,23 +470,26 @@ __device__ __forceinline__ void emit(const TrackState& S, const StepCtx& X, bool
 }
 
 // Claims the unvisited neighbours of p (3x3 in the same layer for Surface, 3x3x{k-1, k}
-// for Volume; src/Melt.cpp:202-257) and queues them for evaluation.
+// for Volume; src/Melt.cpp:202-257) and queues them for evaluation.  A Surface neighbour's
+// item carries its column's depth, read beside the claim: only that item writes the
+// column's depth this step, so the child starts its pass without a load of its own.
 template <bool SURF>
 __device__ __forceinline__ void expand(const DevProblem& P, const TrackState& S, const StepCtx& X, int p, int& nchild) {
   const int lane = threadIdx.x & 31;
   const int nyz = P.ny * P.nz;
   const int pi = p / nyz, pj = (p / P.nz) % P.ny, pk = p % P.nz;
   bool got = false;
-  int q = 0;
+  int q = 0, dq = 0;
   if (lane < (SURF ? 9 : 18)) {
     const int di = (lane % 9) / 3 - 1, dj = lane % 3 - 1, dk = SURF ? 0 : (lane / 9) - 1;
     const int ni = pi + di, nj = pj + dj, nk = pk + dk;
     if (!(ni < 0 || ni > P.nx - 1 || nj < 0 || nj > P.ny - 1 || nk < 0)) {
       q = (int)pid(P, ni, nj, nk);
+      if (SURF) dq = ldcg_i(S.depths + (ni * P.ny + nj));
       got = claim(S, q, X.stamp);
     }
   }
-  emit(S, X, got, IT_VISIT, q, 0, nchild);
+  emit(S, X, got, IT_VISIT, q, dq, nchild);
 }
 
 // A liquid point joins the next step's list with its column's depth (the next re-test
@@ -477,8 +508,10 @@ __device__ __forceinline__ bool step_over(unsigned long long v, int n_init, unsi
 // queue) and k + 2 (the liquid list it will fill), records the step, then publishes the
 // step's end.  Every block has entered step k and no item of it is left, so nothing reads
 // those counters any more and nothing of step k + 1 has started.
-// It also takes the step's verdict for every warp: the finish test (src/Util.cpp:239-243)
-// and the record queue's high-water mark, from the step's final counts.
+// It also takes the step's verdict for every warp - the finish test (src/Util.cpp:239-243)
+// and the record queue's high-water mark, from the step's final counts - and publishes it
+// with the next step's liquid-list length and the step's stamp in one word, so a waiting
+// warp learns all three from the load that ends its wait.
 __device__ void finish_step(const DevProblem& P, const TrackState& S, const StepCtx& X, int k, unsigned long long v,
                             int high_water) {
   TrackCounters* C = S.C;
@@ -489,12 +522,12 @@ __device__ void finish_step(const DevProblem& P, const TrackState& S, const Step
   C->step = k + 1;
   const int items = X.n_init + (int)((v >> 24) & kField);
   if (items > C->max_items) C->max_items = items;
-  unsigned flags = 0;
-  if (X.t > P.end_time && __ldcg(X.lo_n) == 0) { flags |= 1u; C->done = 1; }
-  else if (__ldcg(S.rec_n) > high_water) { flags |= 2u; C->stop = 1; }
-  C->verdict = (X.stamp << 2) | flags;
+  const int n_next = __ldcg(X.lo_n), n_rec = __ldcg(S.rec_n);
+  unsigned long long flags = 0;
+  if (X.t > P.end_time && n_next == 0) { flags |= 1u; C->done = 1; }
+  else if (n_rec > high_water) { flags |= 2u; C->stop = 1; }
   __threadfence();
-  st_release_u32(&C->finished, X.stamp);
+  st_release_u64(&C->fin, ((unsigned long long)n_next << 34) | (flags << 32) | X.stamp);
 }
 
 __device__ __forceinline__ void push_rec(const TrackState& S, const StepCtx& X, int p, double T, double Tl) {
@@ -800,7 +833,7 @@ __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx&
   int D = 0;
   if (SURF && PREC != 0) {                 // the point and the layers its depth walk starts with
     const int col = p / P.nz, top = col * P.nz + (P.nz - 1);
-    D = type == IT_RETEST ? Dk : ldcg_i(S.depths + col);
+    D = type == IT_RETEST ? Dk : (seed ? ldcg_i(S.depths + col) : aux);
     const int down = D + 1 <= P.nz - 1 ? top - (D + 1) : p;
     if (D >= 1) {
       const int pts[3] = {p, down, top - D};
@@ -812,7 +845,7 @@ __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx&
       T3[0] = T2[0]; T3[1] = T2[1]; T3[2] = T2[1];
     }
   } else {
-    if (SURF) D = type == IT_RETEST ? Dk : ldcg_i(S.depths + p / P.nz);
+    if (SURF) D = type == IT_RETEST ? Dk : (seed ? ldcg_i(S.depths + p / P.nz) : aux);
     T3[0] = eval_T<PREC>(P, S, X, X.nb, X.nn, p, X.st);
   }
   if (seed && !__shfl_sync(0xffffffffu, got, 0)) return 0;
@@ -849,6 +882,17 @@ constexpr int kTrackThreads = 128;   // four warps per block, one block per SM
 // trace seeds the new ones, and every claimed point, column and depth walk becomes a work
 // item that any warp may take; a packed (published << 32 | completed) counter tells the
 // warps when the step has no work left, and one grid barrier ends the step.
+// The first 48 bytes of a step's QueueCounters (head, depth, lvl_start, lvl_end) into
+// shared memory, bypassing L1 (the counters are updated by atomics in L2).
+__device__ __forceinline__ void copy_step_prof(const QueueCounters* q, unsigned* dst) {
+  for (int c = 0; c < 3; ++c) cp_async16(dst + 4 * c, (const unsigned*)q + 4 * c);
+  cp_async_commit();
+}
+__device__ __forceinline__ void add_step_prof(const unsigned* q, unsigned long long* acc) {
+  acc[0] += q[1];                                   // depth
+  for (int l = 0; l < 4; ++l) { acc[1 + l] += q[2 + l]; acc[5 + l] += q[6 + l]; }
+}
+
 // FP32 tracking keeps the grid's axis table (8 bytes per axis point) in shared memory
 // behind the staged lists when the axes have at most kAxisSmem points in all.
 constexpr int kAxisSmem = 2048;
@@ -888,8 +932,15 @@ __global__ void __launch_bounds__(kTrackThreads, 1) k_track(DevProblem P, TrackS
   }
   cp_async_wait_all();
   __syncthreads();
-  unsigned long long t_work = 0, n_items = 0, c_items = 0, c_wait = 0, depth_sum = 0;
-  unsigned long long ev_n = 0, ev_c = 0, ev_nodes = 0, lvl_s[4] = {0, 0, 0, 0}, lvl_e[4] = {0, 0, 0, 0};
+  unsigned long long t_work = 0, n_items = 0, c_items = 0, c_wait = 0;
+  unsigned long long ev_n = 0, ev_c = 0, ev_nodes = 0;
+  // block 0's per-step profile (chain depth, latest item start / end per depth): each
+  // step's counters are copied asynchronously at its end and folded in a step later
+  __shared__ __align__(16) unsigned s_qprof[2][12];
+  __shared__ unsigned long long s_acc[9];
+  bool prof_pend = false;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < 9; ++i) s_acc[i] = 0ull;
   // step k's live-list length and this warp's first re-test entry, read when step k - 1
   // ended (for the first step, from memory)
   int nL_next = k_begin < k_end ? ldcg_i(&C->liq_n[k_begin % 3]) : 0;
@@ -938,8 +989,8 @@ __global__ void __launch_bounds__(kTrackThreads, 1) k_track(DevProblem P, TrackS
     X.stl.cap = stage_cap;
     X.stl.n_sm = k == 0 ? 0 : min(cntl_k, stage_cap);
     X.k = k;
-    X.nb = slot_view(W, slot);
-    X.nbl = slot_view(W, slot - 1);
+    X.nb = slot_ref(W, slot);
+    X.nbl = slot_ref(W, slot - 1);
     X.nn = min(cnt_k, W.slot_cap);
     X.nnl = (k == 0) ? 0 : min(cntl_k, W.slot_cap);
     X.L = S.liq[b0];
@@ -958,6 +1009,7 @@ __global__ void __launch_bounds__(kTrackThreads, 1) k_track(DevProblem P, TrackS
     // waiting warps see.  No grid barrier separates steps.
     int next_init = tid >> 5;
     long long idle = 0;
+    unsigned long long fin_seen = 0xffffffffull;   // the step-end word this warp saw
     while (true) {
       const long long c0 = clock64();
       int type, p = 0, aux = 0, Dk = 0;
@@ -991,13 +1043,17 @@ __global__ void __launch_bounds__(kTrackThreads, 1) k_track(DevProblem P, TrackS
         ticket = __shfl_sync(0xffffffffu, ticket, 0);
         const unsigned j = ticket;
         bool ready = false, finished = false;
+        unsigned long long fin = 0;
         unsigned backoff = 8;
         ulonglong2 it = make_ulonglong2(0ull, 0ull);
         while (true) {
           if (lane == 0) {
             if (j < (unsigned)S.queue_cap) it = ld_relaxed_v2(S.queue + j);
             ready = (unsigned)(it.x >> 32) == X.stamp && (unsigned)(it.y >> 32) == X.stamp;
-            if (!ready) finished = ld_acquire_u32(&C->finished) >= X.stamp;
+            if (!ready) {
+              fin = ld_acquire_u64(&C->fin);
+              finished = (unsigned)fin >= X.stamp;
+            }
           }
           ready = __shfl_sync(0xffffffffu, ready, 0);
           finished = __shfl_sync(0xffffffffu, finished, 0);
@@ -1012,14 +1068,20 @@ __global__ void __launch_bounds__(kTrackThreads, 1) k_track(DevProblem P, TrackS
                 g[4] = (int)*(volatile unsigned*)&X.qc->head; g[5] = (int)(st >> 48);
                 g[6] = (int)((st >> 24) & kField); g[7] = (int)(st & kField);
               }
-              st_release_u32(&C->finished, 0xffffffffu);     // let every warp leave
+              st_release_u64(&C->fin, 0xffffffffull);       // let every warp leave
             }
+            fin = 0xffffffffull;
             finished = true;
             break;
           }
           __nanosleep(backoff);
         }
-        if (!ready) { c_wait += clock64() - c0; break; }
+        if (!ready) {
+          fin_seen = ((unsigned long long)__shfl_sync(0xffffffffu, (unsigned)(fin >> 32), 0) << 32) |
+                     __shfl_sync(0xffffffffu, (unsigned)fin, 0);
+          c_wait += clock64() - c0;
+          break;
+        }
         const unsigned w0 = __shfl_sync(0xffffffffu, (unsigned)it.x, 0);
         const unsigned w1 = __shfl_sync(0xffffffffu, (unsigned)it.y, 0);
         p = (int)w0;
@@ -1051,27 +1113,27 @@ __global__ void __launch_bounds__(kTrackThreads, 1) k_track(DevProblem P, TrackS
     ev_n += X.ev_n;
     ev_c += X.ev_c;
     ev_nodes += X.ev_nodes;
-    // The step is over: the next step's live-list length and this step's verdict are final
-    // (the verdict stays until this block has entered the next step).  Every warp of the
-    // block takes the same decisions; the block barrier also completes the next list's
-    // copies.
-    const unsigned verdict = ld_acquire_u32(&C->verdict);
-    nL_next = ldcg_i(X.lo_n);
-    if ((tid >> 5) < S.list_cap) first_next = __ldcg(X.Lo + (tid >> 5));
+    // The step is over.  The word that ended this warp's wait carries the next step's
+    // live-list length and the run's verdict, so every warp of the block takes the same
+    // decisions without another load; the block barrier also completes the next list's
+    // copies (and block 0's copy of the last step's profile counters).
+    const bool aborted = (unsigned)fin_seen == 0xffffffffu;
+    const unsigned verdict = (unsigned)(fin_seen >> 32) & 3u;
+    nL_next = (int)(fin_seen >> 34);
+    if (!aborted && (tid >> 5) < S.list_cap) first_next = __ldcg(X.Lo + (tid >> 5));
     cp_async_wait_all();
     if (threadIdx.x == 0) s_flush[k & 1] = bbuf.nrec >= kBlkRec / 2;
-    if (__syncthreads_or(ld_acquire_u32(&C->finished) == 0xffffffffu)) break;
-    if (tid == 0) {
-      depth_sum += __ldcg(&X.qc->depth);
-      for (int l = 0; l < 4; ++l) {
-        lvl_s[l] += __ldcg(&X.qc->lvl_start[l]);
-        lvl_e[l] += __ldcg(&X.qc->lvl_end[l]);
-      }
+    if (__syncthreads_or(aborted)) break;
+    if (tid == 0) {                           // profile: fold the previous step's copy, copy this one's
+      if (prof_pend) add_step_prof(s_qprof[(k - 1) & 1], s_acc);
+      copy_step_prof(X.qc, s_qprof[k & 1]);
+      prof_pend = true;
     }
-    if (verdict & 3u) { ++k; break; }
+    if (verdict) { ++k; break; }
     if (s_flush[k & 1]) flush_block(S, &bbuf, S.rec_n);
   }
   cp_async_wait_all();
+  if (tid == 0 && prof_pend) add_step_prof(s_qprof[(k - 1) & 1], s_acc);
   flush_block(S, &bbuf, S.rec_n);
   if (lane == 0 && pairs) atomicAdd(S.pairs, pairs);
   if (lane == 0) {
@@ -1084,9 +1146,9 @@ __global__ void __launch_bounds__(kTrackThreads, 1) k_track(DevProblem P, TrackS
   }
   if (tid == 0) {
     atomicAdd(&C->prof[0], t_work);
-    atomicAdd(&C->prof[5], depth_sum);
+    atomicAdd(&C->prof[5], s_acc[0]);
     atomicAdd(&C->prof[6], (unsigned long long)(k - k_begin));
-    for (int l = 0; l < 4; ++l) { atomicAdd(&C->prof[10 + l], lvl_s[l]); atomicAdd(&C->prof[14 + l], lvl_e[l]); }
+    for (int l = 0; l < 4; ++l) { atomicAdd(&C->prof[10 + l], s_acc[1 + l]); atomicAdd(&C->prof[14 + l], s_acc[5 + l]); }
   }
 }
 
@@ -1394,9 +1456,20 @@ void th_launch_nodes_window(const DevProblem& P, const NodeWindow& w, int first_
   k_nodes_window<<<nslots, kGenThreads, 0, s>>>(P, w, first_slot, nslots, is_sol ? 1 : 0, d_err);
 }
 
+// The layout SlotRef reads: every field one array of nb.cap entries, the fields nb.cap apart
+// in the order of SlotRef's field enums.
+static bool window_layout_ok(const NodeBufView& nb) {
+  const double* d[8] = {nb.x, nb.y, nb.z, nb.ipx, nb.ipy, nb.ipz, nb.dtau, nb.amp};
+  const float* f[10] = {nb.kx, nb.ky, nb.kz, nb.w, nb.xh, nb.xl, nb.yh, nb.yl, nb.zh, nb.zl};
+  for (int i = 0; i < 8; ++i) if (d[i] != nb.x + (size_t)i * nb.cap) return false;
+  for (int i = 0; i < 10; ++i) if (f[i] != nb.kx + (size_t)i * nb.cap) return false;
+  return true;
+}
+
 template <int PREC, bool SURF>
 static cudaError_t launch_track_t(const DevProblem& P, const TrackState& S, const NodeWindow& w, int k_begin, int k_end,
                                   int hw, cudaStream_t s) {
+  if (!window_layout_ok(w.nb)) return cudaErrorInvalidValue;
   int dev = 0, sms = 0, occ = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

@@ -49,8 +49,9 @@ struct alignas(128) TrackCounters {
   unsigned long long prof[18];
   alignas(128) int liq_n[3];     // liquid list lengths
   alignas(128) int rec_n[2];     // solidification records queued in each of the two record buffers
-  alignas(128) unsigned finished;// k + 1 once step k is over (0xffffffff: aborted by a bounded wait)
-  unsigned verdict;              // (k + 1) << 2 | 1 finished run | 2 record high-water mark
+  // once step k is over: (next step's liquid-list length << 34) | (flags << 32) | (k + 1), flags
+  // 1 finished run, 2 record high-water mark; low word 0xffffffff: aborted by a bounded wait
+  alignas(128) unsigned long long fin;
   QueueCounters q[3];
 };
 
