@@ -82,6 +82,7 @@ __device__ __forceinline__ void point_xyz(const DevProblem& P, int64_t p, double
 // scan compacts the kept ones in order.  Image copies for the boundary planes follow
 // (src/Calc.cpp:584-605).  blockDim.x must be kGenThreads.
 constexpr int kGenThreads = 256;
+constexpr int kListPad = 128;         // node lists are padded with zero-weight nodes to a multiple of this
 constexpr int kChunkIntervals = 256;
 constexpr int kSegCache = 320;        // path segments staged in shared memory per beam
 
@@ -184,10 +185,11 @@ __device__ __forceinline__ void gen_list_block(const DevProblem& P, double t, bo
     }
     n = n0 * P.n_images;
   }
-  // zero-weight nodes up to a multiple of four (they add exactly nothing), so that FP32
-  // passes read whole groups of four nodes
+  // zero-weight nodes up to a multiple of kListPad (they add exactly nothing), so that the
+  // FP32 tracking passes give every lane of a warp the same number of four-node groups
   if (n <= nb.cap)
-    for (int s = n + tid; s < ((n + 3) & ~3) && s < nb.cap; s += kGenThreads) store_node(nb, s, NodeVal{});
+    for (int s = n + tid; s < ((n + kListPad - 1) & ~(kListPad - 1)) && s < nb.cap; s += kGenThreads)
+      store_node(nb, s, NodeVal{});
   __syncthreads();
   if (tid == 0) {
     int e = sh.err;

@@ -289,7 +289,7 @@ th_status finish_window(th_ctx* ctx, RunState* r, int b) {
     if (st != TH_OK) return st;
     int mx = 0, ms_ = 0;
     for (int i = (w.base == 0 ? 1 : 0); i <= w.n; ++i) { mx = std::max(mx, cnt[i]); ms_ = std::max(ms_, ns[i]); }
-    if (err & 1) r->slot_cap = std::max(r->slot_cap, ((mx + 256) / 32 + 1) * 32);
+    if (err & 1) r->slot_cap = std::max(r->slot_cap, ((mx + 256) / 128 + 1) * 128);   // whole padded lists
     if (err & ERR_SEED_CAPACITY) r->seed_cap = std::max(r->seed_cap, ((ms_ + 64) / 32 + 1) * 32);
     // the other window may still be in use by the tracking stream or the aux stream
     cudaStreamSynchronize(r->aux);

@@ -88,8 +88,9 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 // Issues the block's asynchronous copies of the first m nodes of nb into buf.  FP32 copies
-// whole 16-byte groups of four nodes (a slot's arrays start 128-byte aligned and hold a
-// multiple of 32 nodes, so the group that straddles m stays inside the slot).
+// the list with its zero-weight padding to a multiple of kListPad nodes, in 16-byte groups
+// of four (a slot's arrays start 128-byte aligned and hold a multiple of kListPad nodes, and
+// cap is a multiple of kListPad, so the padding stays inside both).
 template <int PREC>
 __device__ __forceinline__ void stage_issue(const NodeBufView& nb, int m, unsigned char* buf, int cap) {
   if (PREC == 0) {
@@ -101,7 +102,7 @@ __device__ __forceinline__ void stage_issue(const NodeBufView& nb, int m, unsign
     }
   } else {
     const float* src[10] = {nb.xh, nb.yh, nb.zh, nb.xl, nb.yl, nb.zl, nb.kx, nb.ky, nb.kz, nb.w};
-    const int groups = (m + 3) >> 2;
+    const int groups = min((m + kListPad - 1) & ~(kListPad - 1), cap) >> 2;   // with the list's padding
 #pragma unroll
     for (int f = 0; f < 10; ++f) {
       float* dst = (float*)(buf + (size_t)f * cap * 4);
@@ -155,7 +156,7 @@ __device__ __forceinline__ void df_add_lazy(float& hi, float& lo, float bh, floa
 //
 // FP32 form: the points' coordinates come as (hi, lo) float pairs from per-axis tables
 // (`ax`, in shared memory when it fits); each lane takes groups of four staged nodes (the
-// lists are padded with zero-weight nodes to a multiple of four) as two packed pairs, forms
+// lists are padded with zero-weight nodes to a multiple of 128) as two packed pairs, forms
 // the x, y part of the exponent once per node and the z part per point, adds the two
 // pairs' terms and folds them into a packed Kahan sum.  The lanes' results are reduced as
 // double-float pairs, and the liquid test compares that pair with T_L - T_0 split into
@@ -217,7 +218,10 @@ __device__ __forceinline__ void warp_T_n(const DevProblem& P, const TrackState& 
     }
     const int cap4 = st.cap >> 2;
     const ulonglong2* F = (const ulonglong2*)st.base;   // field f, group g of four nodes: F[f * cap4 + g]
-    const int ng = (n_sm + 3) >> 2;
+    // whole padded list: a multiple of 32 groups, the same number for every lane (a warp
+    // whose lanes left the loop at different rounds would run the last round as a separate,
+    // serialised path)
+    const int ng = ((n_sm + kListPad - 1) & ~(kListPad - 1)) >> 2;
     for (int g = lane; g < ng; g += 32) {
       const ulonglong2 xh = F[g], yh = F[cap4 + g], zh = F[2 * cap4 + g], xl = F[3 * cap4 + g],
                        yl = F[4 * cap4 + g], zl = F[5 * cap4 + g], kx = F[6 * cap4 + g], ky = F[7 * cap4 + g],
@@ -1475,7 +1479,7 @@ static cudaError_t launch_track_t(const DevProblem& P, const TrackState& S, cons
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   // stage whole lists up to the slot capacity, within 200 KB of shared memory for the three buffers
   int cap = std::min(w.slot_cap, (200 * 1024) / (3 * staged_bytes_per_node<PREC>()));
-  cap = std::max(8, cap & ~7);
+  cap = std::max(kListPad, cap & ~(kListPad - 1));
   const size_t smem = (size_t)3 * cap * staged_bytes_per_node<PREC>() +
                       (axis_in_smem<PREC>(P) ? (size_t)(P.nx + P.ny + P.nz) * sizeof(float2) : 0);
   cudaError_t e = cudaFuncSetAttribute(k_track<PREC, SURF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
