@@ -1484,9 +1484,15 @@ static cudaError_t launch_track_t(const DevProblem& P, const TrackState& S, cons
                       (axis_in_smem<PREC>(P) ? (size_t)(P.nx + P.ny + P.nz) * sizeof(float2) : 0);
   cudaError_t e = cudaFuncSetAttribute(k_track<PREC, SURF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  // leave the rest of the SM's 256 KB to the L1 cache (the kernel's loads of node windows,
-  // axis tables and local arrays hit there)
-  const int carve = std::min(100, (int)((smem + 16 * 1024) * 100 / (228 * 1024)) + 1);
+  // Shared memory for this block and one k_nodes_window block beside it (the next window's
+  // lists are built on the other stream while this one is tracked; without the room that
+  // launch waits for the tracking launch to end), the rest of the SM's 256 KB to the L1
+  // cache.  A carveout picks the smallest configuration at or above the request.
+  cudaFuncAttributes ta{}, na{};
+  if ((e = cudaFuncGetAttributes(&ta, k_track<PREC, SURF>)) != cudaSuccess) return e;
+  if ((e = cudaFuncGetAttributes(&na, k_nodes_window)) != cudaSuccess) return e;
+  const size_t need = smem + ta.sharedSizeBytes + na.sharedSizeBytes + 2 * 1024;   // + 1 KB reserved per block
+  const int carve = std::min(100, (int)((need * 100 + 228 * 1024 - 1) / (228 * 1024)));
   e = cudaFuncSetAttribute(k_track<PREC, SURF>, cudaFuncAttributePreferredSharedMemoryCarveout, carve);
   if (e != cudaSuccess) return e;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_track<PREC, SURF>, kTrackThreads, smem);
