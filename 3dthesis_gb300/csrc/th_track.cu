@@ -112,17 +112,6 @@ __device__ __forceinline__ void stage_issue(const NodeBufView& nb, int m, unsign
   cp_async_commit();
 }
 
-// (hi, lo) += (bh, bl) in double-float: TwoSum of the heads, then the tails, renormalised
-// with Fast2Sum (Knuth; Dekker).  The result depends only on the two operands as a set
-// (TwoSum's error term is exact either way), so both lanes of a butterfly get the same bits.
-__device__ __forceinline__ void df_add(float& hi, float& lo, float bh, float bl) {
-  const float s = hi + bh;
-  const float v = s - hi;
-  float e = (hi - (s - v)) + (bh - v);
-  e += lo + bl;
-  hi = s + e;
-  lo = e - (hi - s);
-}
 
 // One evaluation's result: T as stored (a double in FP64 runs; in FP32 runs the sum T - T0
 // as a double-float pair (hi, lo) in the double's bits, decoded by t_decode), and T >= T_L.
@@ -139,8 +128,10 @@ __device__ __forceinline__ unsigned udiv(unsigned x, unsigned m, int sh) {
   return (unsigned)(((unsigned long long)x * m) >> sh);
 }
 
-// (hi, lo) += (bh, bl) without the final renormalisation: TwoSum of the heads, the error
-// and both tails summed into lo.  Chained in the lane butterfly, with one Fast2Sum at the end.
+// (hi, lo) += (bh, bl) in double-float without renormalising: TwoSum of the heads (Knuth),
+// the error and both tails summed into lo.  Chained in the lane butterfly, with one
+// Fast2Sum (Dekker) at the end.  The result depends only on the two operands as a set
+// (TwoSum's error term is exact either way), so both lanes of a butterfly get the same bits.
 __device__ __forceinline__ void df_add_lazy(float& hi, float& lo, float bh, float bl) {
   const float s = hi + bh;
   const float v = s - hi;
@@ -405,14 +396,6 @@ __device__ __forceinline__ ulonglong2 ld_relaxed_v2(const ulonglong2* p) {
   asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
-  unsigned v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
 __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
   unsigned long long v;
   asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
@@ -477,23 +460,35 @@ __device__ __forceinline__ void emit(const TrackState& S, const StepCtx& X, bool
 // for Volume; src/Melt.cpp:202-257) and queues them for evaluation.  A Surface neighbour's
 // item carries its column's depth, read beside the claim: only that item writes the
 // column's depth this step, so the child starts its pass without a load of its own.
+// The claims in flight: per lane the neighbour, its column's depth and the stamp the claim
+// replaced (the claim took the point if that is below this step's stamp).
+struct Claims { int q, dq; unsigned old; };
+
 template <bool SURF>
-__device__ __forceinline__ void expand(const DevProblem& P, const TrackState& S, const StepCtx& X, int p, int& nchild) {
+__device__ __forceinline__ Claims claim_neighbours(const DevProblem& P, const TrackState& S, const StepCtx& X, int p) {
   const int lane = threadIdx.x & 31;
   const int nyz = P.ny * P.nz;
   const int pi = p / nyz, pj = (p / P.nz) % P.ny, pk = p % P.nz;
-  bool got = false;
-  int q = 0, dq = 0;
+  Claims c{0, 0, 0xffffffffu};
   if (lane < (SURF ? 9 : 18)) {
     const int di = (lane % 9) / 3 - 1, dj = lane % 3 - 1, dk = SURF ? 0 : (lane / 9) - 1;
     const int ni = pi + di, nj = pj + dj, nk = pk + dk;
     if (!(ni < 0 || ni > P.nx - 1 || nj < 0 || nj > P.ny - 1 || nk < 0)) {
-      q = (int)pid(P, ni, nj, nk);
-      if (SURF) dq = ldcg_i(S.depths + (ni * P.ny + nj));
-      got = claim(S, q, X.stamp);
+      c.q = (int)pid(P, ni, nj, nk);
+      if (SURF) c.dq = ldcg_i(S.depths + (ni * P.ny + nj));
+      c.old = atomicMax(S.stamp + c.q, X.stamp);
     }
   }
-  emit(S, X, got, IT_VISIT, q, dq, nchild);
+  return c;
+}
+
+__device__ __forceinline__ void emit_claimed(const TrackState& S, const StepCtx& X, const Claims& c, int& nchild) {
+  emit(S, X, c.old < X.stamp, IT_VISIT, c.q, c.dq, nchild);
+}
+
+template <bool SURF>
+__device__ __forceinline__ void expand(const DevProblem& P, const TrackState& S, const StepCtx& X, int p, int& nchild) {
+  emit_claimed(S, X, claim_neighbours<SURF>(P, S, X, p), nchild);
 }
 
 // A liquid point joins the next step's list with its column's depth (the next re-test
@@ -830,9 +825,11 @@ __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx&
     if (lane == 0) push_rec(S, X, p, T.T, Tl);
     return 0;
   }
-  // Surface re-tests expand whatever their temperature (src/Run.cpp:655): claim first, so
-  // the neighbours' items start while this point is evaluated.
-  if (SURF && type == IT_RETEST) expand<SURF>(P, S, X, p, nchild);
+  // Surface re-tests expand whatever their temperature (src/Run.cpp:655): the claims are
+  // issued first and run while this point is evaluated; the claimed neighbours are
+  // published after the pass.
+  Claims rc{0, 0, 0xffffffffu};
+  if (SURF && type == IT_RETEST) rc = claim_neighbours<SURF>(P, S, X, p);
   EvalT T3[3];
   int D = 0;
   if (SURF && PREC != 0) {                 // the point and the layers its depth walk starts with
@@ -852,6 +849,7 @@ __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx&
     if (SURF) D = type == IT_RETEST ? Dk : (seed ? ldcg_i(S.depths + p / P.nz) : aux);
     T3[0] = eval_T<PREC>(P, S, X, X.nb, X.nn, p, X.st);
   }
+  if (SURF && type == IT_RETEST) emit_claimed(S, X, rc, nchild);
   if (seed && !__shfl_sync(0xffffffffu, got, 0)) return 0;
   const EvalT T = T3[0];
   pairs += X.nn;
