@@ -214,8 +214,9 @@ def run_solidification(args, th, torch, dev, path, deck, world):
             "achieved": achieved / 1e9, "peak": peak_pairs / 1e9, "unit": "Gpairs/s", "frac": achieved / peak_pairs,
             "peak_basis": f"{SM_COUNT} SMs x {clk_mhz:.0f} MHz x min({FP32_LANES}/{FP32_OPS_KAHAN} FP32 lane-ops, "
                           f"{MUFU_LANES} MUFU) pairs/clk",
-            "note": "each timestep evaluates ~1e3 points x ~300 nodes in a work queue closed by one grid barrier; "
-                    "the loop is bound by per-step latency, not by FP32/MUFU issue or HBM",
+            "note": "each timestep runs ~580 work items (~690 evaluation passes of ~400 nodes) as a chain of "
+                    "dependent L2 round trips (claims, queue slots, step word); the loop is bound by per-step "
+                    "latency, not by FP32/MUFU issue or HBM",
             "traffic": None, "peak_source": src}
     sim.close()
     detail = {"steps": int(st["steps"]), "pairs_per_step": pairs, "ms_node_windows": st["ms_nodes"],
