@@ -55,7 +55,7 @@ FP32_OPS_KAHAN = 9.5
 OPS_PER_PAIR = 16           # algorithmic work of a pair: 15 floating-point operations + 1 exp
 # DRAM bytes (read + write) of one launch of the dominant kernel, from one ncu capture of
 # that kernel on that deck (dram__bytes_read.sum + dram__bytes_write.sum)
-NCU_TRAFFIC = {"snapshot_raster": 21248}
+NCU_TRAFFIC = {"snapshot_raster": 21248, "surface_serpentine": 4024192}
 
 DECK_TEXT = {
     "surface_serpentine": "Solidification/Surface; 50 tracks x 5 mm serpentine, hatch 80 um, 0.8 m/s, P=200 W, "
@@ -217,7 +217,8 @@ def run_solidification(args, th, torch, dev, path, deck, world):
             "note": "each timestep runs ~580 work items (~690 evaluation passes of ~400 nodes) as a chain of "
                     "dependent L2 round trips (claims, queue slots, step word); the loop is bound by per-step "
                     "latency, not by FP32/MUFU issue or HBM",
-            "traffic": None, "peak_source": src}
+            "traffic": NCU_TRAFFIC.get(args.workload) if args.precision == "fp32" else None,
+            "traffic_unit": "DRAM bytes per tracking launch (~256 timesteps)", "peak_source": src}
     sim.close()
     detail = {"steps": int(st["steps"]), "pairs_per_step": pairs, "ms_node_windows": st["ms_nodes"],
               "ms_tracking": st["ms_track"], "ms_solidify": st["ms_solidify"], "records": int(st["records"]),
