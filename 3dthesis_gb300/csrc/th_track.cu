@@ -17,6 +17,7 @@
 #include <cfloat>
 #include <climits>
 #include <cstdint>
+#include <cstdlib>
 #include <cuda_runtime.h>
 
 #include "th_device.cuh"
@@ -1477,6 +1478,12 @@ static cudaError_t launch_track_t(const DevProblem& P, const TrackState& S, cons
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   // stage whole lists up to the slot capacity, within 200 KB of shared memory for the three buffers
   int cap = std::min(w.slot_cap, (200 * 1024) / (3 * staged_bytes_per_node<PREC>()));
+  // THESIS_GB300_STAGE_CAP (tests): stage at most this many nodes of a list, so that the
+  // passes read the rest from the node window as they do for lists longer than the stage
+  if (const char* env = std::getenv("THESIS_GB300_STAGE_CAP")) {
+    const int v = std::atoi(env);
+    if (v > 0) cap = std::min(cap, v);
+  }
   cap = std::max(kListPad, cap & ~(kListPad - 1));
   const size_t smem = (size_t)3 * cap * staged_bytes_per_node<PREC>() +
                       (axis_in_smem<PREC>(P) ? (size_t)(P.nx + P.ny + P.nz) * sizeof(float2) : 0);

@@ -159,3 +159,54 @@ def test_steps_match_oracle_loop(runs):
     for tag, (deck, ref, gpu) in runs.items():
         assert gpu["fp64"]["steps"] == ref["steps"], tag
         assert gpu["fp32"]["steps"] == ref["steps"], tag
+
+
+@pytest.fixture(scope="module")
+def bcs_run(built_library, oracle, tmp_path_factory):
+    """The small Surface deck with four reflecting planes (two reflections): every node list
+    carries its image copies, several hundred nodes."""
+    d = make_golden.run_deck("small_surface")
+    d.name = "small_surface_bcs"
+    d.bcs = {"X_min": -0.1e-3, "X_max": 0.5e-3, "Y_min": -0.15e-3, "Z_min": -0.2e-3, "Reflections": 2}
+    path = d.write(str(tmp_path_factory.mktemp("bcs") / d.name))
+    o = oracle(path)
+    steps = o.solidify(threads=8)
+    ref = {f: o.field(f) for f in _fields(d) + ["output_flag"]}
+    ref["steps"] = steps
+    n = max(len(o.nodes(i * 1e-4, True)["xb"]) for i in range(1, 40))
+    return d, path, ref, n
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_lists_past_the_staged_copy(bcs_run, thesis, monkeypatch, prec):
+    """With at most 128 nodes of each list staged in shared memory, the tracking passes read
+    the rest of the list from the node window (the path of lists longer than the stage).
+    FP64 lanes keep their summation order, so that run is bit-identical to the fully staged
+    one; both precisions meet the oracle tolerances above on a deck with image copies."""
+    deck, path, ref, n_max = bcs_run
+    assert n_max > 256, n_max
+    runs = {}
+    for cap in ("", "128"):
+        monkeypatch.setenv("THESIS_GB300_STAGE_CAP", cap)
+        with thesis.Simulation(path, prec) as sim:
+            steps = sim.solidify()
+            runs[cap] = {f: sim.field(f) for f in _fields(deck) + ["output_flag"]}
+            runs[cap]["steps"] = steps
+    g = runs["128"]
+    assert g["steps"] == runs[""]["steps"] == ref["steps"]
+    if prec == "fp64":
+        for f in g:
+            if f != "steps":
+                assert np.array_equal(g[f], runs[""][f]), f
+    a, b = ref["output_flag"] > 0, g["output_flag"] > 0
+    common = a & b
+    assert common.sum() > 100
+    dT = np.abs(ref["T"][common] - g["T"][common])
+    if prec == "fp64":
+        assert np.array_equal(a, b)
+        assert np.max(dT) <= 1e-7
+    else:
+        assert np.sum(a != b) <= max(3, a.sum() // 2000)
+        assert np.mean(dT <= 0.01) >= 0.998, np.sum(dT > 0.01)
+    tol = 1e-15 if prec == "fp64" else 1e-8
+    assert np.max(np.abs(ref["tSol"][common] - g["tSol"][common])) <= tol
