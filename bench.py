@@ -9,6 +9,8 @@ Workloads (synthetic decks in the reference's own input format, 3dthesis_gb300/d
       tracking: 50 x 5 mm serpentine, hatch 80 um, 0.8 m/s, 200 W, 500x500x100 grid at
       10 um (25 M points), dt = 1e-5 s, outputs tSol/G/V/dTdt.  One step = the whole run
       (31,769 timesteps to the finish test) from t = 0.
+  volume_multibeam - Solidification mode, Volume tracking, four beams on seeded rotated
+      serpentines over a 400x400x80 grid, dt = 5e-6 s.  One step = the whole run.
   snapshot_raster - Snapshots mode: 10 x 2 mm raster on a 200x100x40 grid, snapshots at
       25/50/100 %.  One step = the three snapshots.
   snapshot_sweep - 256 independent Snapshots decks of uneven sizes (a process-parameter
@@ -60,6 +62,9 @@ NCU_TRAFFIC = {"snapshot_raster": 21248, "surface_serpentine": 4024192}
 DECK_TEXT = {
     "surface_serpentine": "Solidification/Surface; 50 tracks x 5 mm serpentine, hatch 80 um, 0.8 m/s, P=200 W, "
                           "eta=0.35, 50/50/1 um; grid 500x500x100 at 10 um; dt=1e-5 s; outputs tSol,G,V,dTdt",
+    "volume_multibeam": "Solidification/Volume, 4 beams (seed 0), each a serpentine of 20 x 3 mm tracks rotated "
+                        "by U[0,pi), v~U(0.5,1.5) m/s, P~U(150,400) W, widths~U(40,100) um; grid 400x400x80 at "
+                        "10 um; dt=5e-6 s; outputs tSol,G,V,dTdt",
     "snapshot_raster": "Snapshots; 10 tracks x 2 mm, hatch 0.1 mm, 1.0 m/s, P=200 W, eta=0.35, 50/50/1 um; "
                        "grid 200x100x40 at 10 um; snapshots at 25/50/100 %",
     "snapshot_sweep": "256 independent Snapshots decks (seed 0): P~U(100,400) W, v~U(0.5,2) m/s, "
@@ -210,7 +215,8 @@ def run_solidification(args, th, torch, dev, path, deck, world):
     track_pairs = st["pairs_total"] - st["pairs_solidify"]
     peak_pairs = SM_COUNT * clk_mhz * 1e6 * min(FP32_LANES / FP32_OPS_KAHAN, MUFU_LANES)
     achieved = track_pairs / (st["ms_track"] / 1e3)
-    roof = {"bound": "latency", "kernel": "k_track (persistent Surface loop)",
+    loop = "Volume" if args.workload == "volume_multibeam" else "Surface"
+    roof = {"bound": "latency", "kernel": f"k_track (persistent {loop} loop)",
             "achieved": achieved / 1e9, "peak": peak_pairs / 1e9, "unit": "Gpairs/s", "frac": achieved / peak_pairs,
             "peak_basis": f"{SM_COUNT} SMs x {clk_mhz:.0f} MHz x min({FP32_LANES}/{FP32_OPS_KAHAN} FP32 lane-ops, "
                           f"{MUFU_LANES} MUFU) pairs/clk",
@@ -497,15 +503,10 @@ def cpu_sample(path, workload, threads, budget_s):
             pairs += o.pairs - p0
             n += 1
         return pairs / used, f"{n} whole snapshots of the deck ({used:.1f} s)"
-    # solidification: a first short run sizes the prefix to the budget
+    # solidification: the run from t = 0 until the step that ends past the time budget
     o = oracle_lib.Oracle(path)
     t0 = time.perf_counter()
-    o.solidify(threads=threads, max_steps=400)
-    dt = time.perf_counter() - t0
-    steps = int(max(400, min(31769, 400 * budget_s / max(dt, 1e-3))))
-    o = oracle_lib.Oracle(path)
-    t0 = time.perf_counter()
-    done = o.solidify(threads=threads, max_steps=steps)
+    done = o.solidify(threads=threads, budget_s=budget_s)
     used = time.perf_counter() - t0
     return o.pairs / used, f"the first {done} timesteps of the run ({used:.1f} s, {o.pairs:.3e} pairs)"
 
@@ -561,7 +562,8 @@ def main():
     torch.cuda.set_device(dev)
     tmp = tempfile.mkdtemp(prefix="thesis_bench_")
     deck, path = make_deck(args.workload, tmp)
-    runner = {"surface_serpentine": run_solidification, "snapshot_raster": run_snapshot,
+    runner = {"surface_serpentine": run_solidification, "volume_multibeam": run_solidification,
+              "snapshot_raster": run_snapshot,
               "snapshot_sweep": run_sweep, "adjoint_calibration": run_adjoint}[args.workload]
     r = runner(args, th, torch, dev, path, deck, world)
     line = {"metric": METRIC, "value": r["value"], "unit": "pairs/s", "n_gpus": world, "steps": args.steps,

@@ -728,7 +728,8 @@ void alloc_state(Problem& P) {
 bool finished(const Problem& P, double t, long liq) { return t > P.end_time && liq == 0; }   // src/Util.cpp:239-243
 
 // src/Run.cpp:409-467
-int64_t run_notracking(Problem& P, int threads, int64_t max_steps) {
+int64_t run_notracking(Problem& P, int threads, int64_t max_steps, double budget_s) {
+  const double t_start = omp_get_wtime();
   std::fill(P.T.begin(), P.T.end(), P.T0);
   Nodes N;
   double t = 0.0;
@@ -745,12 +746,14 @@ int64_t run_notracking(Problem& P, int threads, int64_t max_steps) {
     if (finished(P, t, liq)) break;
     t += P.dt; ++step;
     if (max_steps > 0 && step >= max_steps) break;
+    if (budget_s > 0 && omp_get_wtime() - t_start > budget_s) break;
   }
   return step + 1;
 }
 
 // src/Run.cpp:469-573 (Volume) and 575-709 (Surface)
-int64_t run_tracking(Problem& P, int threads, int64_t max_steps) {
+int64_t run_tracking(Problem& P, int threads, int64_t max_steps, double budget_s) {
+  const double t_start = omp_get_wtime();
   const bool surface = P.tracking == TRACK_SURFACE;
   const int nx = P.nx, ny = P.ny, nz = P.nz;
   std::vector<long> liq, reset;
@@ -861,6 +864,7 @@ int64_t run_tracking(Problem& P, int threads, int64_t max_steps) {
     t += P.dt; ++step;
     Nlast = N;
     if (max_steps > 0 && step >= max_steps) break;
+    if (budget_s > 0 && omp_get_wtime() - t_start > budget_s) break;
   }
   return step + 1;
 }
@@ -924,13 +928,15 @@ void or_snapshot(void* h, int idx, double* T, int threads) {                   /
   for (long p = 0; p < P.pnum; ++p) T[p] = sum_T(P, N, p);
 }
 
-int64_t or_solidify(void* h, int threads, int64_t max_steps) {
+int64_t or_solidify_budget(void* h, int threads, int64_t max_steps, double budget_s) {
   Problem& P = *(Problem*)h;
   if (threads <= 0) threads = omp_get_max_threads();
   if (P.mode != 1) return -1;
-  if (P.tracking == TRACK_NONE) return run_notracking(P, threads, max_steps);
-  return run_tracking(P, threads, max_steps);
+  if (P.tracking == TRACK_NONE) return run_notracking(P, threads, max_steps, budget_s);
+  return run_tracking(P, threads, max_steps, budget_s);
 }
+
+int64_t or_solidify(void* h, int threads, int64_t max_steps) { return or_solidify_budget(h, threads, max_steps, 0.0); }
 
 int or_field(void* h, const char* name, double* out) {
   Problem& P = *(Problem*)h;

@@ -45,6 +45,10 @@ void  or_snapshot(void* h, int idx, double* T, int threads);
  * the reference's finish test.  Returns the number of steps taken. */
 int64_t or_solidify(void* h, int threads, int64_t max_steps);
 
+/* The same, also stopping after the first step that ends more than budget_s seconds of wall
+ * time after the start (budget_s <= 0: no limit); for timing a bounded prefix of a run. */
+int64_t or_solidify_budget(void* h, int threads, int64_t max_steps, double budget_s);
+
 /* Per-point field after or_solidify: "T", "tSol", "G", "V", "Gx", "Gy", "Gz", "dTdt",
  * "eqFrac", "numMelt", "depth", "output_flag".  Returns 0 on success. */
 int   or_field(void* h, const char* name, double* out);

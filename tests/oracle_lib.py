@@ -30,6 +30,8 @@ def load():
         L.or_snapshot.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int]
         L.or_solidify.argtypes = [vp, ctypes.c_int, ctypes.c_int64]
         L.or_solidify.restype = ctypes.c_int64
+        L.or_solidify_budget.argtypes = [vp, ctypes.c_int, ctypes.c_int64, ctypes.c_double]
+        L.or_solidify_budget.restype = ctypes.c_int64
         L.or_field.argtypes = [vp, ctypes.c_char_p, vp]
         L.or_solid_fields.argtypes = [vp, ctypes.c_int64, ctypes.c_double, vp]
         L.or_pairs.argtypes = [vp]
@@ -81,8 +83,10 @@ class Oracle:
         _lib.or_snapshot(self.h, i, out.ctypes.data_as(ctypes.c_void_p), threads)
         return out
 
-    def solidify(self, threads=0, max_steps=0):
-        return _lib.or_solidify(self.h, threads, max_steps)
+    def solidify(self, threads=0, max_steps=0, budget_s=0.0):
+        """Steps taken; stops at the finish test, after max_steps (> 0) or after the first
+        step ending more than budget_s (> 0) seconds after the start."""
+        return _lib.or_solidify_budget(self.h, threads, max_steps, float(budget_s))
 
     def field(self, name):
         out = np.empty(self.pnum)
