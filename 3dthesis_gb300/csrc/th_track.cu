@@ -879,7 +879,17 @@ __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx&
 }
 
 // ------------------------------------------------------------------ the tracking loop
-constexpr int kTrackThreads = 128;   // four warps per block, one block per SM
+// Warps per block, one block per SM: Surface steps are short chains of ~500 items (latency-
+// bound; more waiting warps only add polls), Volume steps have ~1e5 items (throughput-
+// bound: eight warps share one staged copy of the lists).
+template <bool SURF>
+constexpr int track_threads() { return SURF ? 128 : 256; }
+// The thread bound the kernel is compiled for: the Volume kernel is held to the registers of
+// 328 threads (no spills) so that a 128-thread bulk-solidification block of the other
+// stream still fits beside its 256-thread block; at its unconstrained 230 registers the
+// solidification of a window waited for the tracking launch and ran after it.
+template <bool SURF>
+constexpr int track_bound() { return SURF ? 128 : 328; }
 // One launch runs steps [k_begin, k_end) of a Volume or Surface loop (src/Run.cpp:469-709).
 // Each step is a single phase: the previous step's liquid points are re-tested, the beam
 // trace seeds the new ones, and every claimed point, column and depth walk becomes a work
@@ -905,7 +915,7 @@ __host__ __device__ __forceinline__ bool axis_in_smem(const DevProblem& P) {
 }
 
 template <int PREC, bool SURF>
-__global__ void __launch_bounds__(kTrackThreads, 1) k_track(DevProblem P, TrackState S, NodeWindow W, int k_begin,
+__global__ void __launch_bounds__(track_bound<SURF>(), 1) k_track(DevProblem P, TrackState S, NodeWindow W, int k_begin,
                                                             int k_end, int high_water, int stage_cap) {
   extern __shared__ __align__(16) unsigned char stage_mem[];
   __shared__ BlockBuf bbuf;
@@ -1500,14 +1510,14 @@ static cudaError_t launch_track_t(const DevProblem& P, const TrackState& S, cons
   const int carve = std::min(100, (int)((need * 100 + 228 * 1024 - 1) / (228 * 1024)));
   e = cudaFuncSetAttribute(k_track<PREC, SURF>, cudaFuncAttributePreferredSharedMemoryCarveout, carve);
   if (e != cudaSuccess) return e;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_track<PREC, SURF>, kTrackThreads, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_track<PREC, SURF>, track_threads<SURF>(), smem);
   const int blocks = sms * (occ < 1 ? occ : 1);
   if (blocks <= 0) return cudaErrorInvalidConfiguration;
   DevProblem Pc = P;
   TrackState Sc = S;
   NodeWindow Wc = w;
   void* args[] = {&Pc, &Sc, &Wc, &k_begin, &k_end, &hw, &cap};
-  return cudaLaunchCooperativeKernel((const void*)k_track<PREC, SURF>, dim3(blocks), dim3(kTrackThreads), args, smem,
+  return cudaLaunchCooperativeKernel((const void*)k_track<PREC, SURF>, dim3(blocks), dim3(track_threads<SURF>()), args, smem,
                                      s);
 }
 
