@@ -161,7 +161,6 @@ th_status init_run(th_ctx* ctx) {
   ALLOC(r->rec[0], (size_t)kRecCap, 0);
   ALLOC(r->rec[1], (size_t)kRecCap, 0);
   ALLOC(S.C, 1, 0);
-  ALLOC(S.bar, 2, 0);
   ALLOC(S.err, 1, 0);
 #undef ALLOC
   {  // point coordinates (the device's coord(): min + i * h, or max on a one-point axis) as float pairs
@@ -310,8 +309,8 @@ th_status read_counters(th_ctx* ctx, RunState* r, TrackCounters* h) {
   if (st != TH_OK) return st;
   if (err & 16) {
     char b[256];
-    std::snprintf(b, sizeof(b), "a %s wait exceeded its limit (step %d, ticket %d, initial items %d, tickets %d, "
-                  "published %d, published %d, completed %d, errors 0x%x)", h->diag[0] == 2 ? "grid barrier" : "work-queue",
+    std::snprintf(b, sizeof(b), "a work-queue wait exceeded its limit (step %d, ticket %d, initial items %d, "
+                  "tickets taken %d, blocks entered %d, published %d, completed %d, errors 0x%x)",
                   h->diag[1], h->diag[2], h->diag[3], h->diag[4], h->diag[5], h->diag[6], h->diag[7], err);
     return th_fail(ctx, TH_ERR_TIMEOUT, b);
   }
@@ -368,7 +367,6 @@ th_status advance_tracking(th_ctx* ctx, int64_t stop_at) {
     TrackState S = r->S;
     S.rec = r->rec[b];
     S.rec_n = &r->S.C->rec_n[b];
-    if ((st = th_cuda_check(ctx, cudaMemsetAsync(r->S.bar, 0, 2 * sizeof(unsigned), ts), "cudaMemsetAsync")) != TH_OK) return st;
     cudaEventRecord(r->ev_trk[b][0], ts);
     st = th_cuda_check(ctx, th_launch_track(ctx->dp, S, w.W, w.base, w.base + w.n, ctx->precision, r->S.rec_cap / 2, ts),
                        "cooperative launch");

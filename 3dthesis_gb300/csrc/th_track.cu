@@ -890,11 +890,6 @@ constexpr int track_threads() { return SURF ? 128 : 256; }
 // solidification of a window waited for the tracking launch and ran after it.
 template <bool SURF>
 constexpr int track_bound() { return SURF ? 128 : 328; }
-// One launch runs steps [k_begin, k_end) of a Volume or Surface loop (src/Run.cpp:469-709).
-// Each step is a single phase: the previous step's liquid points are re-tested, the beam
-// trace seeds the new ones, and every claimed point, column and depth walk becomes a work
-// item that any warp may take; a packed (published << 32 | completed) counter tells the
-// warps when the step has no work left, and one grid barrier ends the step.
 // The first 48 bytes of a step's QueueCounters (head, depth, lvl_start, lvl_end) into
 // shared memory, bypassing L1 (the counters are updated by atomics in L2).
 __device__ __forceinline__ void copy_step_prof(const QueueCounters* q, unsigned* dst) {
@@ -914,6 +909,12 @@ __host__ __device__ __forceinline__ bool axis_in_smem(const DevProblem& P) {
   return PREC != 0 && P.nx + P.ny + P.nz <= kAxisSmem;
 }
 
+// One launch runs steps [k_begin, k_end) of a Volume or Surface loop (src/Run.cpp:469-709).
+// Each step is a single phase: the previous step's liquid points are re-tested, the beam
+// trace seeds the new ones, and every claimed point, column and depth walk becomes a work
+// item that any warp may take; the step word (entered blocks, published and completed
+// items) tells when the step has no work left, and the step's end is published as one word
+// that the waiting warps poll (no grid barrier).
 template <int PREC, bool SURF>
 __global__ void __launch_bounds__(track_bound<SURF>(), 1) k_track(DevProblem P, TrackState S, NodeWindow W, int k_begin,
                                                             int k_end, int high_water, int stage_cap) {

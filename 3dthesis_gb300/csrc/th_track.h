@@ -41,11 +41,12 @@ struct alignas(128) TrackCounters {
   int done;         // finish test passed
   int stop;         // the loop stopped early (record queue high-water mark)
   int max_items;    // most work items in one step
-  int diag[8];      // where a bounded wait gave up: kind, step, ticket, n_init, head, tail, published, completed
-  // loop profile: block 0's work-phase and barrier time (ns), items run, item and wait
-  // time summed over warps (SM clocks), summed per-step chain depth, steps profiled,
-  // point evaluations and their SM clocks summed over warps, then the per-step latest
-  // start and end of items of chain depth 0..3 (ns) summed over steps
+  int diag[8];      // where a bounded wait gave up: 1, step, ticket, n_init, tickets taken, blocks entered, published, completed
+  // loop profile: [0] block 0's work-phase time (ns), [1] unused (0; the loop has no grid
+  // barrier), [2] items run, [3], [4] item and wait time summed over warps (SM clocks),
+  // [5] summed per-step chain depth, [6] steps profiled, [7], [8], [9] evaluation passes,
+  // their SM clocks and their nodes summed over warps, [10..13], [14..17] the per-step
+  // latest start and end of items of chain depth 0..3 (ns) summed over steps
   unsigned long long prof[18];
   alignas(128) int liq_n[3];     // liquid list lengths
   alignas(128) int rec_n[2];     // solidification records queued in each of the two record buffers
@@ -78,7 +79,6 @@ struct TrackState {
   TrackCounters* C;
   const float2* axis;      // grid coordinates as (hi, lo) floats: x[0, nx), y[nx, nx + ny), z after
   int t_fixed;             // T and the records' T, T_last hold FP32 tracking's fixed point (see t_decode)
-  unsigned* bar;           // grid barrier: [0] arrivals, [1] generation
   int* err;
   unsigned long long* pairs;
 };

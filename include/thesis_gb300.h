@@ -145,7 +145,8 @@ th_status th_run_reset(th_ctx* ctx);
  * records, most work items in one step (tracking), steps, node slots per step,
  * device-elapsed ms of th_solidify calls (host gaps included), point x node pairs of the
  * bulk solidification, all point x node pairs of the context; then the tracking loop's
- * profile: ms of block 0's work phases, ms of block 0's barrier waits, work items run,
+ * profile: ms of block 0's work phases, 0 (a slot kept for a barrier time; the loop has
+ * no grid barrier), work items run,
  * SM clocks spent in items and in waiting for items (summed over warps), the per-step
  * longest parent -> child item chain summed over steps, steps profiled, point evaluations
  * and their SM clocks summed over warps, then per chain depth 0, 1, 2, >= 3 the latest
