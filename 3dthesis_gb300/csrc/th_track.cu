@@ -431,16 +431,31 @@ __device__ __forceinline__ void eval_Tn(const DevProblem& P, const TrackState& S
   X.ev_nodes += X.nn;
 }
 
-// Publishes one child item per lane that has one (warp-uniform call).  The children are
+// A claimed neighbour the warp keeps instead of publishing it (Volume tracking): it runs in
+// the same warp right after the item that claimed it and is part of that item (never
+// published, never completed on its own), so it starts without a trip through the queue.
+struct Kept { int p, aux; bool valid; };
+
+// Publishes one child item per lane that has one (warp-uniform call); with `keep`, the
+// lowest such lane's child is kept instead when the item keeps none yet.  The children are
 // counted as published in the same atomic that hands out their slots, before any of them
 // can be taken, so "completed == initial + published" can only hold once the step has no
 // work left.  Both 64-bit words of a slot carry the step's stamp, so a reader that sees
 // the stamp in both has the whole item without any further ordering.
 __device__ __forceinline__ void emit(const TrackState& S, const StepCtx& X, bool has, int type, int p, int aux,
-                                     int& nchild) {
+                                     int& nchild, Kept* keep = nullptr) {
   const int lane = threadIdx.x & 31;
-  const unsigned m = __ballot_sync(0xffffffffu, has);
+  unsigned m = __ballot_sync(0xffffffffu, has);
   if (!m) return;
+  if (keep != nullptr && !keep->valid) {
+    const int kl = __ffs(m) - 1;
+    keep->p = __shfl_sync(0xffffffffu, p, kl);
+    keep->aux = __shfl_sync(0xffffffffu, aux, kl);
+    keep->valid = true;
+    m &= m - 1u;
+    if (lane == kl) has = false;
+    if (!m) return;
+  }
   unsigned base = 0;
   if (lane == 0) base = (unsigned)((atomicAdd(&X.qc->state, (unsigned long long)__popc(m) << 24) >> 24) & kField);
   base = __shfl_sync(0xffffffffu, base, 0);
@@ -449,7 +464,7 @@ __device__ __forceinline__ void emit(const TrackState& S, const StepCtx& X, bool
     if (j < (unsigned)S.queue_cap) {
       const unsigned long long hi = (unsigned long long)X.stamp << 32;
       st_relaxed_v2(S.queue + j, hi | (unsigned)p,
-                    hi | (unsigned)(type | ((X.depth + 1) << 8) | (aux << 16)));
+                    hi | (unsigned)(type | (min(X.depth + 1, 255) << 8) | (aux << 16)));
     } else {
       atomicOr(S.err, ERR_QUEUE);
     }
@@ -483,13 +498,15 @@ __device__ __forceinline__ Claims claim_neighbours(const DevProblem& P, const Tr
   return c;
 }
 
-__device__ __forceinline__ void emit_claimed(const TrackState& S, const StepCtx& X, const Claims& c, int& nchild) {
-  emit(S, X, c.old < X.stamp, IT_VISIT, c.q, c.dq, nchild);
+__device__ __forceinline__ void emit_claimed(const TrackState& S, const StepCtx& X, const Claims& c, int& nchild,
+                                             Kept* keep) {
+  emit(S, X, c.old < X.stamp, IT_VISIT, c.q, c.dq, nchild, keep);
 }
 
 template <bool SURF>
-__device__ __forceinline__ void expand(const DevProblem& P, const TrackState& S, const StepCtx& X, int p, int& nchild) {
-  emit_claimed(S, X, claim_neighbours<SURF>(P, S, X, p), nchild);
+__device__ __forceinline__ void expand(const DevProblem& P, const TrackState& S, const StepCtx& X, int p, int& nchild,
+                                       Kept* keep) {
+  emit_claimed(S, X, claim_neighbours<SURF>(P, S, X, p), nchild, keep);
 }
 
 // A liquid point joins the next step's list with its column's depth (the next re-test
@@ -813,7 +830,7 @@ __device__ int depth_walk(const DevProblem& P, const TrackState& S, const StepCt
 // A re-test brings its column's depth from the liquid list (Dk); other items read it.
 template <int PREC, bool SURF>
 __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx& X, int type, int p, int aux,
-                        int Dk, bool seed, bool got, unsigned long long& pairs) {
+                        int Dk, bool seed, bool got, unsigned long long& pairs, Kept& kept) {
   const int lane = threadIdx.x & 31;
   int nchild = 0;
   const double Told = ldcg_d(S.T + p);
@@ -850,7 +867,7 @@ __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx&
     if (SURF) D = type == IT_RETEST ? Dk : (seed ? ldcg_i(S.depths + p / P.nz) : aux);
     T3[0] = eval_T<PREC>(P, S, X, X.nb, X.nn, p, X.st);
   }
-  if (SURF && type == IT_RETEST) emit_claimed(S, X, rc, nchild);
+  if (SURF && type == IT_RETEST) emit_claimed(S, X, rc, nchild, nullptr);
   if (seed && !__shfl_sync(0xffffffffu, got, 0)) return 0;
   const EvalT T = T3[0];
   pairs += X.nn;
@@ -859,7 +876,10 @@ __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx&
     int slot = 0;
     if (lane == 0) slot = atomicAdd(X.lo_n, 1);
     // Volume expands the liquid points; Surface the liquid visits (re-tests did above)
-    if (!(SURF && type == IT_RETEST)) expand<SURF>(P, S, X, p, nchild);
+    // Volume items keep one claimed neighbour to run next in the same warp; Surface items
+    // publish all of them (a kept child would wait for the rest of a long re-test or depth
+    // walk, longer than the queue takes to hand it to another warp)
+    if (!(SURF && type == IT_RETEST)) expand<SURF>(P, S, X, p, nchild, SURF ? nullptr : &kept);
     // the depth walk under a liquid surface point needs nothing else from this step
     int Dn = 0;
     if (SURF) Dn = depth_walk<PREC>(P, S, X, p, D, T3[1], T3[2], pairs);
@@ -1109,12 +1129,26 @@ __global__ void __launch_bounds__(track_bound<SURF>(), 1) k_track(DevProblem P, 
         max_depth = X.depth;
         if (lane == 0) atomicMax(&X.qc->depth, (unsigned)max_depth);
       }
-      const unsigned long long g_item = globaltimer();
-      run_item<PREC, SURF>(P, S, X, type, p, aux, Dk, is_seed, got, pairs);
-      if (lane == 0) {
-        const int l = min(X.depth, 3);
-        atomicMax(&X.qc->lvl_start[l], (unsigned)(g_item - g0));
-        atomicMax(&X.qc->lvl_end[l], (unsigned)(globaltimer() - g0));
+      unsigned long long g_item = globaltimer();
+      Kept kept{0, 0, false};
+      while (true) {
+        run_item<PREC, SURF>(P, S, X, type, p, aux, Dk, is_seed, got, pairs, kept);
+        if (lane == 0) {
+          const int l = min(X.depth, 3);
+          atomicMax(&X.qc->lvl_start[l], (unsigned)(g_item - g0));
+          atomicMax(&X.qc->lvl_end[l], (unsigned)(globaltimer() - g0));
+        }
+        if (!kept.valid) break;
+        // the kept child runs next; the item completes once its chain of kept children ends
+        type = IT_VISIT; p = kept.p; aux = kept.aux; Dk = 0; is_seed = false; got = false;
+        kept.valid = false;
+        ++X.depth;
+        if (X.depth > max_depth) {
+          max_depth = X.depth;
+          if (lane == 0) atomicMax(&X.qc->depth, (unsigned)max_depth);
+        }
+        ++n_items;
+        g_item = globaltimer();
       }
       if (lane == 0) {                                           // completed, after the item's writes
         const unsigned long long st = atom_add_release(&X.qc->state, 1ull);
