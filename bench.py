@@ -1,7 +1,8 @@
 """Benchmark of the 3DThesis hot path on GB300: point x node pairs per second.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload surface_serpentine|snapshot_raster|snapshot_sweep]
+                    [--workload surface_serpentine|volume_multibeam|snapshot_raster|snapshot_sweep|
+                                adjoint_calibration]
                     [--precision fp32|fp64] [--tile KPxKCH]
 
 Workloads (synthetic decks in the reference's own input format, 3dthesis_gb300/decks.py):
@@ -15,6 +16,8 @@ Workloads (synthetic decks in the reference's own input format, 3dthesis_gb300/d
       25/50/100 %.  One step = the three snapshots.
   snapshot_sweep - 256 independent Snapshots decks of uneven sizes (a process-parameter
       sweep) evaluated as one batch: one step = one CUDA-graph replay of the batch snapshot.
+  adjoint_calibration - probe temperatures of the Surface deck's path on a 300x300x60 grid
+      and their gradient over all parameters: one step = forward + adjoint.
 
 ``value`` = point x node pairs of the step / the step's time with the deck resident in HBM
 (inputs on the device before timing; L2 flushed with a 256 MiB write before each step,
@@ -22,7 +25,8 @@ outside the timed region; times from CUDA events on the library's stream).
 ``e2e`` times what a user calls through the C ABI with host buffers: context creation from
 the deck files (parse + upload), the run, and the D2H copy of the output fields into
 pinned memory.  ``cpu_baseline`` and ``--impl reference`` time the CPU oracle (the
-reference's algorithm restated in C++, OpenMP over all host cores) on a bounded sample.
+reference's algorithm restated in C++, OpenMP over all host cores) on a bounded sample
+(solidification: the run from t = 0 until the timestep that ends past a ~15 s budget).
 
 Under torchrun each rank runs the same per-GPU workload (weak scaling, no collective on
 the data path); rank 0 prints the max-over-ranks time.
