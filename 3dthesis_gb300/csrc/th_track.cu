@@ -65,13 +65,14 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 }
 
 // A step's node list staged in shared memory, one copy per block.  FP32: ten float arrays
-// of cap entries (xh, yh, zh, xl, yl, zl, kx, ky, kz, w), read two consecutive nodes at a
-// time; FP64: four double2 arrays (x, y), (z, 1/phix), (1/phiy, 1/phiz), (dtau, amp).
-// Nodes at and beyond n_sm are read from the window in global memory.
+// of cap entries (xh, yh, zh, xl, yl, zl, kx, ky, kz, w), read as 16-byte groups of four
+// consecutive nodes, the list's zero-weight padding included; FP64: four double2 arrays
+// (x, y), (z, 1/phix), (1/phiy, 1/phiz), (dtau, amp).  Nodes at and beyond n_sm are read
+// from the window in global memory.
 struct Staged {
   const unsigned char* base;
   int n_sm;                // staged nodes
-  int cap;                 // nodes per staged array (a multiple of 8)
+  int cap;                 // nodes per staged array (a multiple of kListPad)
 };
 
 template <int PREC>
@@ -1039,7 +1040,7 @@ __global__ void __launch_bounds__(track_bound<SURF>(), 1) k_track(DevProblem P, 
     // w, w + warps, ...), so they all start at once; items published during the step are
     // taken with tickets from the queue.  The step is over when every block has entered
     // it and every item has completed; whoever's update of the step word makes that true
-    // resets the counters the next steps use and publishes the step's stamp, which the
+    // resets the counters the next steps use and publishes the step-end word, which the
     // waiting warps see.  No grid barrier separates steps.
     int next_init = tid >> 5;
     long long idle = 0;
