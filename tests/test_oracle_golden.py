@@ -55,3 +55,18 @@ def test_oracle_solidification_matches_reference(tag, oracle, tmp_path):
         v = o.field(f)
         np.testing.assert_allclose(v[sub], g[key], rtol=1e-12, atol=1e-12, err_msg=f)
         np.testing.assert_allclose(np.sum(v[flag]), g[f + "_sum"], rtol=1e-11, err_msg=f)
+
+
+def test_oracle_solidification_time_budget(oracle, tmp_path):
+    """The budgeted run (the bench's bounded CPU sample) stops after the first step that ends
+    past the budget and otherwise runs exactly the unbudgeted loop."""
+    deck = make_golden.run_deck("small_surface")
+    path = deck.write(str(tmp_path / "budget"))
+    full = oracle(path).solidify(threads=2)
+    cut = oracle(path).solidify(threads=2, budget_s=1e-9)
+    assert cut == 2 < full
+    ample = oracle(path)
+    assert ample.solidify(threads=2, budget_s=3600.0) == full
+    ref = oracle(path)
+    ref.solidify(threads=2)
+    assert np.array_equal(ample.field("tSol"), ref.field("tSol"))
