@@ -61,7 +61,7 @@ FP32_OPS_KAHAN = 9.5
 OPS_PER_PAIR = 16           # algorithmic work of a pair: 15 floating-point operations + 1 exp
 # DRAM bytes (read + write) of one launch of the dominant kernel, from one ncu capture of
 # that kernel on that deck (dram__bytes_read.sum + dram__bytes_write.sum)
-NCU_TRAFFIC = {"snapshot_raster": 21248, "surface_serpentine": 4024192}
+NCU_TRAFFIC = {"snapshot_raster": 21248, "surface_serpentine": 4024192, "volume_multibeam": 22929684}
 
 DECK_TEXT = {
     "surface_serpentine": "Solidification/Surface; 50 tracks x 5 mm serpentine, hatch 80 um, 0.8 m/s, P=200 W, "
@@ -224,9 +224,12 @@ def run_solidification(args, th, torch, dev, path, deck, world):
             "achieved": achieved / 1e9, "peak": peak_pairs / 1e9, "unit": "Gpairs/s", "frac": achieved / peak_pairs,
             "peak_basis": f"{SM_COUNT} SMs x {clk_mhz:.0f} MHz x min({FP32_LANES}/{FP32_OPS_KAHAN} FP32 lane-ops, "
                           f"{MUFU_LANES} MUFU) pairs/clk",
-            "note": "each timestep runs ~580 work items (~690 evaluation passes of ~400 nodes) as a chain of "
-                    "dependent L2 round trips (claims, queue slots, step word); the loop is bound by per-step "
-                    "latency, not by FP32/MUFU issue or HBM",
+            "note": (("each timestep runs ~96,000 work items (one evaluation pass of ~1,465 nodes each) over "
+                      "eight warps per SM; bound by the items' L2 round trips (claims, queue slots) and passes, "
+                      "not by FP32/MUFU issue or HBM") if loop == "Volume" else
+                     ("each timestep runs ~580 work items (~690 evaluation passes of ~400 nodes) as a chain of "
+                      "dependent L2 round trips (claims, queue slots, step word); the loop is bound by per-step "
+                      "latency, not by FP32/MUFU issue or HBM")),
             "traffic": NCU_TRAFFIC.get(args.workload) if args.precision == "fp32" else None,
             "traffic_unit": "DRAM bytes per tracking launch (~256 timesteps)", "peak_source": src}
     sim.close()
