@@ -1,5 +1,6 @@
 """The multi-rank path of bench.py (replicas: every rank runs the whole workload, rank 0
-reports the slowest rank's time) with two gloo ranks on the CPU."""
+reports the slowest rank's time) with two gloo ranks on the CPU, and bench.py's bounded
+CPU-oracle sample."""
 import os
 import socket
 import sys
@@ -43,3 +44,16 @@ def test_two_gloo_replicas(tmp_path, decks):
         res = dict(out)
     assert res[0][0] == res[1][0] == 2.0          # both ranks see the slowest rank's time
     assert res[0][1] == res[1][1]                 # replicas compute the same result
+
+
+def test_bench_cpu_sample_is_bounded(tmp_path, decks):
+    """The bench's CPU leg on a solidification deck stops near its time budget (the sample
+    is the run from t = 0 up to the step that ends past the budget) and reports pairs/s."""
+    import time
+    sys.path.insert(0, ROOT)
+    import bench
+    path = decks.small_surface("Surface").write(str(tmp_path / "surface"))
+    t0 = time.perf_counter()
+    value, sample = bench.cpu_sample(path, "surface_serpentine", 2, budget_s=0.05)
+    assert time.perf_counter() - t0 < 10.0
+    assert value > 0 and "timesteps of the run" in sample
