@@ -108,6 +108,10 @@ struct Problem {
   bool do_sol;
   // grid state
   std::vector<double> T, T_last, tSol, G, V, Gx, Gy, Gz, dTdt, eqFrac, depth;
+  // per point, for the parity tests' explanations: the closest approach of an evaluated T
+  // to T_L (DBL_MAX: never evaluated) and the secant's T - T_last at its latest
+  // solidification (0: never solidified)
+  std::vector<double> band, sol_dT;
   std::vector<int> numMelt;
   std::vector<unsigned char> calc, outflag;
   std::atomic<long long> pairs{0};
@@ -434,13 +438,26 @@ int find_seg(const std::vector<Seg>& path, double t) {
   return s;
 }
 
-// Adaptive Gauss integration back along every beam's path (src/Calc.cpp:67-211).
-void gauss_nodes(const Problem& P, double t, bool is_sol, Nodes& N) {
+// FNV-1a over 64-bit words: the signature of a walk's discrete choices.
+inline void sig_mix(uint64_t* h, uint64_t v) {
+  if (!h) return;
+  for (int i = 0; i < 8; ++i) { *h ^= (v >> (8 * i)) & 0xffu; *h *= 1099511628211ull; }
+}
+
+// Adaptive Gauss integration back along every beam's path (src/Calc.cpp:67-211).  With
+// sig, also hashes every discrete choice of the walk - per beam the starting segment, per
+// interval its segment, the number of step-cap doublings so far, its Gauss order and
+// whether it was cut at the segment's start, and per candidate node whether it was kept -
+// so that two times with equal signatures have node lists that are the same continuous
+// function of t.
+void gauss_nodes(const Problem& P, double t, bool is_sol, Nodes& N, uint64_t* sig = nullptr) {
   const GaussTables& G = gauss();
   for (size_t b = 0; b < P.paths.size(); ++b) {
     const Beam& B = P.beams[b];
     const std::vector<Seg>& path = P.paths[b];
     int s = find_seg(path, t);
+    sig_mix(sig, 0xbea0000000000000ull | (uint64_t)b);
+    sig_mix(sig, (uint64_t)s);
     const double beta = std::pow(3.0 / kPi, 1.5) * B.q / (P.rho * P.cps);
     const double t0 = 0.0;                               // src/Util.cpp:174-190 always returns 0
     double step0 = B.nond;
@@ -450,12 +467,14 @@ void gauss_nodes(const Problem& P, double t, bool is_sol, Nodes& N) {
     {
       Loc L = beam_loc(P, path, t, s);
       const double qb = L.q * beta;
-      if (t <= path.back().tend && qb > 0.0)
-        add_node(N, L.x, L.y, L.z, B.ax * B.ax + 0.0, B.ay * B.ay + 0.0, B.az * B.az + 0.0, 0.0, qb);
+      const bool keep = t <= path.back().tend && qb > 0.0;
+      sig_mix(sig, keep ? 1u : 0u);
+      if (keep) add_node(N, L.x, L.y, L.z, B.ax * B.ax + 0.0, B.ay * B.ay + 0.0, B.az * B.az + 0.0, 0.0, qb);
     }
     double t2 = t, t1 = t, tpp = 0.0;
+    int ndbl = 0;                                        // doublings of the step cap so far
     if (t > path.back().tend) { tpp += t - path.back().tend; t2 = path.back().tend; }
-    while (tpp >= 2 * stepmax - step0) { stepmax *= 2.0; if (order != 2) order /= 2; }
+    while (tpp >= 2 * stepmax - step0) { stepmax *= 2.0; ++ndbl; if (order != 2) order /= 2; }
     bool more = true;
     while (more) {
       bool sw = false;
@@ -463,7 +482,9 @@ void gauss_nodes(const Problem& P, double t, bool is_sol, Nodes& N) {
       const double use = (rt < stepmax) ? rt : stepmax;
       t1 = t2 - use;
       const double next = path[s - 1].tend;
+      const bool cut = t1 <= next;
       if (t1 <= next) { t1 = next; if (next > t0) sw = true; else more = false; }
+      sig_mix(sig, ((uint64_t)s << 16) | ((uint64_t)ndbl << 6) | ((uint64_t)order << 1) | (cut ? 1u : 0u));
       const int base = order - 2;
       for (int k = base + order - 1; k >= base; --k) {
         const double tp = 0.5 * ((t2 - t1) * G.loc[k] + (t2 + t1));
@@ -472,13 +493,14 @@ void gauss_nodes(const Problem& P, double t, bool is_sol, Nodes& N) {
         Loc L = beam_loc(P, path, tp, s);
         const double qb = L.q * beta;
         const double dtau = 0.5 * (t2 - t1) * G.w[k];
-        if (qb > 0.0 && dtau > 0.0)
-          add_node(N, L.x, L.y, L.z, B.ax * B.ax + ct, B.ay * B.ay + ct, B.az * B.az + ct, dtau, qb);
+        const bool keep = qb > 0.0 && dtau > 0.0;
+        sig_mix(sig, keep ? 3u : 2u);
+        if (keep) add_node(N, L.x, L.y, L.z, B.ax * B.ax + ct, B.ay * B.ay + ct, B.az * B.az + ct, dtau, qb);
       }
       if (sw) --s;
       tpp += (t2 - t1);
       t2 = t1;
-      if (tpp >= 2 * stepmax - step0) { stepmax *= 2.0; if (order != 2) order /= 2; }
+      if (tpp >= 2 * stepmax - step0) { stepmax *= 2.0; ++ndbl; if (order != 2) order /= 2; }
     }
   }
 }
@@ -549,6 +571,7 @@ double sum_T(Problem& P, const Nodes& N, long p) {                           // 
 double eval_set(Problem& P, const Nodes& N, long p) {
   const double T = sum_T(P, N, p);
   P.T[p] = T;
+  if (!P.band.empty()) P.band[p] = std::min(P.band[p], std::fabs(T - P.TL));
   if (!P.calc.empty()) P.calc[p] = 1;
   if (T >= P.TL) {
     if (!P.G.empty()) P.G[p] = DBL_MIN;
@@ -576,6 +599,7 @@ void solidify(Problem& P, double t, long p) {                                 //
   if (!P.do_sol) return;
   // secant search for the liquidus crossing (src/Grid.cpp:340-404)
   double T2 = P.T[p], T1 = P.T_last[p];
+  P.sol_dT[p] = T2 - T1;
   const double T0 = P.TL;
   double t2 = t, t1 = t - P.dt, tsol = 0.0;
   Nodes N;
@@ -589,7 +613,7 @@ void solidify(Problem& P, double t, long p) {                                 //
     if (Tt > T0) { t1 = tsol; T1 = Tt; } else { t2 = tsol; T2 = Tt; }
   }
   P.tSol[p] = tsol;
-  double out[8];
+  double out[10];
   solid_fields(P, p, tsol, out);
   P.G[p] = out[0]; P.Gx[p] = out[1]; P.Gy[p] = out[2]; P.Gz[p] = out[3];
   P.dTdt[p] = out[4]; P.V[p] = out[5]; P.eqFrac[p] = out[6];
@@ -597,12 +621,15 @@ void solidify(Problem& P, double t, long p) {                                 //
 
 // Nodes at tsol with the refined schedule, then the gradient / Laplacian / source sums
 // (src/Grid.cpp:406-453) and the derived fields (src/Grid.cpp:522-548):
-// out = {G, Gx/G, Gy/G, Gz/G, dTdt, V, eqFrac}.
+// out = {G, Gx/G, Gy/G, Gz/G, dTdt, V, eqFrac}, then three numbers that say how well the
+// fields are conditioned: the cooling rate before its integer truncation, a * lap + dT_t,
+// the magnitude its terms add up to, a * sum |seg (dp^2 + dd)| + sum |dT_t terms|, and the
+// magnitude of the gradient's terms, sum |seg| |dp| (out[7..9]).
 void solid_fields(Problem& P, long p, double tsol, double* out) {
   Nodes N;
   make_nodes(P, tsol, true, N);
   const double xp = px_(P, p), yp = py_(P, p), zp = pz_(P, p);
-  double gx = 0, gy = 0, gz = 0, lap = 0, dTt = 0;
+  double gx = 0, gy = 0, gz = 0, lap = 0, dTt = 0, lap_mag = 0, dtt_mag = 0, g_mag = 0;
   for (size_t n = 0; n < N.size(); ++n) {
     const double dx = xp - N.xb[n], dy = yp - N.yb[n], dz = zp - N.zb[n];
     const double phi = std::exp(-3.0 * ((dx * dx * N.ipx[n]) + (dy * dy * N.ipy[n]) + (dz * dz * N.ipz[n])) + N.expmod[n]);
@@ -612,6 +639,9 @@ void solid_fields(Problem& P, long p, double tsol, double* out) {
     gx += seg * dpx; gy += seg * dpy; gz += seg * dpz;
     lap += seg * (dpx * dpx + dpy * dpy + dpz * dpz + ddx + ddy + ddz);
     dTt += (N.dtau[n] == 0) ? phi : 0;
+    lap_mag += std::fabs(seg) * (dpx * dpx + dpy * dpy + dpz * dpz - (ddx + ddy + ddz));
+    dtt_mag += (N.dtau[n] == 0) ? std::fabs(phi) : 0;
+    g_mag += std::fabs(seg) * std::sqrt(dpx * dpx + dpy * dpy + dpz * dpz);
   }
   P.pairs.fetch_add((long long)N.size(), std::memory_order_relaxed);
   // derived quantities (src/Grid.cpp:522-548)
@@ -620,6 +650,7 @@ void solid_fields(Problem& P, long p, double tsol, double* out) {
   const double V = dTdt / G;
   const double eq = (1.0 - std::exp((-4 * kPi * P.cetN0 / 3) * std::pow(G * (P.cetn + 1) / (std::pow(P.ceta * V, 1 / P.cetn)), -3)));
   out[0] = G; out[1] = gx / G; out[2] = gy / G; out[3] = gz / G; out[4] = dTdt; out[5] = V; out[6] = eq;
+  out[7] = P.a * lap + dTt; out[8] = P.a * lap_mag + dtt_mag; out[9] = g_mag;
 }
 
 // ------------------------------------------------------------------ melt tracking
@@ -716,12 +747,13 @@ void neighbor_round(Problem& P, const Nodes& N, std::vector<long>& test, std::ve
 void alloc_state(Problem& P) {
   const long n = P.pnum;
   P.T.assign(n, 0.0);
-  if (P.mode == 1 || P.tracking != TRACK_NONE) { P.calc.assign(n, 0); P.outflag.assign(n, 0); }
+  if (P.mode == 1 || P.tracking != TRACK_NONE) { P.calc.assign(n, 0); P.outflag.assign(n, 0); P.band.assign(n, DBL_MAX); }
   if (P.mode == 1) {
     P.T_last.assign(n, 0.0);
     P.tSol.assign(n, 0.0); P.G.assign(n, 0.0); P.V.assign(n, 0.0); P.Gx.assign(n, 0.0); P.Gy.assign(n, 0.0);
     P.Gz.assign(n, 0.0); P.dTdt.assign(n, 0.0); P.eqFrac.assign(n, 0.0); P.depth.assign(n, 0.0);
     P.numMelt.assign(n, 0);
+    P.sol_dT.assign(n, 0.0);
   }
 }
 
@@ -745,8 +777,8 @@ int64_t run_notracking(Problem& P, int threads, int64_t max_steps, double budget
     }
     if (finished(P, t, liq)) break;
     t += P.dt; ++step;
-    if (max_steps > 0 && step >= max_steps) break;
-    if (budget_s > 0 && omp_get_wtime() - t_start > budget_s) break;
+    if (max_steps > 0 && step >= max_steps) return step;            // steps run
+    if (budget_s > 0 && omp_get_wtime() - t_start > budget_s) return step;
   }
   return step + 1;
 }
@@ -863,8 +895,8 @@ int64_t run_tracking(Problem& P, int threads, int64_t max_steps, double budget_s
     if (finished(P, t, (long)liq.size())) break;
     t += P.dt; ++step;
     Nlast = N;
-    if (max_steps > 0 && step >= max_steps) break;
-    if (budget_s > 0 && omp_get_wtime() - t_start > budget_s) break;
+    if (max_steps > 0 && step >= max_steps) return step;            // steps run
+    if (budget_s > 0 && omp_get_wtime() - t_start > budget_s) return step;
   }
   return step + 1;
 }
@@ -942,7 +974,8 @@ int or_field(void* h, const char* name, double* out) {
   Problem& P = *(Problem*)h;
   const std::string f(name);
   const std::vector<double>* v = nullptr;
-  if (f == "T") v = &P.T; else if (f == "tSol") v = &P.tSol; else if (f == "G") v = &P.G;
+  if (f == "band") v = &P.band; else if (f == "sol_dT") v = &P.sol_dT;
+  else if (f == "T") v = &P.T; else if (f == "tSol") v = &P.tSol; else if (f == "G") v = &P.G;
   else if (f == "V") v = &P.V; else if (f == "Gx") v = &P.Gx; else if (f == "Gy") v = &P.Gy;
   else if (f == "Gz") v = &P.Gz; else if (f == "dTdt") v = &P.dTdt; else if (f == "eqFrac") v = &P.eqFrac;
   else if (f == "depth") {
@@ -964,5 +997,27 @@ int or_field(void* h, const char* name, double* out) {
 int64_t or_pairs(void* h) { return ((Problem*)h)->pairs.load(); }
 
 void or_solid_fields(void* h, int64_t p, double tsol, double* out) { solid_fields(*(Problem*)h, (long)p, tsol, out); }
+
+void or_solid_fields_many(void* h, const int64_t* pts, const double* tsol, int64_t n, double* out, int threads) {
+  Problem& P = *(Problem*)h;
+  if (threads <= 0) threads = omp_get_max_threads();
+  #pragma omp parallel for num_threads(threads) schedule(dynamic, 16)
+  for (int64_t i = 0; i < n; ++i) solid_fields(P, (long)pts[i], tsol[i], out + 10 * i);
+}
+
+uint64_t or_schedule(void* h, double t, int is_sol) {
+  Problem& P = *(Problem*)h;
+  Nodes N;
+  uint64_t sig = 1469598103934665603ull;
+  gauss_nodes(P, t, is_sol != 0, N, &sig);
+  sig_mix(&sig, (uint64_t)N.size());
+  return sig;
+}
+
+void or_schedule_many(void* h, const double* t, int64_t n, int is_sol, uint64_t* out, int threads) {
+  if (threads <= 0) threads = omp_get_max_threads();
+  #pragma omp parallel for num_threads(threads) schedule(dynamic, 16)
+  for (int64_t i = 0; i < n; ++i) out[i] = or_schedule(h, t[i], is_sol);
+}
 
 }  // extern "C"

@@ -42,7 +42,7 @@ void  or_calc_T(void* h, double t, const int64_t* pts, int64_t n, double* T, int
 void  or_snapshot(void* h, int idx, double* T, int threads);
 
 /* Full solidification run (Solidify_NoTracking / _Volume / _Surface).  max_steps<=0: until
- * the reference's finish test.  Returns the number of steps taken. */
+ * the reference's finish test.  Returns the number of steps run. */
 int64_t or_solidify(void* h, int threads, int64_t max_steps);
 
 /* The same, also stopping after the first step that ends more than budget_s seconds of wall
@@ -50,12 +50,24 @@ int64_t or_solidify(void* h, int threads, int64_t max_steps);
 int64_t or_solidify_budget(void* h, int threads, int64_t max_steps, double budget_s);
 
 /* Per-point field after or_solidify: "T", "tSol", "G", "V", "Gx", "Gy", "Gz", "dTdt",
- * "eqFrac", "numMelt", "depth", "output_flag".  Returns 0 on success. */
+ * "eqFrac", "numMelt", "depth", "output_flag"; and for the tests' explanations "band" (the
+ * closest approach of an evaluated T to T_L, DBL_MAX if never evaluated) and "sol_dT" (T -
+ * T_last of the latest solidification's secant, 0 if none).  Returns 0 on success. */
 int   or_field(void* h, const char* name, double* out);
 
 /* G, Gx/G, Gy/G, Gz/G, dT/dt, V, eqFrac of point p for a solidification time tsol
- * (the second half of Grid::Solidify), into out[0..6]. */
+ * (the second half of Grid::Solidify), into out[0..6]; then the cooling rate before its
+ * integer truncation, the magnitude of its terms and the magnitude of the gradient's terms
+ * (out[7..9]: how well the fields are conditioned). */
 void  or_solid_fields(void* h, int64_t p, double tsol, double* out);
+/* The same for n points, out[10 * i ...]. */
+void  or_solid_fields_many(void* h, const int64_t* pts, const double* tsol, int64_t n, double* out, int threads);
+
+/* Signature (64-bit hash) of the discrete choices of the quadrature walk at t: segments,
+ * interval cuts, step-cap doublings, Gauss orders and kept nodes.  Equal signatures at two
+ * times mean the node lists are the same continuous function of t between them. */
+uint64_t or_schedule(void* h, double t, int is_sol);
+void  or_schedule_many(void* h, const double* t, int64_t n, int is_sol, uint64_t* out, int threads);
 
 /* Point x node pairs evaluated since load (temperature sums + gradient sums). */
 int64_t or_pairs(void* h);

@@ -34,6 +34,10 @@ def load():
         L.or_solidify_budget.restype = ctypes.c_int64
         L.or_field.argtypes = [vp, ctypes.c_char_p, vp]
         L.or_solid_fields.argtypes = [vp, ctypes.c_int64, ctypes.c_double, vp]
+        L.or_solid_fields_many.argtypes = [vp, vp, vp, ctypes.c_int64, vp, ctypes.c_int]
+        L.or_schedule.argtypes = [vp, ctypes.c_double, ctypes.c_int]
+        L.or_schedule.restype = ctypes.c_uint64
+        L.or_schedule_many.argtypes = [vp, vp, ctypes.c_int64, ctypes.c_int, vp, ctypes.c_int]
         L.or_pairs.argtypes = [vp]
         L.or_pairs.restype = ctypes.c_int64
         _lib = L
@@ -95,10 +99,31 @@ class Oracle:
             raise KeyError(name)
         return out
 
+    SOLID = ("G", "Gx", "Gy", "Gz", "dTdt", "V", "eqFrac", "dTdt_raw", "dTdt_mag", "G_mag")
+
     def solid_fields(self, p, tsol):
-        out = np.zeros(8)
+        out = np.zeros(10)
         _lib.or_solid_fields(self.h, int(p), float(tsol), out.ctypes.data_as(ctypes.c_void_p))
-        return dict(zip(("G", "Gx", "Gy", "Gz", "dTdt", "V", "eqFrac"), out[:7]))
+        return dict(zip(self.SOLID, out))
+
+    def solid_fields_many(self, pts, tsol, threads=0):
+        """The fields of Grid::Solidify at each point's given solidification time: a dict of
+        arrays (G ... eqFrac, then dTdt_raw = a lap + dT_t before its truncation, and the
+        magnitudes dTdt_mag, G_mag of the terms the cooling rate and the gradient sum)."""
+        p = np.ascontiguousarray(pts, dtype=np.int64)
+        t = np.ascontiguousarray(tsol, dtype=np.float64)
+        out = np.zeros((p.size, 10))
+        _lib.or_solid_fields_many(self.h, p.ctypes.data_as(ctypes.c_void_p), t.ctypes.data_as(ctypes.c_void_p),
+                                  p.size, out.ctypes.data_as(ctypes.c_void_p), threads)
+        return {f: out[:, i].copy() for i, f in enumerate(self.SOLID)}
+
+    def schedule(self, t, is_sol=False, threads=0):
+        """Signature of the quadrature walk's discrete choices at each time in t."""
+        tt = np.ascontiguousarray(np.atleast_1d(t), dtype=np.float64)
+        out = np.zeros(tt.size, dtype=np.uint64)
+        _lib.or_schedule_many(self.h, tt.ctypes.data_as(ctypes.c_void_p), tt.size, int(is_sol),
+                              out.ctypes.data_as(ctypes.c_void_p), threads)
+        return out
 
     @property
     def pairs(self):
