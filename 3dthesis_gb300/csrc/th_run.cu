@@ -28,6 +28,7 @@ enum { F_T, F_TSOL, F_G, F_V, F_GX, F_GY, F_GZ, F_DTDT, F_EQ, F_NUMMELT, F_DEPTH
 constexpr int kWindowTrack = 256;     // steps per node window (tracking)
 constexpr int kWindowNoTrack = 32;    // steps per node window (NoTracking: whole grid per step)
 constexpr int kRecCap = 1 << 22;      // solidification records per buffer
+constexpr int kRedoListCap = 4096;    // nodes of each FP64 redo block's scratch list (longer lists: warp path)
 
 struct Window {
   void* mem = nullptr;
@@ -160,6 +161,26 @@ th_status init_run(th_ctx* ctx) {
   S.rec_cap = kRecCap;
   ALLOC(r->rec[0], (size_t)kRecCap, 0);
   ALLOC(r->rec[1], (size_t)kRecCap, 0);
+  if (ctx->precision == TH_FP32_KAHAN) {       // the FP64 redo of FP32 solidification: queue, scratch lists
+    ALLOC(S.redo, (size_t)kRecCap, 0);
+    ALLOC(S.redo_n, 1, 0);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    S.redo_blocks = std::max(1, sms);
+    S.redo_cap = kRedoListCap;
+    const size_t cap = (size_t)S.redo_blocks * S.redo_cap;
+    double* d = nullptr;
+    ALLOC(d, cap * 13, 0);                      // 8 double and 10 float fields per node
+    float* f = (float*)(d + 8 * cap);
+    NodeBufView& nb = S.redo_nb;
+    nb.cap = (int)cap;
+    nb.x = d; nb.y = d + cap; nb.z = d + 2 * cap; nb.ipx = d + 3 * cap; nb.ipy = d + 4 * cap; nb.ipz = d + 5 * cap;
+    nb.dtau = d + 6 * cap; nb.amp = d + 7 * cap;
+    nb.kx = f; nb.ky = f + cap; nb.kz = f + 2 * cap; nb.w = f + 3 * cap; nb.xh = f + 4 * cap; nb.xl = f + 5 * cap;
+    nb.yh = f + 6 * cap; nb.yl = f + 7 * cap; nb.zh = f + 8 * cap; nb.zl = f + 9 * cap;
+    ALLOC(S.redo_aux, 2 * (size_t)S.redo_blocks, 0);
+  }
   ALLOC(S.C, 1, 0);
   ALLOC(S.err, 1, 0);
 #undef ALLOC
@@ -331,7 +352,8 @@ th_status solidify_buffer(th_ctx* ctx, RunState* r, int b, int nrec, cudaStream_
   r->sol_timed[b] = false;
   cudaEventRecord(r->ev_sol[b][0], s);
   if (nrec > 0) {
-    th_launch_solidify(ctx->dp, r->S, r->rec[b], std::min(nrec, r->S.rec_cap), ctx->precision, ctx->hp.do_sol, s);
+    th_launch_solidify(ctx->dp, r->S, r->win[b].W, r->rec[b], std::min(nrec, r->S.rec_cap), ctx->precision,
+                       ctx->hp.do_sol, s);
     th_status st = th_cuda_check(ctx, cudaGetLastError(), "solidify");
     if (st != TH_OK) return st;
   }
@@ -572,20 +594,20 @@ th_status th_run_stats(th_ctx* ctx, double* out, int32_t n) {
   unsigned long long pairs[2] = {0, 0};
   th_status st = th_cuda_check(ctx, cudaMemcpy(pairs, ctx->d_pairs, sizeof(pairs), cudaMemcpyDeviceToHost), "cudaMemcpy");
   if (st != TH_OK) return st;
-  unsigned long long prof[18] = {};
+  unsigned long long prof[19] = {};     // the loop profile, then the FP64 redo count
   if (r && r->S.C) {
     st = th_cuda_check(ctx, cudaMemcpy(prof, r->S.C->prof, sizeof(prof), cudaMemcpyDeviceToHost), "cudaMemcpy");
     if (st != TH_OK) return st;
   }
-  const double v[29] = {r ? r->ms_nodes : 0, r ? r->ms_track : 0, r ? r->ms_solid : 0, r ? (double)r->windows : 0,
+  const double v[30] = {r ? r->ms_nodes : 0, r ? r->ms_track : 0, r ? r->ms_solid : 0, r ? (double)r->windows : 0,
                         r ? (double)r->records : 0, r ? (double)r->max_items : 0, r ? (double)r->k : 0,
                         r ? (double)r->slot_cap : 0, r ? r->ms_device : 0, (double)pairs[1],
                         (double)pairs[0], prof[0] * 1e-6, prof[1] * 1e-6, (double)prof[2], (double)prof[3],
                         (double)prof[4], (double)prof[5], (double)prof[6], (double)prof[7], (double)prof[8],
                         prof[10] * 1e-6, prof[11] * 1e-6, prof[12] * 1e-6, prof[13] * 1e-6,
                         prof[14] * 1e-6, prof[15] * 1e-6, prof[16] * 1e-6, prof[17] * 1e-6,
-                        (double)prof[9]};
-  for (int i = 0; i < n && i < 29; ++i) out[i] = v[i];
+                        (double)prof[9], (double)prof[18]};
+  for (int i = 0; i < n && i < 30; ++i) out[i] = v[i];
   return TH_OK;
 }
 

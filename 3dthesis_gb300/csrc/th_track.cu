@@ -141,6 +141,30 @@ __device__ __forceinline__ void df_add_lazy(float& hi, float& lo, float bh, floa
   hi = s;
 }
 
+// The FP32 form takes the liquid decision (T >= T_L) on its own sum except within kGuardK of
+// T_L.  There the point's sum is taken again in FP64 from the node window's FP64 fields and
+// decides, exactly as the FP64 form decides: the FP32 sum's error (about 1.4e-7 of T - T_0,
+// 2e-4 K at the liquidus of the benchmark decks) is far inside the band, so the molten-point
+// set, and with it every later claim and evaluation, is the FP64 form's.
+constexpr float kGuardK = 0.01f;
+
+// FP64 sum of one point over a list's first nn nodes in global memory (the fields of a
+// SlotRef: x y z 1/phix 1/phiy 1/phiz dtau amp, `stride` apart), the lanes splitting the
+// nodes as the FP64 tracking pass does; every lane returns the sum.  Warp-collective.
+__device__ __noinline__ double warp_sum_fp64_global(const double* d, int stride, int nn, double x, double y, double z) {
+  const int lane = threadIdx.x & 31;
+  double s = 0.0;
+  for (int n = lane; n < nn; n += 32) {
+    const double dx = x - __ldg(d + n), dy = y - __ldg(d + stride + n), dz = z - __ldg(d + 2 * (size_t)stride + n);
+    const double wa = __ldg(d + 6 * (size_t)stride + n) * __ldg(d + 7 * (size_t)stride + n);
+    s += wa * exp(-3.0 * (dx * dx * __ldg(d + 3 * (size_t)stride + n) + dy * dy * __ldg(d + 4 * (size_t)stride + n) +
+                          dz * dz * __ldg(d + 5 * (size_t)stride + n)));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  return s;
+}
+
 // T at NP points of one grid column (the same i, j; the callers' passes - a point and the
 // layers under it, or a run of layers of a depth walk - always are) from one node list,
 // the 32 lanes of a warp splitting the nodes; every lane returns the same values.  Each node
@@ -289,6 +313,16 @@ __device__ __forceinline__ void warp_T_n(const DevProblem& P, const TrackState& 
       const float d = ((hi[q] - P.tl_df[0]) + (lo[q] - P.tl_df[1])) - P.tl_df[2];
       out[q].liquid = d >= 0.f;
       out[q].T = pack_df(hi[q], lo[q]);
+      if (fabsf(d) < kGuardK) {      // warp-uniform: the butterfly leaves every lane the same pair
+        const unsigned pu = (unsigned)pts[q], c = pu / (unsigned)P.nz;
+        const unsigned pk = pu - c * (unsigned)P.nz, pi = c / (unsigned)P.ny, pj = c - pi * (unsigned)P.ny;
+        const double s = warp_sum_fp64_global(nb.d, nb.stride, nn, coord(P.gx, P.xmin, P.xmax, P.hx, (int)pi),
+                                              coord(P.gy, P.ymin, P.ymax, P.hy, (int)pj),
+                                              coord(P.gz, P.zmin, P.zmax, P.hz, (int)pk));
+        out[q].liquid = P.T0 + s >= P.TL;
+        const float sh = __double2float_rn(s);
+        out[q].T = pack_df(sh, __double2float_rn(s - (double)sh));
+      }
     }
   }
 }
@@ -1251,6 +1285,16 @@ __global__ void __launch_bounds__(256) k_notrack(DevProblem P, TrackState S, Nod
       }
     }
     sum = (double)s - (double)c;
+    // within kGuardK of T_L the liquid decision is taken on the FP64 sum (as in tracking)
+    if (live && fabs(P.T0 + sum - P.TL) < (double)kGuardK) {
+      double s64 = 0.0;
+      for (int n = 0; n < nn; ++n) {
+        const double dx = x - __ldg(nb.x + n), dy = y - __ldg(nb.y + n), dz = z - __ldg(nb.z + n);
+        s64 += __ldg(nb.dtau + n) * __ldg(nb.amp + n) *
+               exp(-3.0 * (dx * dx * __ldg(nb.ipx + n) + dy * dy * __ldg(nb.ipy + n) + dz * dz * __ldg(nb.ipz + n)));
+      }
+      sum = s64;
+    }
   }
   __syncthreads();
   if (live) {
@@ -1283,14 +1327,17 @@ __global__ void k_notrack_finish(DevProblem P, TrackState S, NodeWindow W, int k
 }
 
 // ------------------------------------------------------------------ bulk solidification
-struct PointSums { double T, gx, gy, gz, lap, dtt; };
+// The sums of Grid::Solidify at one point; the FP32 form also returns the magnitudes its
+// gradient and Laplacian terms add up to (sum |seg| (|dpx| + |dpy| + |dpz|) and
+// sum |seg| (dp^2 - dd)), which bound how far FP32 term errors can move the results.
+struct PointSums { double T, gx, gy, gz, lap, dtt, g_mag, lap_mag; };
 
 // Every node of the list at time t, one thread walking the path serially (the same walk as
 // gen_list_warp, nodes in the reference's order, image copies applied node by node).
 template <bool GRAD>
-__device__ void point_sums(const DevProblem& P, double x, double y, double z, double t, bool is_sol, PointSums& o,
+__device__ __forceinline__ void point_sums(const DevProblem& P, double x, double y, double z, double t, bool is_sol, PointSums& o,
                            unsigned long long& pairs, int& err) {
-  o.T = o.gx = o.gy = o.gz = o.lap = o.dtt = 0.0;
+  o.T = o.gx = o.gy = o.gz = o.lap = o.dtt = o.g_mag = o.lap_mag = 0.0;
   auto add = [&](const NodeVal& v) {
     for (int im = 0; im < P.n_images; ++im) {
       double nx = v.x, ny = v.y, nz = v.z;
@@ -1332,18 +1379,73 @@ __device__ void point_sums(const DevProblem& P, double x, double y, double z, do
   }
 }
 
+// The FP64 sums of point_sums by one warp: every lane walks the path (the walk's
+// arithmetic is the same in all lanes) and the lanes share each interval's Gauss nodes,
+// lane l taking node l; the lanes' partial sums are reduced at the end, so every lane
+// returns the sums.  Warp-collective.
+template <bool GRAD>
+__device__ __forceinline__ void point_sums_warp(const DevProblem& P, double x, double y, double z, double t,
+                                                bool is_sol, PointSums& o, unsigned long long& pairs, int& err) {
+  const int lane = threadIdx.x & 31;
+  double s[6] = {0, 0, 0, 0, 0, 0};
+  auto add = [&](const NodeVal& v) {
+    for (int im = 0; im < P.n_images; ++im) {
+      double nx = v.x, ny = v.y, nz = v.z;
+      if (im) {
+        nx = image_coord(P.img[im][0], P.bcx0, P.bcx1, v.x);
+        ny = image_coord(P.img[im][1], P.bcy0, P.bcy1, v.y);
+        nz = image_coord(P.img[im][2], P.bcz0, P.bcz1, v.z);
+      }
+      const double dx = x - nx, dy = y - ny, dz = z - nz;
+      const double phi = v.amp * exp(-3.0 * ((dx * dx * v.ipx) + (dy * dy * v.ipy) + (dz * dz * v.ipz)));
+      const double seg = v.dtau * phi;
+      s[0] += seg;
+      if (GRAD) {
+        const double ddx = -6.0 * v.ipx, ddy = -6.0 * v.ipy, ddz = -6.0 * v.ipz;
+        const double dpx = ddx * dx, dpy = ddy * dy, dpz = ddz * dz;
+        s[1] += seg * dpx; s[2] += seg * dpy; s[3] += seg * dpz;
+        s[4] += seg * (dpx * dpx + dpy * dpy + dpz * dpz + ddx + ddy + ddz);
+        s[5] += (v.dtau == 0) ? phi : 0.0;
+      }
+      ++pairs;
+    }
+  };
+  for (int b = 0; b < P.nbeams; ++b) {
+    const DevBeam B = P.beam[b];
+    const DevSeg* path = P.segs + B.seg_off;
+    Walk W;
+    walk_begin(B, path, t, is_sol, W);
+    NodeVal v;
+    if (lane == 0 && instant_node(P, B, path, W, v)) add(v);
+    int steps = 0;
+    while (W.more) {
+      if (++steps > kMaxWalkSteps) { err |= ERR_WALK_LIMIT; break; }
+      walk_interval(B, path, W);
+      if (lane < W.order && gauss_node(P, B, path, W, W.order - 2 + lane, v)) add(v);
+      walk_advance(W);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 6; ++j)
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) s[j] += __shfl_xor_sync(0xffffffffu, s[j], off);
+  o.T = s[0]; o.gx = s[1]; o.gy = s[2]; o.gz = s[3]; o.lap = s[4]; o.dtt = s[5];
+  o.g_mag = o.lap_mag = 0.0;
+}
+
 // The same sums in the FP32 form: the walk and each node's time, t - t', position and
 // offset from the point stay FP64; the inverse widths, amplitude, exponential and the six
 // sums (Kahan-compensated) are FP32.  The line position uses the segment's reciprocal
 // duration, formed once per interval.
 template <bool GRAD>
-__device__ void point_sums_f32(const DevProblem& P, double x, double y, double z, double t, bool is_sol,
+__device__ __forceinline__ void point_sums_f32(const DevProblem& P, double x, double y, double z, double t, bool is_sol,
                                PointSums& o, unsigned long long& pairs, int& err) {
-  float s[6] = {0, 0, 0, 0, 0, 0}, c[6] = {0, 0, 0, 0, 0, 0};
-  auto kahan = [&](int j, float v) {
-    const float yy = v - c[j], tt = s[j] + yy;
-    c[j] = (tt - s[j]) - yy;
-    s[j] = tt;
+  float s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0, c0 = 0, c1 = 0, c2 = 0, c3 = 0, c4 = 0, c5 = 0;
+  float m_g = 0.f, m_lap = 0.f;             // magnitudes (positive terms: plain sums suffice)
+  auto kahan = [](float& sj, float& cj, float v) {
+    const float yy = v - cj, tt = sj + yy;
+    cj = (tt - sj) - yy;
+    sj = tt;
   };
   auto add = [&](double nx0, double ny0, double nz0, double ct, double qb, double dtau, const DevBeam& B) {
     const float fx = (float)(B.ax2 + ct), fy = (float)(B.ay2 + ct), fz = (float)(B.az2 + ct);
@@ -1361,13 +1463,16 @@ __device__ void point_sums_f32(const DevProblem& P, double x, double y, double z
       const float e = (float)kNeg3Log2e * ((dx * dx * ipx + dy * dy * ipy) + dz * dz * ipz);
       const float phi = amp * ex2_approx(e);
       const float seg = fdt * phi;
-      kahan(0, seg);
+      kahan(s0, c0, seg);
       if (GRAD) {
         const float ddx = -6.f * ipx, ddy = -6.f * ipy, ddz = -6.f * ipz;
         const float dpx = ddx * dx, dpy = ddy * dy, dpz = ddz * dz;
-        kahan(1, seg * dpx); kahan(2, seg * dpy); kahan(3, seg * dpz);
-        kahan(4, seg * (((dpx * dpx + dpy * dpy) + dpz * dpz) + ((ddx + ddy) + ddz)));
-        if (dtau == 0) kahan(5, phi);
+        kahan(s1, c1, seg * dpx); kahan(s2, c2, seg * dpy); kahan(s3, c3, seg * dpz);
+        const float dp2 = (dpx * dpx + dpy * dpy) + dpz * dpz, dd = (ddx + ddy) + ddz;
+        kahan(s4, c4, seg * (dp2 + dd));
+        if (dtau == 0) kahan(s5, c5, phi);
+        m_g += seg * ((fabsf(dpx) + fabsf(dpy)) + fabsf(dpz));
+        m_lap += seg * (dp2 - dd);
       }
       ++pairs;
     }
@@ -1405,12 +1510,14 @@ __device__ void point_sums_f32(const DevProblem& P, double x, double y, double z
       walk_advance(W);
     }
   }
-  o.T = (double)s[0] - (double)c[0];
-  o.gx = (double)s[1] - (double)c[1];
-  o.gy = (double)s[2] - (double)c[2];
-  o.gz = (double)s[3] - (double)c[3];
-  o.lap = (double)s[4] - (double)c[4];
-  o.dtt = (double)s[5] - (double)c[5];
+  o.T = (double)s0 - (double)c0;
+  o.gx = (double)s1 - (double)c1;
+  o.gy = (double)s2 - (double)c2;
+  o.gz = (double)s3 - (double)c3;
+  o.lap = (double)s4 - (double)c4;
+  o.dtt = (double)s5 - (double)c5;
+  o.g_mag = m_g;
+  o.lap_mag = m_lap;
 }
 
 // C int abs() applied to a double (the reference's int abs on doubles, src/Grid.cpp:381,535),
@@ -1427,19 +1534,12 @@ __global__ void k_sol_latest(TrackState S, const SolRec* rec, int nrec) {
   if (i < nrec) atomicMax(&S.sol_step[rec[i].p], rec[i].step);
 }
 
-// Solidification time by the reference's secant step, then gradient, Laplacian and source
-// sums at that time with the refined schedule, and the derived fields (src/Grid.cpp:316-548).
+// The reference's secant step for the solidification time from (t - dt, T1) and (t, T2)
+// (src/Grid.cpp:340-404; with its int abs() the search stops after the first iteration).
 template <int PREC>
-__global__ void __launch_bounds__(128) k_solidify(DevProblem P, TrackState S, const SolRec* rec, int nrec) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nrec) return;
-  const SolRec r = rec[i];
-  if (S.sol_step[r.p] != r.step) return;            // a later record of this point wins
-  double x, y, z;
-  point_xyz(P, r.p, x, y, z);
-  unsigned long long pairs = 0;
-  int err = 0;
-  double T2 = t_decode(S, P, r.T), T1 = t_decode(S, P, r.Tl), t2 = r.t, t1 = rn_sub(r.t, P.dt), tsol = 0.0;
+__device__ __forceinline__ double secant_tsol(const DevProblem& P, double x, double y, double z, double T2, double T1,
+                                              double t, unsigned long long& pairs, int& err) {
+  double t2 = t, t1 = rn_sub(t, P.dt), tsol = 0.0;
   PointSums ps;
   for (int it = 1;; ++it) {
     const double m = rn_div(rn_sub(T2, T1), rn_sub(t2, t1));
@@ -1451,14 +1551,18 @@ __global__ void __launch_bounds__(128) k_solidify(DevProblem P, TrackState S, co
     if ((e < P.sol_tol) || (it >= P.sol_iter)) break;
     if (Tt > P.TL) { t1 = tsol; T1 = Tt; } else { t2 = tsol; T2 = Tt; }
   }
-  if (PREC == 0) point_sums<true>(P, x, y, z, tsol, true, ps, pairs, err);
-  else point_sums_f32<true>(P, x, y, z, tsol, true, ps, pairs, err);
+  return tsol;
+}
+
+// G, the unit gradient, dT/dt (the reference's int abs), V and eqFrac of point p from the
+// gradient sums at tsol (src/Grid.cpp:522-548), stored in the output fields.
+__device__ __forceinline__ void store_fields(const DevProblem& P, const TrackState& S, int p, double tsol,
+                                             const PointSums& ps) {
   const double G = sqrt(ps.gx * ps.gx + ps.gy * ps.gy + ps.gz * ps.gz);
   const double dTdt = int_abs(rn_add(rn_mul(P.a, ps.lap), ps.dtt));
   const double V = dTdt / G;
   const double kPi = 3.14159265358979323846;
   const double eq = 1.0 - exp((-4 * kPi * P.cetN0 / 3) * pow(G * (P.cetn + 1) / (pow(P.ceta * V, 1 / P.cetn)), -3.0));
-  const int p = r.p;
   if (S.tSol) S.tSol[p] = tsol;
   if (S.G) S.G[p] = G;
   if (S.Gx) S.Gx[p] = ps.gx / G;
@@ -1467,9 +1571,188 @@ __global__ void __launch_bounds__(128) k_solidify(DevProblem P, TrackState S, co
   if (S.dTdt) S.dTdt[p] = dTdt;
   if (S.V) S.V[p] = V;
   if (S.eqFrac) S.eqFrac[p] = eq;
+}
+
+// FP32 runs hand a record's solidification to the FP64 redo pass (which takes the secant's
+// two temperatures and every sum in FP64) when FP32 arithmetic could miss the fields'
+// 1e-4 relative accuracy:
+//  - kCondMax: the gradient or cooling-rate terms add up to more than kCondMax times the
+//    result (they cancel); FP32 terms are good to about 1e-6 relative, so the results of the
+//    rest are good to about 3e-5;
+//  - kSecantMinK, kSensMax: the solidification time moves by dt * e / |T2 - T1| for an error
+//    e in either secant temperature (kTempErr (T_L - T_0) for FP32 sums near the liquidus:
+//    2e-4 K on the benchmark decks), and the cooling rate, a sum that cancels by its
+//    condition number c, moves with it roughly in proportion to c.  Records with |T2 - T1|
+//    below kSecantMinK or c * dt * e / |T2 - T1| above kSensMax (seconds) are redone.  The
+//    bound was set on the 500 x 500 x 100 Surface deck: shifting every point's
+//    solidification time by the largest FP32 error leaves the rest within 1.8e-5 relative,
+//    and 1.4 % of the records are redone.
+constexpr double kCondMax = 32.0;
+constexpr double kSecantMinK = 1.0;
+constexpr double kTempErr = 1.5e-7;
+constexpr double kSensMax = 4e-9;
+
+// Solidification time by the reference's secant step, then gradient, Laplacian and source
+// sums at that time with the refined schedule, and the derived fields (src/Grid.cpp:316-548).
+template <int PREC>
+__global__ void __launch_bounds__(128, 4) k_solidify(DevProblem P, TrackState S, const SolRec* rec, int nrec) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nrec) return;
+  const SolRec r = rec[i];
+  if (S.sol_step[r.p] != r.step) return;            // a later record of this point wins
+  double x, y, z;
+  point_xyz(P, r.p, x, y, z);
+  unsigned long long pairs = 0;
+  int err = 0;
+  const double T2 = t_decode(S, P, r.T), T1 = t_decode(S, P, r.Tl);
+  const double tsol = secant_tsol<PREC>(P, x, y, z, T2, T1, r.t, pairs, err);
+  PointSums ps;
+  if (PREC == 0) point_sums<true>(P, x, y, z, tsol, true, ps, pairs, err);
+  else point_sums_f32<true>(P, x, y, z, tsol, true, ps, pairs, err);
+  if (PREC != 0) {
+    const double G = sqrt(ps.gx * ps.gx + ps.gy * ps.gy + ps.gz * ps.gz);
+    const double rate = fabs(rn_add(rn_mul(P.a, ps.lap), ps.dtt));
+    const double mag = P.a * ps.lap_mag + ps.dtt, dT = fabs(T2 - T1);
+    int why = 0;
+    if (!(ps.g_mag <= kCondMax * G) || !(mag <= kCondMax * rate)) why |= 1;
+    if (!(dT >= kSecantMinK) || !(mag * P.dt * kTempErr * (P.TL - P.T0) <= kSensMax * rate * dT)) why |= 2;
+    if (why) {                                      // at most one entry per record: no overflow
+      const int j = atomicAdd(S.redo_n, 1);
+      if (j < S.rec_cap) S.redo[j] = RedoRec{i, why};
+    }
+  }
+  store_fields(P, S, r.p, tsol, ps);
   atomicAdd(S.pairs, pairs);
   atomicAdd(S.pairs + 1, pairs);
   if (err) atomicOr(S.err, err);
+}
+
+// FP64 sums of a point over the first nn nodes of a list, by the whole block (each thread a
+// strided share of the nodes, then a block reduction); every thread returns the sums.
+// `red` holds a block's partial sums (kGenThreads / 32 warps x 6).
+template <bool GRAD>
+__device__ void block_sums(const NodeBufView& nb, int nn, double x, double y, double z, PointSums& o,
+                           double (*red)[6], unsigned long long& pairs) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double s[6] = {0, 0, 0, 0, 0, 0};
+  for (int n = threadIdx.x; n < nn; n += blockDim.x) {
+    const double ipx = nb.ipx[n], ipy = nb.ipy[n], ipz = nb.ipz[n], dtau = nb.dtau[n];
+    const double dx = x - nb.x[n], dy = y - nb.y[n], dz = z - nb.z[n];
+    const double phi = nb.amp[n] * exp(-3.0 * ((dx * dx * ipx) + (dy * dy * ipy) + (dz * dz * ipz)));
+    const double seg = dtau * phi;
+    s[0] += seg;
+    if (GRAD) {
+      const double ddx = -6.0 * ipx, ddy = -6.0 * ipy, ddz = -6.0 * ipz;
+      const double dpx = ddx * dx, dpy = ddy * dy, dpz = ddz * dz;
+      s[1] += seg * dpx; s[2] += seg * dpy; s[3] += seg * dpz;
+      s[4] += seg * (dpx * dpx + dpy * dpy + dpz * dpz + ddx + ddy + ddz);
+      s[5] += (dtau == 0) ? phi : 0.0;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) s[j] += __shfl_xor_sync(0xffffffffu, s[j], off);
+  }
+  __syncthreads();                                  // the previous use of red is over
+  if (lane == 0)
+    for (int j = 0; j < 6; ++j) red[warp][j] = s[j];
+  __syncthreads();
+  double t[6] = {0, 0, 0, 0, 0, 0};
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+    for (int j = 0; j < 6; ++j) t[j] += red[w][j];
+  o.T = t[0]; o.gx = t[1]; o.gy = t[2]; o.gz = t[3]; o.lap = t[4]; o.dtt = t[5];
+  o.g_mag = o.lap_mag = 0.0;
+  pairs += threadIdx.x == 0 ? (unsigned long long)nn : 0ull;
+}
+
+// point_sums_warp kept out of line (the rare path of block_sums_at).
+template <bool GRAD>
+__device__ __noinline__ void point_sums_warp_call(const DevProblem* P, double x, double y, double z, double t,
+                                                  bool is_sol, PointSums* o, unsigned long long* pairs, int* err) {
+  point_sums_warp<GRAD>(*P, x, y, z, t, is_sol, *o, *pairs, *err);
+}
+
+// Sums at time t from a list generated by the block into its scratch buffer; a list longer
+// than the buffer is summed by warp 0 walking the path itself (point_sums_warp) instead.
+template <bool GRAD>
+__device__ void block_sums_at(const DevProblem& P, const TrackState& S, double t, bool is_sol, double x, double y,
+                              double z, PointSums& o, GenShared& sh, double (*red)[6], PointSums& bc,
+                              unsigned long long& pairs, int& err) {
+  NodeBufView nb = S.redo_nb;
+  const size_t off = (size_t)blockIdx.x * S.redo_cap;
+  nb.x += off; nb.y += off; nb.z += off; nb.ipx += off; nb.ipy += off; nb.ipz += off; nb.dtau += off; nb.amp += off;
+  nb.kx += off; nb.ky += off; nb.kz += off; nb.w += off; nb.xh += off; nb.xl += off; nb.yh += off; nb.yl += off;
+  nb.zh += off; nb.zl += off;
+  nb.cap = S.redo_cap;
+  int* cnt = S.redo_aux + 2 * blockIdx.x;
+  if (threadIdx.x == 0) cnt[1] = 0;
+  __syncthreads();
+  gen_list_block(P, t, is_sol, nb, cnt, cnt + 1, sh);
+  __syncthreads();
+  const int n = __ldcg(cnt), e = __ldcg(cnt + 1);
+  err |= e & ERR_WALK_LIMIT;
+  if (!(e & ERR_NODE_CAPACITY) && n <= nb.cap) {
+    block_sums<GRAD>(nb, n, x, y, z, o, red, pairs);
+    return;
+  }
+  if (threadIdx.x < 32) {
+    PointSums w;
+    int e2 = 0;
+    unsigned long long pr = 0;
+    point_sums_warp_call<GRAD>(&P, x, y, z, t, is_sol, &w, &pr, &e2);
+    if (threadIdx.x == 0) { bc = w; pairs += pr; err |= e2; }
+  }
+  __syncthreads();
+  o = bc;
+  __syncthreads();
+}
+
+// The FP64 redo of the records an FP32 pass queued, one thread block per record: T and
+// T_last again in FP64 from the node window's lists of the record's step and the step
+// before it (the lists the tracking loop summed in FP32), the reference's secant, and the
+// gradient sums at the solidification time from a list the block generates, all in FP64;
+// then the fields, overwriting the FP32 pass's values of the record.  The window is intact:
+// a window is rebuilt on the same stream only after its records' solidification.
+__global__ void __launch_bounds__(kGenThreads, 2) k_solidify_redo(DevProblem P, TrackState S, NodeWindow W,
+                                                                  const SolRec* rec) {
+  __shared__ GenShared sh;
+  __shared__ double red[kGenThreads / 32][6];
+  __shared__ PointSums bc;
+  const int n = min(__ldcg(S.redo_n), S.rec_cap);
+  unsigned long long pairs = 0;
+  int err = 0;
+  for (int e = blockIdx.x; e < n; e += gridDim.x) {
+    const SolRec r = rec[S.redo[e].i];
+    double x, y, z;
+    point_xyz(P, r.p, x, y, z);
+    const int slot = r.step - W.base + 1;
+    PointSums ps;
+    block_sums<false>(slot_view(W, slot), min(W.count[slot], W.slot_cap), x, y, z, ps, red, pairs);
+    double T2 = P.T0 + ps.T;
+    block_sums<false>(slot_view(W, slot - 1), min(W.count[slot - 1], W.slot_cap), x, y, z, ps, red, pairs);
+    double T1 = P.T0 + ps.T;
+    // the reference's secant (see secant_tsol), every sum by the block
+    double t2 = r.t, t1 = rn_sub(r.t, P.dt), tsol = 0.0;
+    for (int it = 1;; ++it) {
+      const double m = rn_div(rn_sub(T2, T1), rn_sub(t2, t1));
+      tsol = rn_add(t1, rn_div(rn_sub(P.TL, T1), m));
+      block_sums_at<false>(P, S, tsol, false, x, y, z, ps, sh, red, bc, pairs, err);
+      const double Tt = P.T0 + ps.T;
+      const double e2 = int_abs(rn_sub(1.0, rn_div(Tt, P.TL)));
+      if ((e2 < P.sol_tol) || (it >= P.sol_iter)) break;
+      if (Tt > P.TL) { t1 = tsol; T1 = Tt; } else { t2 = tsol; T2 = Tt; }
+    }
+    block_sums_at<true>(P, S, tsol, true, x, y, z, ps, sh, red, bc, pairs, err);
+    if (threadIdx.x == 0) {
+      store_fields(P, S, r.p, tsol, ps);
+      atomicAdd(&S.C->redo_total, 1ull);
+    }
+  }
+  if (threadIdx.x == 0) {
+    if (pairs) { atomicAdd(S.pairs, pairs); atomicAdd(S.pairs + 1, pairs); }
+    if (err) atomicOr(S.err, err);
+  }
 }
 
 // field ids for k_final_field
@@ -1574,13 +1857,20 @@ void th_launch_notrack_step(const DevProblem& P, const TrackState& S, const Node
   k_notrack_finish<<<1, 1, 0, s>>>(P, S, w, k);
 }
 
-void th_launch_solidify(const DevProblem& P, const TrackState& S, const SolRec* rec, int nrec, int precision,
-                        bool do_sol, cudaStream_t s) {
+void th_launch_solidify(const DevProblem& P, const TrackState& S, const NodeWindow& w, const SolRec* rec, int nrec,
+                        int precision, bool do_sol, cudaStream_t s) {
   if (nrec <= 0) return;
   k_sol_latest<<<(nrec + 255) / 256, 256, 0, s>>>(S, rec, nrec);
   if (!do_sol) return;
-  if (precision == 0) k_solidify<0><<<(nrec + 127) / 128, 128, 0, s>>>(P, S, rec, nrec);
-  else k_solidify<1><<<(nrec + 127) / 128, 128, 0, s>>>(P, S, rec, nrec);
+  if (precision == 0) {
+    k_solidify<0><<<(nrec + 127) / 128, 128, 0, s>>>(P, S, rec, nrec);
+    return;
+  }
+  k_solidify<1><<<(nrec + 127) / 128, 128, 0, s>>>(P, S, rec, nrec);
+  // one to five percent of the records are redone, a block each: a persistent pass over the
+  // queue, then the queue is emptied
+  k_solidify_redo<<<S.redo_blocks, kGenThreads, 0, s>>>(P, S, w, rec);
+  cudaMemsetAsync(S.redo_n, 0, sizeof(int), s);
 }
 
 void th_launch_final_field(const DevProblem& P, const TrackState& S, int field, double* out, cudaStream_t s) {

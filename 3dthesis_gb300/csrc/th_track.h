@@ -18,6 +18,14 @@ struct SolRec {
   double Tl;       // temperature at the previous step (T_last)
 };
 
+// A record of an FP32 run whose solidification is redone in FP64 (see k_solidify): the
+// record's index, and why (bit 0: the gradient or cooling-rate sum was ill-conditioned for
+// FP32 terms; bit 1: the solidification time was too sensitive to FP32 temperatures).
+struct RedoRec {
+  int32_t i;
+  int32_t why;
+};
+
 // Per-step counters; one struct in device memory.  Lists rotate over three buffers by
 // step (k % 3: this step's liquid list, (k + 1) % 3: the next one, (k + 2) % 3: being
 // cleared), so no buffer is reset while another block may still read it.
@@ -48,6 +56,8 @@ struct alignas(128) TrackCounters {
   // their SM clocks and their nodes summed over warps, [10..13], [14..17] the per-step
   // latest start and end of items of chain depth 0..3 (ns) summed over steps
   unsigned long long prof[18];
+  unsigned long long redo_total;   // FP32 runs: records whose solidification was redone in FP64
+                                   // (read with prof as its 19th word)
   alignas(128) int liq_n[3];     // liquid list lengths
   alignas(128) int rec_n[2];     // solidification records queued in each of the two record buffers
   // once step k is over: (next step's liquid-list length << 34) | (flags << 32) | (k + 1), flags
@@ -76,6 +86,12 @@ struct TrackState {
   SolRec* rec;             // the record buffer this launch appends to
   int* rec_n;              // and its length (one of TrackCounters::rec_n)
   int rec_cap;
+  RedoRec* redo;           // FP32 runs: records queued for the FP64 redo of their solidification
+  int* redo_n;             // (capacity rec_cap; emptied after each redo pass)
+  NodeBufView redo_nb;     // FP32 runs: a scratch node list of redo_cap nodes per redo block
+  int redo_cap;            // (block b's at b * redo_cap), and per block its list's count and
+  int redo_blocks;         // error bits (redo_aux[2 b], redo_aux[2 b + 1])
+  int* redo_aux;
   TrackCounters* C;
   const float2* axis;      // grid coordinates as (hi, lo) floats: x[0, nx), y[nx, nx + ny), z after
   int t_fixed;             // T and the records' T, T_last hold FP32 tracking's fixed point (see t_decode)
@@ -115,9 +131,11 @@ cudaError_t th_launch_track(const DevProblem& P, const TrackState& S, const Node
 void th_launch_notrack_step(const DevProblem& P, const TrackState& S, const NodeWindow& w, int k, int precision,
                             cudaStream_t s);
 
-// Solidification time, gradients and derived fields for nrec records of `rec`.
-void th_launch_solidify(const DevProblem& P, const TrackState& S, const SolRec* rec, int nrec, int precision,
-                        bool do_sol, cudaStream_t s);
+// Solidification time, gradients and derived fields for nrec records of `rec`; `w` is the
+// node window of the records' steps (the FP64 redo of FP32 runs reads the lists of each
+// record's step and of the step before it).
+void th_launch_solidify(const DevProblem& P, const TrackState& S, const NodeWindow& w, const SolRec* rec, int nrec,
+                        int precision, bool do_sol, cudaStream_t s);
 
 // Final per-point field with the reference's liquid markers applied.
 void th_launch_final_field(const DevProblem& P, const TrackState& S, int field, double* out, cudaStream_t s);
