@@ -239,14 +239,14 @@ class Simulation:
 
     def run_stats(self) -> Dict[str, float]:
         """Device time (ms) and counters of the solidification loop so far."""
-        out = np.zeros(30)
-        self._check(self._lib.th_run_stats(self._ctx, _ptr(out), 30))
+        out = np.zeros(31)
+        self._check(self._lib.th_run_stats(self._ctx, _ptr(out), 31))
         keys = ("ms_nodes", "ms_track", "ms_solidify", "windows", "records", "max_items", "steps", "slot_cap",
                 "ms_device", "pairs_solidify", "pairs_total", "loop_ms_work", "loop_ms_barrier", "loop_items",
                 "loop_item_clocks", "loop_wait_clocks", "loop_depth_sum", "loop_steps", "loop_evals",
                 "loop_eval_clocks", "loop_ms_start0", "loop_ms_start1", "loop_ms_start2", "loop_ms_start3",
                 "loop_ms_end0", "loop_ms_end1", "loop_ms_end2", "loop_ms_end3", "loop_eval_nodes",
-                "records_redone_fp64")
+                "records_redone_fp64", "guarded_decisions")
         return dict(zip(keys, out.tolist()))
 
     def field(self, name: str) -> np.ndarray:

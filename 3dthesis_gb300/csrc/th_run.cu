@@ -594,20 +594,20 @@ th_status th_run_stats(th_ctx* ctx, double* out, int32_t n) {
   unsigned long long pairs[2] = {0, 0};
   th_status st = th_cuda_check(ctx, cudaMemcpy(pairs, ctx->d_pairs, sizeof(pairs), cudaMemcpyDeviceToHost), "cudaMemcpy");
   if (st != TH_OK) return st;
-  unsigned long long prof[19] = {};     // the loop profile, then the FP64 redo count
+  unsigned long long prof[20] = {};     // the loop profile, then the FP64 redo and guard counts
   if (r && r->S.C) {
     st = th_cuda_check(ctx, cudaMemcpy(prof, r->S.C->prof, sizeof(prof), cudaMemcpyDeviceToHost), "cudaMemcpy");
     if (st != TH_OK) return st;
   }
-  const double v[30] = {r ? r->ms_nodes : 0, r ? r->ms_track : 0, r ? r->ms_solid : 0, r ? (double)r->windows : 0,
+  const double v[31] = {r ? r->ms_nodes : 0, r ? r->ms_track : 0, r ? r->ms_solid : 0, r ? (double)r->windows : 0,
                         r ? (double)r->records : 0, r ? (double)r->max_items : 0, r ? (double)r->k : 0,
                         r ? (double)r->slot_cap : 0, r ? r->ms_device : 0, (double)pairs[1],
                         (double)pairs[0], prof[0] * 1e-6, prof[1] * 1e-6, (double)prof[2], (double)prof[3],
                         (double)prof[4], (double)prof[5], (double)prof[6], (double)prof[7], (double)prof[8],
                         prof[10] * 1e-6, prof[11] * 1e-6, prof[12] * 1e-6, prof[13] * 1e-6,
                         prof[14] * 1e-6, prof[15] * 1e-6, prof[16] * 1e-6, prof[17] * 1e-6,
-                        (double)prof[9], (double)prof[18]};
-  for (int i = 0; i < n && i < 30; ++i) out[i] = v[i];
+                        (double)prof[9], (double)prof[18], (double)prof[19]};
+  for (int i = 0; i < n && i < 31; ++i) out[i] = v[i];
   return TH_OK;
 }
 

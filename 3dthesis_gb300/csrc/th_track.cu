@@ -141,18 +141,30 @@ __device__ __forceinline__ void df_add_lazy(float& hi, float& lo, float bh, floa
   hi = s;
 }
 
-// The FP32 form takes the liquid decision (T >= T_L) on its own sum except within kGuardK of
-// T_L.  There the point's sum is taken again in FP64 from the node window's FP64 fields and
-// decides, exactly as the FP64 form decides: the FP32 sum's error (about 1.4e-7 of T - T_0,
-// 2e-4 K at the liquidus of the benchmark decks) is far inside the band, so the molten-point
-// set, and with it every later claim and evaluation, is the FP64 form's.
-constexpr float kGuardK = 0.01f;
+// The FP32 form takes the liquid decision (T >= T_L) on its own sum except within
+// kGuardRel (T_L - T_0) of T_L (2 mK on the benchmark decks).  There the point's sum is taken
+// again in FP64 from the node window's FP64 fields and decides, exactly as the FP64 form
+// decides.  The FP32 sums' error stays below 2.2e-7 of T - T_0 (the largest over every
+// evaluated point of the benchmark decks; 1.9e-4 K at their liquidus), seven times inside
+// the band, so the molten-point set, and with it every later claim and evaluation, is the
+// FP64 form's.  The check sits where a decision is used (guard_T), not in the evaluation
+// pass: inside the pass it cost a fifth of the pass's time.  An FP64 pass costs about 20 us
+// on this GPU, so the band is kept narrow: about one decision in 70 timesteps takes it.
+constexpr float kGuardRel = 1.5e-6f;
 
-// FP64 sum of one point over a list's first nn nodes in global memory (the fields of a
+// FP64 sum of grid point p over a list's first nn nodes in global memory (the fields of a
 // SlotRef: x y z 1/phix 1/phiy 1/phiz dtau amp, `stride` apart), the lanes splitting the
-// nodes as the FP64 tracking pass does; every lane returns the sum.  Warp-collective.
-__device__ __noinline__ double warp_sum_fp64_global(const double* d, int stride, int nn, double x, double y, double z) {
+// nodes as the FP64 tracking pass does; every lane returns the sum.  Warp-collective.  The
+// point's FP64 coordinates are formed in here from its index: FP64 instructions are slow on
+// this GPU, and arguments formed at the call site would be computed on every pass.
+__device__ __noinline__ double warp_sum_fp64_point(const double* d, int stride, int nn, unsigned p, unsigned ny,
+                                                   unsigned nz, int gx, int gy, int gz, double xmin, double xmax,
+                                                   double hx, double ymin, double ymax, double hy, double zmin,
+                                                   double zmax, double hz) {
   const int lane = threadIdx.x & 31;
+  const unsigned c = p / nz, pk = p - c * nz, pi = c / ny, pj = c - pi * ny;
+  const double x = coord(gx, xmin, xmax, hx, (int)pi), y = coord(gy, ymin, ymax, hy, (int)pj),
+               z = coord(gz, zmin, zmax, hz, (int)pk);
   double s = 0.0;
   for (int n = lane; n < nn; n += 32) {
     const double dx = x - __ldg(d + n), dy = y - __ldg(d + stride + n), dz = z - __ldg(d + 2 * (size_t)stride + n);
@@ -313,16 +325,6 @@ __device__ __forceinline__ void warp_T_n(const DevProblem& P, const TrackState& 
       const float d = ((hi[q] - P.tl_df[0]) + (lo[q] - P.tl_df[1])) - P.tl_df[2];
       out[q].liquid = d >= 0.f;
       out[q].T = pack_df(hi[q], lo[q]);
-      if (fabsf(d) < kGuardK) {      // warp-uniform: the butterfly leaves every lane the same pair
-        const unsigned pu = (unsigned)pts[q], c = pu / (unsigned)P.nz;
-        const unsigned pk = pu - c * (unsigned)P.nz, pi = c / (unsigned)P.ny, pj = c - pi * (unsigned)P.ny;
-        const double s = warp_sum_fp64_global(nb.d, nb.stride, nn, coord(P.gx, P.xmin, P.xmax, P.hx, (int)pi),
-                                              coord(P.gy, P.ymin, P.ymax, P.hy, (int)pj),
-                                              coord(P.gz, P.zmin, P.zmax, P.hz, (int)pk));
-        out[q].liquid = P.T0 + s >= P.TL;
-        const float sh = __double2float_rn(s);
-        out[q].T = pack_df(sh, __double2float_rn(s - (double)sh));
-      }
     }
   }
 }
@@ -464,6 +466,26 @@ __device__ __forceinline__ void eval_Tn(const DevProblem& P, const TrackState& S
   X.ev_c += clock64() - c0;
   X.ev_n += 1;
   X.ev_nodes += X.nn;
+}
+
+// FP32 runs: an evaluation of point p on this step's list whose sum lies within the guard band of
+// T_L takes its liquid decision, and its T, from the FP64 sum instead.  Warp-collective (T
+// is the same in every lane); called before the decision is used or stored.
+template <int PREC>
+__device__ __forceinline__ void guard_T(const DevProblem& P, const TrackState& S, const StepCtx& X, EvalT& T, int p) {
+  if (PREC == 0) return;
+  const unsigned long long b = (unsigned long long)__double_as_longlong(T.T);
+  const float hi = __uint_as_float((unsigned)(b >> 32)), lo = __uint_as_float((unsigned)b);
+  const float d = ((hi - P.tl_df[0]) + (lo - P.tl_df[1])) - P.tl_df[2];
+  if (fabsf(d) < kGuardRel * P.tl_df[0]) {
+    const double s = warp_sum_fp64_point(X.nb.d, X.nb.stride, X.nn, (unsigned)p, (unsigned)P.ny, (unsigned)P.nz,
+                                         P.gx, P.gy, P.gz, P.xmin, P.xmax, P.hx, P.ymin, P.ymax, P.hy, P.zmin,
+                                         P.zmax, P.hz);
+    T.liquid = P.T0 + s >= P.TL;
+    const float sh = __double2float_rn(s);
+    T.T = pack_df(sh, __double2float_rn(s - (double)sh));
+    if ((threadIdx.x & 31) == 0) atomicAdd(&S.C->guard_total, 1ull);
+  }
 }
 
 // A claimed neighbour the warp keeps instead of publishing it (Volume tracking): it runs in
@@ -792,7 +814,8 @@ __device__ int depth_walk(const DevProblem& P, const TrackState& S, const StepCt
 #pragma unroll
       for (int q = 0; q < NB; ++q) Tc[q] = tmp[q];
     }
-    const EvalT T = pick4(Tc, d - cb);
+    EvalT T = pick4(Tc, d - cb);
+    guard_T<PREC>(P, S, X, T, top - d);
     pairs += X.nn;
     if (lane == 0) set_T(S, top - d, T, X.k);
     if (!T.liquid) break;
@@ -827,7 +850,8 @@ __device__ int depth_walk(const DevProblem& P, const TrackState& S, const StepCt
     }
     const int q = top - d;
     const double Told = ldcg_d(S.T + q);
-    const EvalT T = pick4(Tu, ub - d);
+    EvalT T = pick4(Tu, ub - d);
+    guard_T<PREC>(P, S, X, T, q);
     pairs += X.nn;
     if (lane == 0) set_T(S, q, T, X.k);
     if (!T.liquid) {
@@ -870,7 +894,8 @@ __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx&
   int nchild = 0;
   const double Told = ldcg_d(S.T + p);
   if (type == IT_COLUMN) {                 // a layer under a surface point that solidified
-    const EvalT T = eval_T<PREC>(P, S, X, X.nb, X.nn, p, X.st);
+    EvalT T = eval_T<PREC>(P, S, X, X.nb, X.nn, p, X.st);
+    guard_T<PREC>(P, S, X, T, p);
     pairs += X.nn;
     if (lane == 0) set_T(S, p, T, X.k);
     double Tl = Told;
@@ -904,7 +929,8 @@ __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx&
   }
   if (SURF && type == IT_RETEST) emit_claimed(S, X, rc, nchild, nullptr);
   if (seed && !__shfl_sync(0xffffffffu, got, 0)) return 0;
-  const EvalT T = T3[0];
+  EvalT T = T3[0];
+  guard_T<PREC>(P, S, X, T, p);
   pairs += X.nn;
   if (lane == 0) set_T(S, p, T, X.k);
   if (T.liquid) {
@@ -1285,8 +1311,8 @@ __global__ void __launch_bounds__(256) k_notrack(DevProblem P, TrackState S, Nod
       }
     }
     sum = (double)s - (double)c;
-    // within kGuardK of T_L the liquid decision is taken on the FP64 sum (as in tracking)
-    if (live && fabs(P.T0 + sum - P.TL) < (double)kGuardK) {
+    // within the guard band of T_L the liquid decision is taken on the FP64 sum (as in tracking)
+    if (live && fabs(P.T0 + sum - P.TL) < (double)kGuardRel * (P.TL - P.T0)) {
       double s64 = 0.0;
       for (int n = 0; n < nn; ++n) {
         const double dx = x - __ldg(nb.x + n), dy = y - __ldg(nb.y + n), dz = z - __ldg(nb.z + n);

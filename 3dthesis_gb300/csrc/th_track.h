@@ -57,7 +57,8 @@ struct alignas(128) TrackCounters {
   // latest start and end of items of chain depth 0..3 (ns) summed over steps
   unsigned long long prof[18];
   unsigned long long redo_total;   // FP32 runs: records whose solidification was redone in FP64
-                                   // (read with prof as its 19th word)
+  unsigned long long guard_total;  // FP32 runs: liquid decisions taken on an FP64 sum
+                                   // (both read with prof as its 19th and 20th words)
   alignas(128) int liq_n[3];     // liquid list lengths
   alignas(128) int rec_n[2];     // solidification records queued in each of the two record buffers
   // once step k is over: (next step's liquid-list length << 34) | (flags << 32) | (k + 1), flags

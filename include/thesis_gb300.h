@@ -151,8 +151,9 @@ th_status th_run_reset(th_ctx* ctx);
  * longest parent -> child item chain summed over steps, steps profiled, point evaluations
  * and their SM clocks summed over warps, then per chain depth 0, 1, 2, >= 3 the latest
  * item start and the latest item end after the step began, in ms summed over steps, the
- * nodes of the evaluation passes summed over passes, and the records of an FP32 run whose
- * solidification was redone in FP64 (30 values). */
+ * nodes of the evaluation passes summed over passes, the records of an FP32 run whose
+ * solidification was redone in FP64, and the liquid decisions of an FP32 run taken on an
+ * FP64 sum (31 values). */
 th_status th_run_stats(th_ctx* ctx, double* out, int32_t n);
 
 /* Whole run as the reference CLI does it: the mode loop, then the CSV files under

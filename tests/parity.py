@@ -5,8 +5,8 @@ Every difference is either within its stated tolerance or named by the reason it
 allowed; nothing is absorbed by a percentage.
 
 * The molten-point set, the set of evaluated points, numMelt and the number of steps are
-  identical.  The FP32 form takes each liquid decision within 0.01 K of T_L on an FP64 sum,
-  so its decisions are the FP64 form's, and the FP64 form's are the oracle's.
+  identical.  The FP32 form takes each liquid decision within 1.5e-6 (T_L - T_0) of T_L on an
+  FP64 sum, so its decisions are the FP64 form's, and the FP64 form's are the oracle's.
 * T (at each point's last evaluation, the same step in both runs) within ``T_tol`` K.
 * tSol within the secant's own sensitivity to its temperatures: the reference's secant
   (src/Grid.cpp:366-401) puts t_sol on the line through (t - dt, T_last) and (t, T), so
