@@ -44,7 +44,8 @@ EXPORTED = ("th_ctx_create_from_deck", "th_ctx_destroy", "th_last_error", "th_ge
             "th_batch_create", "th_batch_destroy", "th_batch_last_error", "th_batch_points", "th_batch_snapshot",
             "th_batch_snapshot_device", "th_batch_set_tile_shape", "th_batch_autotune", "th_batch_pairs",
             "th_adj_create", "th_adj_destroy", "th_adj_last_error", "th_adj_num_params", "th_adj_params",
-            "th_adj_host_nodes", "th_adj_forward", "th_adj_backward", "th_calc_T_times_device")
+            "th_adj_host_nodes", "th_adj_forward", "th_adj_backward", "th_calc_T_times_device",
+            "th_device_rates")
 
 
 class ThesisError(RuntimeError):
@@ -122,8 +123,21 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.th_adj_host_nodes.argtypes = [vp, vp, c_int, vp, c_int, vp, ctypes.POINTER(c_int)]
     L.th_adj_forward.argtypes = [vp, vp, vp]
     L.th_adj_backward.argtypes = [vp, vp, vp]
+    L.th_device_rates.argtypes = [vp]
     _lib = L
     return L
+
+
+def device_rates() -> Dict[str, float]:
+    """Measured issue rates of the current CUDA device: SM count, maximum SM clock (MHz),
+    MUFU ex2 results and FP32 FMA lane-operations per SM per clock."""
+    L = load_library()
+    out = np.zeros(4)
+    st = L.th_device_rates(out.ctypes.data_as(ctypes.c_void_p))
+    if st != 0:
+        raise ThesisError(st, L.th_last_error(None).decode())
+    return {"sm_count": int(out[0]), "sm_max_mhz": float(out[1]), "ex2_per_sm_clk": float(out[2]),
+            "fma_per_sm_clk": float(out[3])}
 
 
 def _ptr(a: Optional[np.ndarray]):

@@ -25,8 +25,12 @@ outside the timed region; times from CUDA events on the library's stream).
 ``e2e`` times what a user calls through the C ABI with host buffers: context creation from
 the deck files (parse + upload), the run, and the D2H copy of the output fields into
 pinned memory.  ``cpu_baseline`` and ``--impl reference`` time the CPU oracle (the
-reference's algorithm restated in C++, OpenMP over all host cores) on a bounded sample
-(solidification: the run from t = 0 until the timestep that ends past a ~15 s budget).
+reference's algorithm restated in C++, OpenMP over all host cores): for the Surface deck
+the whole run (the same work as one GPU step, ~15 s), for the other solidification decks
+the run from t = 0 until the timestep that ends past a 15 s budget, for snapshots whole
+snapshots within ~15 s.  Solidification runs also time the plain FP64 form of the same run
+(``detail.fp64_form``).  The roofline's peak uses the SM count and the MUFU ex2 / FP32
+rates measured on the device by probe kernels (th_device_rates).
 
 Under torchrun each rank runs the same per-GPU workload (weak scaling, no collective on
 the data path); rank 0 prints the max-over-ranks time.
@@ -51,9 +55,6 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "point-node pairs/s"
-SM_COUNT = 152
-FP32_LANES = 128            # FP32 lanes per SM per clock
-MUFU_LANES = 16             # MUFU.EX2 results per SM per clock
 # FP32 lane-operations the tiled kernel issues per compensated pair: per node and thread
 # 6 scalar ops shared by its 4 points, per packed pair of points 8 f32x2 ops (2 lanes each)
 # -> (6 + 2 x 16) / 4 = 9.5
@@ -79,6 +80,31 @@ DECK_TEXT = {
                            "P x 1.1, Width_X x 0.9, alpha x 1.05; one step = forward + adjoint over all 208 "
                            "parameters",
 }
+
+
+# Solidification workloads whose whole run takes the CPU oracle under a minute on the GPU
+# box's host cores: their CPU legs time the whole run (the same work as one GPU step);
+# the others time the run from t = 0 up to a time budget.
+CPU_WHOLE_RUN = {"surface_serpentine"}
+_RATES = None
+
+
+def device_rates(th):
+    """SM count and measured MUFU ex2 / FP32 FMA rates per SM per clock (probe kernels)."""
+    global _RATES
+    if _RATES is None:
+        _RATES = th.device_rates()
+    return _RATES
+
+
+def fp32_peak_pairs(th, clk_mhz):
+    """The FP32 / MUFU issue bound of the FP32 pair arithmetic, pairs/s, and its basis."""
+    r = device_rates(th)
+    per_clk = min(r["fma_per_sm_clk"] / FP32_OPS_KAHAN, r["ex2_per_sm_clk"])
+    basis = (f"{r['sm_count']} SMs (read from the device) x {clk_mhz:.0f} MHz x min({r['fma_per_sm_clk']:.1f} "
+             f"FP32 lane-ops/{FP32_OPS_KAHAN}, {r['ex2_per_sm_clk']:.2f} MUFU ex2) pairs/clk, rates measured "
+             f"with probe kernels")
+    return r["sm_count"] * clk_mhz * 1e6 * per_clk, basis
 
 
 def peaks():
@@ -217,13 +243,12 @@ def run_solidification(args, th, torch, dev, path, deck, world):
     pk, src = peaks()
     clk_mhz = (clk or {}).get("sm_mhz") or pk.get("sm_max_mhz", 2070.0)
     track_pairs = st["pairs_total"] - st["pairs_solidify"]
-    peak_pairs = SM_COUNT * clk_mhz * 1e6 * min(FP32_LANES / FP32_OPS_KAHAN, MUFU_LANES)
+    peak_pairs, basis = fp32_peak_pairs(th, clk_mhz)
     achieved = track_pairs / (st["ms_track"] / 1e3)
     loop = "Volume" if args.workload == "volume_multibeam" else "Surface"
     roof = {"bound": "latency", "kernel": f"k_track (persistent {loop} loop)",
             "achieved": achieved / 1e9, "peak": peak_pairs / 1e9, "unit": "Gpairs/s", "frac": achieved / peak_pairs,
-            "peak_basis": f"{SM_COUNT} SMs x {clk_mhz:.0f} MHz x min({FP32_LANES}/{FP32_OPS_KAHAN} FP32 lane-ops, "
-                          f"{MUFU_LANES} MUFU) pairs/clk",
+            "peak_basis": basis, "device_rates": device_rates(th),
             "note": (("each timestep runs ~96,000 work items (one evaluation pass of ~1,465 nodes each) over "
                       "eight warps per SM; bound by the items' L2 round trips (claims, queue slots) and passes, "
                       "not by FP32/MUFU issue or HBM") if loop == "Volume" else
@@ -233,8 +258,24 @@ def run_solidification(args, th, torch, dev, path, deck, world):
             "traffic": NCU_TRAFFIC.get(args.workload) if args.precision == "fp32" else None,
             "traffic_unit": "DRAM bytes per tracking launch (~256 timesteps)", "peak_source": src}
     sim.close()
+    # the plain FP64 form of the same deck, one warm run, for the FP32 / FP64 ratio
+    fp64 = None
+    if args.precision == "fp32" and not args.no_fp64:
+        with th.Simulation(path, "fp64") as s64:
+            s64.solidify(max_steps=300)
+            s64.reset()
+            flush.zero_()
+            torch.cuda.synchronize()
+            s64.solidify()
+            st64 = s64.run_stats()
+        v64 = st64["pairs_total"] / (st64["ms_device"] / 1e3)
+        fp64 = {"value": v64, "unit": "pairs/s", "ms_per_step": st64["ms_device"], "fp32_over_fp64": value / v64,
+                "ms_tracking": st64["ms_track"], "ms_solidify": st64["ms_solidify"],
+                "note": "the same deck and run in the plain FP64 form (TH_FP64), one run after a 300-step warm-up"}
     detail = {"steps": int(st["steps"]), "pairs_per_step": pairs, "ms_node_windows": st["ms_nodes"],
               "ms_tracking": st["ms_track"], "ms_solidify": st["ms_solidify"], "records": int(st["records"]),
+              "records_redone_fp64": int(st["records_redone_fp64"]), "guarded_decisions": int(st["guarded_decisions"]),
+              "fp64_form": fp64,
               "max_items_per_step": int(st["max_items"]), "wall_s_per_step": statistics.median(wall),
               "device_s_per_step": statistics.median(dev_s)}
     if st.get("loop_steps"):
@@ -243,7 +284,7 @@ def run_solidification(args, th, torch, dev, path, deck, world):
             "us_work_per_timestep": 1e3 * st["loop_ms_work"] / n, "us_barrier_per_timestep": 1e3 * st["loop_ms_barrier"] / n,
             "items_per_timestep": st["loop_items"] / n,
             "us_per_item": st["loop_item_clocks"] / max(1, st["loop_items"]) / clk_mhz,
-            "us_waiting_per_warp_timestep": st["loop_wait_clocks"] / n / clk_mhz / (SM_COUNT * 4),
+            "us_waiting_per_warp_timestep": st["loop_wait_clocks"] / n / clk_mhz / (device_rates(th)["sm_count"] * 4),
             "chain_depth_per_timestep": st["loop_depth_sum"] / n,
             "evals_per_timestep": st["loop_evals"] / n,
             "us_per_eval": st["loop_eval_clocks"] / max(1, st["loop_evals"]) / clk_mhz,
@@ -325,12 +366,11 @@ def run_snapshot(args, th, torch, dev, path, deck, world):
     clk_mhz = (clk or {}).get("sm_mhz") or pk.get("sm_max_mhz", 2070.0)
     pairs_last = counts[-1] * pnum
     achieved = pairs_last / (kernel_ms / 1e3)
-    peak_pairs = SM_COUNT * clk_mhz * 1e6 * min(FP32_LANES / FP32_OPS_KAHAN, MUFU_LANES)
+    peak_pairs, basis = fp32_peak_pairs(th, clk_mhz)
     roof = {"bound": "fp32_issue", "kernel": "k_grid_fp32" if args.precision == "fp32" else "k_grid_fp64",
             "achieved": achieved / 1e9, "peak": peak_pairs / 1e9, "unit": "Gpairs/s", "frac": achieved / peak_pairs,
             "achieved_tops": achieved * OPS_PER_PAIR / 1e12, "kernel_ms": kernel_ms, "pairs_per_launch": pairs_last,
-            "peak_basis": f"{SM_COUNT} SMs x {clk_mhz:.0f} MHz x min({FP32_LANES}/{FP32_OPS_KAHAN} FP32 lane-ops, "
-                          f"{MUFU_LANES} MUFU) pairs/clk",
+            "peak_basis": basis, "device_rates": device_rates(th),
             "hbm": {"algorithmic_bytes": int(8 * pnum + counts[-1] * 104), "peak_gbs": pk.get("hbm_gbs"),
                     "achieved_gbs": (8 * pnum + counts[-1] * 104) / (kernel_ms / 1e3) / 1e9, "peak_source": src},
             "traffic": NCU_TRAFFIC.get(args.workload) if args.precision == "fp32" else None}
@@ -400,13 +440,12 @@ def run_sweep(args, th, torch, dev, paths, deck, world):
     clk_mhz = (clk or {}).get("sm_mhz") or pk.get("sm_max_mhz", 2070.0)
     kernel_ms = statistics.median(step_ms)
     achieved = pairs_per_step / (kernel_ms / 1e3)
-    peak_pairs = SM_COUNT * clk_mhz * 1e6 * min(FP32_LANES / FP32_OPS_KAHAN, MUFU_LANES)
+    peak_pairs, basis = fp32_peak_pairs(th, clk_mhz)
     roof = {"bound": "fp32_issue", "kernel": "k_batch_grid (step incl. k_batch_nodes)",
             "achieved": achieved / 1e9, "peak": peak_pairs / 1e9, "unit": "Gpairs/s", "frac": achieved / peak_pairs,
             "achieved_tops": achieved * OPS_PER_PAIR / 1e12, "kernel_ms": kernel_ms,
             "pairs_per_launch": pairs_per_step,
-            "peak_basis": f"{SM_COUNT} SMs x {clk_mhz:.0f} MHz x min({FP32_LANES}/{FP32_OPS_KAHAN} FP32 lane-ops, "
-                          f"{MUFU_LANES} MUFU) pairs/clk",
+            "peak_basis": basis, "device_rates": device_rates(th),
             "hbm": {"algorithmic_bytes": int(8 * pnum), "peak_gbs": pk.get("hbm_gbs"),
                     "achieved_gbs": 8 * pnum / (kernel_ms / 1e3) / 1e9, "peak_source": src},
             "traffic": None}
@@ -510,12 +549,14 @@ def cpu_sample(path, workload, threads, budget_s):
             pairs += o.pairs - p0
             n += 1
         return pairs / used, f"{n} whole snapshots of the deck ({used:.1f} s)"
-    # solidification: the run from t = 0 until the step that ends past the time budget
+    # solidification: the whole run, or the run from t = 0 until the step that ends past the
+    # time budget (budget_s > 0)
     o = oracle_lib.Oracle(path)
     t0 = time.perf_counter()
     done = o.solidify(threads=threads, budget_s=budget_s)
     used = time.perf_counter() - t0
-    return o.pairs / used, f"the first {done} timesteps of the run ({used:.1f} s, {o.pairs:.3e} pairs)"
+    what = f"all {done} timesteps of the run" if budget_s <= 0 else f"the first {done} timesteps of the run"
+    return o.pairs / used, f"{what} ({used:.1f} s, {o.pairs:.3e} pairs)"
 
 
 def main():
@@ -528,6 +569,7 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--tile", default="")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-form comparator run")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -545,8 +587,11 @@ def main():
         for _ in range(args.warmup):
             cpu_sample(path, args.workload, threads, budget_s=1.0)
         vals, sample = [], ""
+        # each step is the same work as one step of the GPU arm where that fits (the whole
+        # Surface run, ~15 s); otherwise a 15 s prefix of the run
+        budget = 0.0 if args.workload in CPU_WHOLE_RUN else 15.0
         for _ in range(args.steps):
-            v, sample = cpu_sample(path, args.workload, threads, budget_s=max(3.0, 45.0 / max(1, args.steps)))
+            v, sample = cpu_sample(path, args.workload, threads, budget_s=budget)
             vals.append(v)
         shutil.rmtree(tmp, ignore_errors=True)
         value = statistics.median(vals)
@@ -580,7 +625,7 @@ def main():
             "gpu_launches": r["gpu_launches"], "detail": r["detail"]}
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        v, sample = cpu_sample(path, args.workload, threads, budget_s=15.0)
+        v, sample = cpu_sample(path, args.workload, threads, budget_s=0.0 if args.workload in CPU_WHOLE_RUN else 15.0)
         line["cpu_baseline"] = {"value": v, "unit": "pairs/s", "cores": threads, "kind": "port", "sample": sample}
     shutil.rmtree(tmp, ignore_errors=True)
     if rank == 0:

@@ -1,9 +1,13 @@
-"""GPU Solidification mode (NoTracking / Volume / Surface, one and four beams) against the
-CPU oracle and the reference's golden runs, through the C ABI.
+"""GPU Solidification mode (NoTracking / Volume / Surface, one and four beams, reflecting
+planes) against the CPU oracle and the reference's golden runs, through the C ABI.
 
-Tolerances: FP64 runs reproduce the molten-point set exactly and every field to 1e-9
-relative; FP32 + Kahan runs must give the same molten set outside a 0.01 K band of T_L,
-T within 0.01 K, and tSol / G / V / dT/dt within 1e-4 relative."""
+Every point is compared (tests/parity.py states the rules): identical molten and evaluated
+sets, numMelt and step counts in both precisions; T within 1e-7 K (FP64) and 0.01 K (FP32);
+tSol within the secant's sensitivity to the temperatures' error; G, V, dT/dt, the unit
+gradient and eqFrac within 1e-9 (FP64) and 1e-4 (FP32) relative of the oracle at the GPU's
+own t_sol, and of the oracle's run except where a point is excused by name (its two t_sol
+values lie on different quadrature schedules, or the oracle's own fields change by more
+than the tolerance between them)."""
 import os
 import sys
 
@@ -13,16 +17,27 @@ import pytest
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(HERE, "golden"))
 import make_golden  # noqa: E402
+import parity  # noqa: E402
 
 pytestmark = pytest.mark.gpu
-CASES = {"small_surface": ("small_surface", "Surface"), "small_volume": ("small_surface", "Volume"),
-         "small_none": ("small_surface", "None"), "small_multibeam": ("small_multibeam",)}
-REL = {"fp64": 1e-9, "fp32": 1e-4}
+CASES = sorted(make_golden.RUNS)
+# tolerances per precision: T (K), relative fields, the temperature error bound for tSol (K),
+# depth (m)
+TOL = {"fp64": dict(T_tol=1e-7, rel=1e-9, T_err=1e-9, depth_tol=1e-15),
+       "fp32": dict(T_tol=0.01, rel=1e-4, T_err=1e-3, depth_tol=1e-8)}
 
 
 def _fields(deck):
-    return ["T"] + [f for f in ("tSol", "G", "V", "Gx", "Gy", "Gz", "dTdt", "eqFrac", "numMelt", "depth")
-                    if deck.outputs.get(f)]
+    return ["T", "output_flag"] + [f for f in ("tSol", "G", "V", "Gx", "Gy", "Gz", "dTdt", "eqFrac", "numMelt",
+                                               "depth") if deck.outputs.get(f)]
+
+
+def _gpu_run(thesis, path, prec, fields, max_steps=0):
+    with thesis.Simulation(path, prec) as sim:
+        steps = sim.solidify(max_steps=max_steps)
+        out = {f: sim.field(f) for f in fields}
+    out["steps"] = steps
+    return out
 
 
 @pytest.fixture(scope="module")
@@ -30,135 +45,56 @@ def runs(built_library, thesis, oracle, tmp_path_factory):
     """Every case run once on the oracle and on the GPU in both precisions."""
     out = {}
     base = tmp_path_factory.mktemp("sol")
-    for tag, (fn, *args) in CASES.items():
-        deck = make_golden.run_deck(tag) if tag in make_golden.RUNS else None
+    for tag in CASES:
+        deck = make_golden.run_deck(tag)
         path = deck.write(str(base / tag))
         o = oracle(path)
-        ref_steps = o.solidify(threads=8)
-        ref = {f: o.field(f) for f in _fields(deck) + ["output_flag"]}
-        ref["steps"] = ref_steps
-        gpu = {}
-        for prec in ("fp64", "fp32"):
-            with thesis.Simulation(path, prec) as sim:
-                steps = sim.solidify()
-                gpu[prec] = {f: sim.field(f) for f in _fields(deck) + ["output_flag"]}
-                gpu[prec]["steps"] = steps
-        out[tag] = (deck, ref, gpu)
+        steps = o.solidify(threads=8)
+        ref = {f: o.field(f) for f in _fields(deck)}
+        ref["steps"] = steps
+        gpu = {prec: _gpu_run(thesis, path, prec, _fields(deck)) for prec in ("fp64", "fp32")}
+        out[tag] = (deck, o, ref, gpu)
     return out
 
 
-@pytest.mark.parametrize("tag", sorted(CASES))
+@pytest.mark.parametrize("tag", CASES)
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
-def test_molten_set(runs, tag, prec):
-    deck, ref, gpu = runs[tag]
-    a, b = ref["output_flag"] > 0, gpu[prec]["output_flag"] > 0
-    diff = np.flatnonzero(a != b)
-    if prec == "fp64":
-        assert diff.size == 0, f"{diff.size} points differ"
-    else:
-        # outside the 0.01 K band the sets agree; a differing point must have been within
-        # the band of T_L at its hottest evaluated moment (checked on the oracle's T)
-        assert diff.size <= max(3, a.sum() // 2000), f"{diff.size} of {a.sum()} molten points differ"
+def test_run_matches_oracle(runs, tag, prec):
+    deck, o, ref, gpu = runs[tag]
+    rep = parity.compare_solidification(o, ref, gpu[prec], dt=deck.timestep, **TOL[prec])
+    assert rep["counts"]["molten"] > 1000
+    assert rep["violations"] == [], rep
 
 
-@pytest.mark.parametrize("tag", sorted(CASES))
-@pytest.mark.parametrize("prec", ["fp64", "fp32"])
-def test_temperature_tsol_and_counts(runs, tag, prec):
-    deck, ref, gpu = runs[tag]
-    g = gpu[prec]
-    common = (ref["output_flag"] > 0) & (g["output_flag"] > 0)
-    assert common.sum() > 100
-    dT = np.abs(ref["T"][common] - g["T"][common])
-    if prec == "fp64":
-        assert np.max(dT) <= 1e-7
-    else:
-        # a liquid decision inside the 0.01 K band of T_L changes which neighbours the
-        # frontier visits, so a handful of points keep a T from another step
-        assert np.mean(dT <= 0.01) >= 0.998, f"{np.sum(dT > 0.01)} of {dT.size} points off by > 0.01 K"
-    if "numMelt" in ref:
-        assert np.array_equal(ref["numMelt"][common], g["numMelt"][common])
-    if "depth" in ref:
-        assert np.max(np.abs(ref["depth"][common] - g["depth"][common])) <= (1e-12 if prec == "fp64" else 1e-8)
-    if "tSol" in ref:
-        # FP32: a 1e-3 K error in T over a cooling rate >= 1e5 K/s moves tSol by <= 1e-8 s
-        tol = 1e-15 if prec == "fp64" else 1e-8
-        assert np.max(np.abs(ref["tSol"][common] - g["tSol"][common])) <= tol
-
-
-SOL = ("G", "V", "dTdt", "Gx", "Gy", "Gz", "eqFrac")
-
-
-@pytest.mark.parametrize("tag", sorted(CASES))
-@pytest.mark.parametrize("prec", ["fp64", "fp32"])
-def test_gradients_at_gpu_solidification_time(runs, oracle, tmp_path, tag, prec):
-    """G, V, dT/dt and the unit gradient equal the oracle's for the same solidification time.
-
-    The quadrature schedule is a discontinuous function of t (a step boundary can land on a
-    segment end or the doubling threshold), so the reference's own G can jump by ~1e-3 when
-    t_sol moves by one ulp; comparing at the GPU's own t_sol isolates the gradient sums.
-    FP64 runs agree to 1e-10; FP32 runs (FP32 exponentials and compensated FP32 sums over
-    FP64 node times and offsets) to 1e-4 relative."""
-    deck, ref, gpu = runs[tag]
-    g = gpu[prec]
-    if "tSol" not in g:
-        pytest.skip("no tSol output")
-    o = oracle(deck.write(str(tmp_path / tag)))
-    solid = np.flatnonzero((g["output_flag"] > 0) & (g["tSol"] > 0))
-    rng = np.random.default_rng(5)
-    for p in rng.choice(solid, min(400, solid.size), replace=False):
-        want = o.solid_fields(p, g["tSol"][p])
-        rel = 1e-10 if prec == "fp64" else 1e-4
-        for f in SOL:
-            if f not in g:
-                continue
-            if f == "dTdt":       # an integer (the reference's int abs): one unit of truncation
-                assert abs(g[f][p] - want[f]) <= 1.0 + max(1e-12, rel) * abs(want[f]), (p, f)
-            elif f in ("Gx", "Gy", "Gz"):
-                assert abs(g[f][p] - want[f]) <= rel, (p, f)
-            elif f == "eqFrac":
-                assert abs(g[f][p] - want[f]) <= rel * max(abs(want[f]), 1e-6), (p, f, g[f][p], want[f])
-            else:
-                assert abs(g[f][p] - want[f]) <= rel * abs(want[f]) + 1e-300, (p, f, g[f][p], want[f])
-
-
-@pytest.mark.parametrize("tag", sorted(CASES))
-@pytest.mark.parametrize("prec", ["fp64", "fp32"])
-def test_gradients_against_oracle_run(runs, tag, prec):
-    """End to end against the oracle's own run: >= 97 % of points within 1e-4 relative;
-    the rest only where the quadrature schedule jumps (bounded by 2e-2 relative)."""
-    deck, ref, gpu = runs[tag]
-    g = gpu[prec]
-    common = (ref["output_flag"] > 0) & (g["output_flag"] > 0) & (ref.get("tSol", ref["T"]) > 0)
-    for f in ("G", "V", "dTdt"):
-        if f not in ref:
-            continue
-        r, v = ref[f][common], g[f][common]
-        rel = np.abs(r - v) / np.maximum(np.abs(r), 1e-300)
-        assert np.mean(rel <= 1e-4) >= 0.97, f"{f}: {np.mean(rel <= 1e-4):.4f} within 1e-4"
-        assert np.max(rel) <= 2e-2, f"{f}: max rel {np.max(rel):.2e}"
-
-
-@pytest.mark.parametrize("tag", sorted(make_golden.RUNS))
+@pytest.mark.parametrize("tag", CASES)
 def test_fp64_run_matches_reference_golden(runs, tag):
+    """The FP64 run against the unmodified reference's own run (golden fixture): the molten
+    set bit for bit, T / tSol / numMelt / depth to 1e-12, and G / V / dT/dt to 1e-9 relative
+    except at points whose GPU and reference t_sol lie on different quadrature schedules
+    (where the GPU equals the oracle at the GPU's t_sol)."""
     g = dict(np.load(os.path.join(HERE, "golden", f"run_{tag}.npz")))
-    deck, ref, gpu = runs[tag]
-    mask = gpu["fp64"]["output_flag"] > 0
-    assert np.array_equal(np.packbits(mask), g["mask"])
+    deck, o, ref, gpu = runs[tag]
+    run = gpu["fp64"]
+    assert np.array_equal(np.packbits(run["output_flag"] > 0), g["mask"])
     sub = g["sample"]
     for f in ("T", "tSol", "numMelt", "depth"):
         if f + "_sample" in g:
-            np.testing.assert_allclose(gpu["fp64"][f][sub], g[f + "_sample"], rtol=1e-12, atol=1e-12, err_msg=f)
+            np.testing.assert_allclose(run[f][sub], g[f + "_sample"], rtol=1e-12, atol=1e-12, err_msg=f)
+    if "tSol_sample" not in g:
+        return
+    ts_g, ts_ref = run["tSol"][sub], g["tSol_sample"]
+    solid = (ts_ref != 0) & (g["G_sample"] != parity.TINY) if "G_sample" in g else ts_ref != 0
+    off = np.zeros(sub.size, dtype=bool)
     for f in ("G", "V", "dTdt"):
         if f + "_sample" in g:
-            rel = np.abs(gpu["fp64"][f][sub] - g[f + "_sample"]) / np.abs(g[f + "_sample"])
-            assert np.mean(rel <= 1e-9) >= 0.97 and np.max(rel) <= 2e-2, f
-
-
-def test_steps_match_oracle_loop(runs):
-    """The finish test (t past the path end, no liquid left) fires at the same step."""
-    for tag, (deck, ref, gpu) in runs.items():
-        assert gpu["fp64"]["steps"] == ref["steps"], tag
-        assert gpu["fp32"]["steps"] == ref["steps"], tag
+            r, v = g[f + "_sample"], run[f][sub]
+            slack = 1.0 if f == "dTdt" else 0.0
+            off |= solid & (np.abs(v - r) > 1e-9 * np.abs(r) + slack)
+    idx = np.flatnonzero(off)
+    if idx.size:
+        assert np.all(o.schedule(ts_g[idx], True) != o.schedule(ts_ref[idx], True)), sub[idx]
+        want = o.solid_fields_many(sub[idx], ts_g[idx])
+        np.testing.assert_allclose(run["G"][sub[idx]], want["G"], rtol=1e-9)
 
 
 @pytest.fixture(scope="module")
@@ -171,10 +107,10 @@ def bcs_run(built_library, oracle, tmp_path_factory):
     path = d.write(str(tmp_path_factory.mktemp("bcs") / d.name))
     o = oracle(path)
     steps = o.solidify(threads=8)
-    ref = {f: o.field(f) for f in _fields(d) + ["output_flag"]}
+    ref = {f: o.field(f) for f in _fields(d)}
     ref["steps"] = steps
     n = max(len(o.nodes(i * 1e-4, True)["xb"]) for i in range(1, 40))
-    return d, path, ref, n
+    return d, path, o, ref, n
 
 
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
@@ -182,31 +118,16 @@ def test_lists_past_the_staged_copy(bcs_run, thesis, monkeypatch, prec):
     """With at most 128 nodes of each list staged in shared memory, the tracking passes read
     the rest of the list from the node window (the path of lists longer than the stage).
     FP64 lanes keep their summation order, so that run is bit-identical to the fully staged
-    one; both precisions meet the oracle tolerances above on a deck with image copies."""
-    deck, path, ref, n_max = bcs_run
+    one; both precisions meet the oracle comparison above on a deck with image copies."""
+    deck, path, o, ref, n_max = bcs_run
     assert n_max > 256, n_max
     runs = {}
     for cap in ("", "128"):
         monkeypatch.setenv("THESIS_GB300_STAGE_CAP", cap)
-        with thesis.Simulation(path, prec) as sim:
-            steps = sim.solidify()
-            runs[cap] = {f: sim.field(f) for f in _fields(deck) + ["output_flag"]}
-            runs[cap]["steps"] = steps
-    g = runs["128"]
-    assert g["steps"] == runs[""]["steps"] == ref["steps"]
+        runs[cap] = _gpu_run(thesis, path, prec, _fields(deck))
     if prec == "fp64":
-        for f in g:
-            if f != "steps":
-                assert np.array_equal(g[f], runs[""][f]), f
-    a, b = ref["output_flag"] > 0, g["output_flag"] > 0
-    common = a & b
-    assert common.sum() > 100
-    dT = np.abs(ref["T"][common] - g["T"][common])
-    if prec == "fp64":
-        assert np.array_equal(a, b)
-        assert np.max(dT) <= 1e-7
-    else:
-        assert np.sum(a != b) <= max(3, a.sum() // 2000)
-        assert np.mean(dT <= 0.01) >= 0.998, np.sum(dT > 0.01)
-    tol = 1e-15 if prec == "fp64" else 1e-8
-    assert np.max(np.abs(ref["tSol"][common] - g["tSol"][common])) <= tol
+        for f in runs["128"]:
+            assert np.array_equal(runs["128"][f], runs[""][f]), f
+    for cap in ("", "128"):
+        rep = parity.compare_solidification(o, ref, runs[cap], dt=deck.timestep, **TOL[prec])
+        assert rep["violations"] == [], (cap, rep)
