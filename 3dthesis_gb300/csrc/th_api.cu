@@ -1,6 +1,8 @@
 // C ABI: context life cycle, node lists, temperature evaluation and snapshots.
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -32,11 +34,26 @@ th_status th_cuda_check(th_ctx* ctx, cudaError_t e, const char* what) {
     if (st_ != TH_OK) return st_;                                 \
   } while (0)
 
+// Device allocations of context creation, numbered from 1 per creation.  The test knob
+// THESIS_GB300_FAIL_ALLOC=n makes the n-th one fail as an out-of-memory cudaMalloc would,
+// without allocating, so the failure path of creation can be exercised.
+static thread_local int g_create_allocs = 0;
+
+static cudaError_t create_malloc(void** p, size_t bytes) {
+  ++g_create_allocs;
+  if (const char* env = std::getenv("THESIS_GB300_FAIL_ALLOC"))
+    if (std::atoi(env) == g_create_allocs) { *p = nullptr; return cudaErrorMemoryAllocation; }
+  return cudaMalloc(p, bytes);
+}
+
 static th_status alloc_nodes(th_ctx* ctx, int cap) {
   if (ctx->node_mem) cudaFree(ctx->node_mem);
   ctx->node_mem = nullptr;
   const size_t bytes = (size_t)cap * (8 * sizeof(double) + 10 * sizeof(float));
-  TH_CUDA(ctx, cudaMalloc(&ctx->node_mem, bytes));
+  {
+    const th_status st = th_cuda_check(ctx, create_malloc(&ctx->node_mem, bytes), "cudaMalloc");
+    if (st != TH_OK) return st;
+  }
   double* d = (double*)ctx->node_mem;
   float* f = (float*)(d + 8 * (size_t)cap);
   NodeBufView& nb = ctx->nb;
@@ -98,6 +115,7 @@ th_status th_ctx_create_from_deck(const char* param_input, int32_t precision, th
   *out = nullptr;
   if (precision != TH_FP64 && precision != TH_FP32_KAHAN) return th_fail(nullptr, TH_ERR_INVALID, "unknown precision");
   th_ctx* ctx = new th_ctx();
+  g_create_allocs = 0;
   std::string err;
   if (!th_load_deck(param_input, ctx->hp, err)) {
     delete ctx;
@@ -120,7 +138,8 @@ th_status th_ctx_create_from_deck(const char* param_input, int32_t precision, th
   cudaEventCreate(&ctx->ev0);
   cudaEventCreate(&ctx->ev1);
   const std::vector<DevSeg> segs = th_pack_segments(ctx->hp);
-  if (th_cuda_check(ctx, cudaMalloc(&ctx->d_segs, segs.size() * sizeof(DevSeg)), "cudaMalloc") != TH_OK) return fail(TH_ERR_CUDA);
+  if (th_cuda_check(ctx, create_malloc((void**)&ctx->d_segs, segs.size() * sizeof(DevSeg)), "cudaMalloc") != TH_OK)
+    return fail(TH_ERR_CUDA);
   if (th_cuda_check(ctx, cudaMemcpy(ctx->d_segs, segs.data(), segs.size() * sizeof(DevSeg), cudaMemcpyHostToDevice),
                     "cudaMemcpy") != TH_OK)
     return fail(TH_ERR_CUDA);
@@ -129,9 +148,11 @@ th_status th_ctx_create_from_deck(const char* param_input, int32_t precision, th
     ctx->err = "more boundary images than TH_MAX_IMAGES";
     return fail(TH_ERR_CAPACITY);
   }
-  if (th_cuda_check(ctx, cudaMalloc(&ctx->d_small, 16 * sizeof(int)), "cudaMalloc") != TH_OK) return fail(TH_ERR_CUDA);
+  if (th_cuda_check(ctx, create_malloc((void**)&ctx->d_small, 16 * sizeof(int)), "cudaMalloc") != TH_OK)
+    return fail(TH_ERR_CUDA);
   if (th_cuda_check(ctx, cudaMemset(ctx->d_small, 0, 16 * sizeof(int)), "cudaMemset") != TH_OK) return fail(TH_ERR_CUDA);
-  if (th_cuda_check(ctx, cudaMalloc(&ctx->d_pairs, 2 * sizeof(unsigned long long)), "cudaMalloc") != TH_OK) return fail(TH_ERR_CUDA);
+  if (th_cuda_check(ctx, create_malloc((void**)&ctx->d_pairs, 2 * sizeof(unsigned long long)), "cudaMalloc") != TH_OK)
+    return fail(TH_ERR_CUDA);
   if (th_cuda_check(ctx, cudaMemset(ctx->d_pairs, 0, 2 * sizeof(unsigned long long)), "cudaMemset") != TH_OK) return fail(TH_ERR_CUDA);
   // capacity: 64 nodes per segment per beam and a margin, times the image count; grown on demand
   size_t segs_total = segs.size();

@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -156,9 +157,19 @@ th_status init_run(th_ctx* ctx) {
     // work items of one step: every claimed point and column layer at most once, which
     // in practice stays far below 2 * pnum
     S.queue_cap = (int)std::min<size_t>(2 * n + 4096, ((size_t)1 << 24) - 1);   // fits the step word's fields
+    // test knob of the failure path: a smaller work queue overflows (ERR_QUEUE)
+    if (const char* env = std::getenv("THESIS_GB300_QUEUE_CAP")) {
+      const int v = std::atoi(env);
+      if (v > 0) S.queue_cap = std::min(S.queue_cap, v);
+    }
     ALLOC(S.queue, (size_t)S.queue_cap, 0);
   }
   S.rec_cap = kRecCap;
+  // test knob of the failure path: record buffers this small overflow in one step (ERR_RECORDS)
+  if (const char* env = std::getenv("THESIS_GB300_REC_CAP")) {
+    const int v = std::atoi(env);
+    if (v > 0) S.rec_cap = std::min(S.rec_cap, v);
+  }
   ALLOC(r->rec[0], (size_t)kRecCap, 0);
   ALLOC(r->rec[1], (size_t)kRecCap, 0);
   if (ctx->precision == TH_FP32_KAHAN) {       // the FP64 redo of FP32 solidification: queue, scratch lists
@@ -328,6 +339,10 @@ th_status read_counters(th_ctx* ctx, RunState* r, TrackCounters* h) {
   if (st != TH_OK) return st;
   st = th_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "solidification step");
   if (st != TH_OK) return st;
+  // a capacity overflow first: a lost work item also leaves the step's waits to run out
+  if (err & 32) return th_fail(ctx, TH_ERR_CAPACITY, "solidification record queue overflowed");
+  if (err & 64) return th_fail(ctx, TH_ERR_CAPACITY, "a tracking list overflowed");
+  if (err & 128) return th_fail(ctx, TH_ERR_CAPACITY, "the per-step work queue overflowed");
   if (err & 16) {
     char b[256];
     std::snprintf(b, sizeof(b), "a work-queue wait exceeded its limit (step %d, ticket %d, initial items %d, "
@@ -335,9 +350,6 @@ th_status read_counters(th_ctx* ctx, RunState* r, TrackCounters* h) {
                   h->diag[1], h->diag[2], h->diag[3], h->diag[4], h->diag[5], h->diag[6], h->diag[7], err);
     return th_fail(ctx, TH_ERR_TIMEOUT, b);
   }
-  if (err & 32) return th_fail(ctx, TH_ERR_CAPACITY, "solidification record queue overflowed");
-  if (err & 64) return th_fail(ctx, TH_ERR_CAPACITY, "a tracking list overflowed");
-  if (err & 128) return th_fail(ctx, TH_ERR_CAPACITY, "the per-step work queue overflowed");
   if (err & 2) return th_fail(ctx, TH_ERR_TIMEOUT, "quadrature walk exceeded its step limit");
   return TH_OK;
 }

@@ -375,7 +375,8 @@ __device__ __forceinline__ void set_T(const TrackState& S, int p, const EvalT& e
 }
 
 // Bound on the polls of one wait for work (about 8 s at the longest back-off); past it the
-// waiter latches ERR_BARRIER and releases every warp of the launch.
+// waiter latches ERR_BARRIER and releases every warp of the launch.  The test knob
+// THESIS_GB300_SPIN_LIMIT lowers it.
 constexpr long long kSpinLimit = 1ll << 25;
 
 
@@ -996,9 +997,14 @@ __host__ __device__ __forceinline__ bool axis_in_smem(const DevProblem& P) {
 // item that any warp may take; the step word (entered blocks, published and completed
 // items) tells when the step has no work left, and the step's end is published as one word
 // that the waiting warps poll (no grid barrier).
+//
+// spin_limit bounds every wait (kSpinLimit unless a test lowers it); hold (a test knob, 0
+// otherwise) counts items into every step that are never dealt, so no step can end and the
+// waits run out: the path of a lost item.
 template <int PREC, bool SURF>
 __global__ void __launch_bounds__(track_bound<SURF>(), 1) k_track(DevProblem P, TrackState S, NodeWindow W, int k_begin,
-                                                            int k_end, int high_water, int stage_cap) {
+                                                            int k_end, int high_water, int stage_cap,
+                                                            long long spin_limit, int hold) {
   extern __shared__ __align__(16) unsigned char stage_mem[];
   __shared__ BlockBuf bbuf;
   const int lane = threadIdx.x & 31;
@@ -1131,7 +1137,8 @@ __global__ void __launch_bounds__(track_bound<SURF>(), 1) k_track(DevProblem P, 
         }
         if (arrival_pending) {              // this block's entry, checked once its result is back
           arrival_pending = false;
-          if (step_over(arrival + kArrive, X.n_init, gridDim.x)) finish_step(P, S, X, k, arrival + kArrive, high_water);
+          if (step_over(arrival + kArrive, X.n_init + hold, gridDim.x))
+            finish_step(P, S, X, k, arrival + kArrive, high_water);
         }
         unsigned ticket = 0;
         if (lane == 0) ticket = atomicAdd(&X.qc->head, 1u);
@@ -1154,7 +1161,7 @@ __global__ void __launch_bounds__(track_bound<SURF>(), 1) k_track(DevProblem P, 
           finished = __shfl_sync(0xffffffffu, finished, 0);
           if (ready || finished) break;
           backoff = backoff < 256 ? backoff * 2 : 256;
-          if (++idle > kSpinLimit) {
+          if (++idle > spin_limit) {
             if (lane == 0) {
               if (atomicOr(S.err, ERR_BARRIER) == 0) {        // first waiter to give up records its view
                 const unsigned long long st = ld_relaxed_u64(&X.qc->state);
@@ -1213,7 +1220,7 @@ __global__ void __launch_bounds__(track_bound<SURF>(), 1) k_track(DevProblem P, 
       }
       if (lane == 0) {                                           // completed, after the item's writes
         const unsigned long long st = atom_add_release(&X.qc->state, 1ull);
-        if (step_over(st + 1ull, X.n_init, gridDim.x)) finish_step(P, S, X, k, st + 1ull, high_water);
+        if (step_over(st + 1ull, X.n_init + hold, gridDim.x)) finish_step(P, S, X, k, st + 1ull, high_water);
       }
       ++n_items;
       c_items += clock64() - c1;
@@ -1839,6 +1846,15 @@ static cudaError_t launch_track_t(const DevProblem& P, const TrackState& S, cons
     const int v = std::atoi(env);
     if (v > 0) cap = std::min(cap, v);
   }
+  // test knobs of the failure paths: a shorter bound on every wait, and items that are
+  // counted into each step but never dealt (the step cannot end; its waits run out)
+  long long spin_limit = kSpinLimit;
+  int hold = 0;
+  if (const char* env = std::getenv("THESIS_GB300_SPIN_LIMIT")) {
+    const long long v = std::atoll(env);
+    if (v > 0) spin_limit = std::min(v, kSpinLimit);
+  }
+  if (const char* env = std::getenv("THESIS_GB300_HOLD_ITEMS")) hold = std::max(0, std::atoi(env));
   cap = std::max(kListPad, cap & ~(kListPad - 1));
   const size_t smem = (size_t)3 * cap * staged_bytes_per_node<PREC>() +
                       (axis_in_smem<PREC>(P) ? (size_t)(P.nx + P.ny + P.nz) * sizeof(float2) : 0);
@@ -1861,7 +1877,7 @@ static cudaError_t launch_track_t(const DevProblem& P, const TrackState& S, cons
   DevProblem Pc = P;
   TrackState Sc = S;
   NodeWindow Wc = w;
-  void* args[] = {&Pc, &Sc, &Wc, &k_begin, &k_end, &hw, &cap};
+  void* args[] = {&Pc, &Sc, &Wc, &k_begin, &k_end, &hw, &cap, &spin_limit, &hold};
   return cudaLaunchCooperativeKernel((const void*)k_track<PREC, SURF>, dim3(blocks), dim3(track_threads<SURF>()), args, smem,
                                      s);
 }

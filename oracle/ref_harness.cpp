@@ -7,7 +7,8 @@
  * Entry points call the reference's public interface:
  *   Init::GetFileNames / Init::ReadSimParams (src/Init.h), Grid (src/Grid.h),
  *   Calc::Integrate_Serial (src/Calc.h:23), Grid::Calc_T (src/Grid.h:290),
- *   Run::Simulate (src/Run.h), and the Grid getters (src/Grid.h:299-370).
+ *   Run::Simulate (src/Run.h), Grid::Output (src/Grid.h), and the Grid getters
+ *   (src/Grid.h:299-370).
  */
 #include <cstdint>
 #include <cstring>
@@ -73,6 +74,13 @@ void ref_calc_T(void* h, double t, const int64_t* pts, int64_t n, double* T) {
 void ref_simulate(void* h) {
   RefRun* r = (RefRun*)h;
   Run::Simulate(*r->grid, r->sim);
+}
+
+// The reference's CSV writer for the grid's current state (Grid::Output, src/Grid.cpp:72-99),
+// as bin/Main.cpp:104-108 calls it after a Solidification run: Data/<Name>.<name>.csv.
+void ref_output(void* h, const char* name) {
+  RefRun* r = (RefRun*)h;
+  r->grid->Output(r->sim, name);
 }
 
 int ref_field(void* h, const char* name, double* out) {

@@ -15,6 +15,11 @@ own process (the reference keeps function-static state).  The fixtures hold:
 * ``run_<deck>.npz`` - a full Run::Simulate on a small solidification deck: the packed
   molten-point mask, per-field checksums over all output points, and every output
   field at a seeded subset of 1500 output points.
+* ``csv_<deck>.npz`` - the reference's own output files (Grid::Output) of a whole run of
+  a small Snapshots deck and a small Solidification deck, byte for byte: ``names`` and
+  ``file<i>`` (the file's bytes).
+
+``python tests/golden/make_golden.py csv`` regenerates only the csv fixtures.
 """
 from __future__ import annotations
 
@@ -57,6 +62,16 @@ if "pts" in job:
         L.ref_calc_T(h, ctypes.c_double(t), pts.ctypes.data_as(ctypes.c_void_p), ctypes.c_int64(len(pts)),
                      T.ctypes.data_as(ctypes.c_void_p))
         out[f"t{i}"] = np.float64(t); out[f"T{i}"] = T
+if "csv" in job:
+    import os
+    L.ref_simulate(h)
+    if str(job["csv"]) == "Solidification":
+        L.ref_output(h, b"Solidification.Final")
+    names = sorted(os.listdir("Data"))
+    out["names"] = np.array(names)
+    for i, nm in enumerate(names):
+        with open(os.path.join("Data", nm), "rb") as f:
+            out[f"file{i}"] = np.frombuffer(f.read(), dtype=np.uint8)
 if "fields" in job:
     L.ref_simulate(h)
     for f in job["fields"]:
@@ -113,6 +128,27 @@ RUNS = {"small_surface": ("small_surface", "Surface"), "small_volume": ("small_s
         "small_none": ("small_surface", "None"), "small_multibeam": ("small_multibeam",)}
 
 
+CSV_DECKS = ("csv_snapshot", "small_multibeam")
+
+
+def csv_deck(name):
+    """The deck each csv_<name>.npz fixture was made from."""
+    if name == "csv_snapshot":
+        d = decks.small_snapshot()
+        d.name = "csv_snapshot"
+        d.axes = (decks.AxisSpec(0.0, 0.58e-3, num=30), decks.AxisSpec(-0.05e-3, 0.33e-3, num=20),
+                  decks.AxisSpec(-0.08e-3, 0.0, num=5))
+        return d
+    return getattr(decks, name)()
+
+
+def csv_fixture(deck, scratch):
+    r = run_ref(deck, {"csv": np.asarray(deck.mode)}, scratch)
+    out = {k: v for k, v in r.items() if k == "names" or k.startswith("file")}
+    np.savez_compressed(os.path.join(HERE, f"csv_{deck.name}.npz"), **out)
+    return out
+
+
 def node_deck(name):
     """The deck each nodes_<name>.npz fixture was made from."""
     if name == "small_bcs":
@@ -132,6 +168,12 @@ def run_deck(tag):
 def main():
     if not os.path.exists(REF_LIB):
         sys.exit(f"missing {REF_LIB}: build it with `make -C oracle ref`")
+    if sys.argv[1:] == ["csv"]:
+        with tempfile.TemporaryDirectory() as scratch:
+            for name in CSV_DECKS:
+                csv_fixture(csv_deck(name), scratch)
+        print("csv fixtures written to", HERE)
+        return
     with tempfile.TemporaryDirectory() as scratch:
         for name, times in NODE_TIMES.items():
             node_fixture(node_deck(name), times, scratch)
@@ -141,6 +183,8 @@ def main():
         np.savez_compressed(os.path.join(HERE, "temp_snapshot_raster.npz"), pts=pts, **r)
         for tag in RUNS:
             run_fixture(run_deck(tag), scratch, tag)
+        for name in CSV_DECKS:
+            csv_fixture(csv_deck(name), scratch)
     print("golden fixtures written to", HERE)
 
 
