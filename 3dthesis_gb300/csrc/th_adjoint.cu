@@ -446,6 +446,10 @@ th_status th_adj_create(const char* param_input, int32_t precision, const int64_
   std::string e;
   if (!th_load_deck(param_input, A->hp, e)) { delete A; return afail(nullptr, TH_ERR_INVALID, e); }
   if (A->hp.beams.size() != 1) { delete A; return afail(nullptr, TH_ERR_UNSUPPORTED, "the adjoint takes single-beam decks"); }
+  if (A->hp.compress) {
+    delete A;
+    return afail(nullptr, TH_ERR_UNSUPPORTED, "the adjoint takes decks without path compression");
+  }
   A->precision = precision;
   th_make_dev_problem(A->hp, nullptr, A->dp);
   if (A->dp.n_images > 1) { delete A; return afail(nullptr, TH_ERR_UNSUPPORTED, "the adjoint takes decks without reflections"); }

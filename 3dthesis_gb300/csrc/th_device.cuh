@@ -94,11 +94,18 @@ struct GenShared {
   int m, more, nout, err, kept;
 };
 
-__device__ __forceinline__ void gen_list_block(const DevProblem& P, double t, bool is_sol, const NodeBufView& nb,
-                                               int* count, int* err, GenShared& sh) {
+// The combined intervals' centre and mean power of a chunk (path compression only); the
+// kernels that generate lists take it as dynamic shared memory when the deck compresses.
+struct GenComp {
+  double cx[kChunkIntervals], cy[kChunkIntervals], cq[kChunkIntervals];
+};
+constexpr int kOrdComb = 0x100;        // flag in GenShared::ord: a combined interval
+
+// Every beam's nodes appended to the list (sh.nout counts them, nodes past nb.cap are
+// counted but not stored): the plain walk, or with cs the compressed walk.
+__device__ __forceinline__ void gen_walk_block(const DevProblem& P, double t, bool is_sol, const NodeBufView& nb,
+                                               GenShared& sh, GenComp* cs) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid == 0) { sh.nout = 0; sh.err = 0; }
-  __syncthreads();
   for (int b = 0; b < P.nbeams; ++b) {
     const DevBeam B = P.beam[b];
     const DevSeg* path = P.segs + B.seg_off;
@@ -109,10 +116,13 @@ __device__ __forceinline__ void gen_list_block(const DevProblem& P, double t, bo
       path = sh.seg_cache;
     }
     Walk W;
+    CWalk C;
     if (tid == 0) {
-      walk_begin(B, path, t, is_sol, W);
       NodeVal v;
-      if (instant_node(P, B, path, W, v)) {
+      bool inst;
+      if (cs) { cwalk_begin(B, path, t, is_sol, C); W.t = t; W.s = C.s; inst = instant_node(P, B, path, W, v); }
+      else { walk_begin(B, path, t, is_sol, W); inst = instant_node(P, B, path, W, v); }
+      if (inst) {
         if (sh.nout < nb.cap) store_node(nb, sh.nout, v);
         sh.nout++;
       }
@@ -122,17 +132,35 @@ __device__ __forceinline__ void gen_list_block(const DevProblem& P, double t, bo
       __syncthreads();
       if (tid == 0) {                                  // next chunk of the interval schedule
         int m = 0, off = 0;
-        while (W.more && m < kChunkIntervals) {
-          if (++steps > kMaxWalkSteps) { sh.err |= ERR_WALK_LIMIT; W.more = false; break; }
-          walk_interval(B, path, W);
-          sh.t1[m] = W.t1; sh.t2[m] = W.t2; sh.seg[m] = W.s; sh.ord[m] = W.order; sh.off[m] = off;
-          off += W.order;
-          ++m;
-          walk_advance(W);
+        if (cs) {
+          CInterval I;
+          while (m < kChunkIntervals) {
+            if (++steps > kMaxWalkSteps) { sh.err |= ERR_WALK_LIMIT; C.more = false; break; }
+            int e = 0;
+            const bool got = cwalk_next(P, B, path, C, I, e);
+            sh.err |= e;
+            if (!got) break;
+            sh.t1[m] = I.t1; sh.t2[m] = I.t2; sh.seg[m] = I.s; sh.ord[m] = I.order | (I.comb ? kOrdComb : 0);
+            cs->cx[m] = I.cx; cs->cy[m] = I.cy; cs->cq[m] = I.cq;
+            sh.off[m] = off;
+            off += I.order;
+            ++m;
+            if (!C.more) break;
+          }
+          sh.more = C.more;
+        } else {
+          while (W.more && m < kChunkIntervals) {
+            if (++steps > kMaxWalkSteps) { sh.err |= ERR_WALK_LIMIT; W.more = false; break; }
+            walk_interval(B, path, W);
+            sh.t1[m] = W.t1; sh.t2[m] = W.t2; sh.seg[m] = W.s; sh.ord[m] = W.order; sh.off[m] = off;
+            off += W.order;
+            ++m;
+            walk_advance(W);
+          }
+          sh.more = W.more;
         }
         sh.off[m] = off;
         sh.m = m;
-        sh.more = W.more;
       }
       __syncthreads();
       const int m = sh.m, total = sh.off[m];
@@ -143,10 +171,18 @@ __device__ __forceinline__ void gen_list_block(const DevProblem& P, double t, bo
         if (c < total) {
           int lo = 0, hi = m - 1;                      // interval of candidate c
           while (lo < hi) { const int mid = (lo + hi + 1) >> 1; if (sh.off[mid] <= c) lo = mid; else hi = mid - 1; }
-          const int order = sh.ord[lo], g = c - sh.off[lo];
-          Walk w;
-          w.t = t; w.t1 = sh.t1[lo]; w.t2 = sh.t2[lo]; w.s = sh.seg[lo];
-          keep = gauss_node(P, B, path, w, order - 2 + order - 1 - g, v);
+          const int order = sh.ord[lo] & 0xff, g = c - sh.off[lo];
+          const int k = order - 2 + order - 1 - g;
+          if (sh.ord[lo] & kOrdComb) {
+            CInterval I;
+            I.t1 = sh.t1[lo]; I.t2 = sh.t2[lo]; I.s = sh.seg[lo]; I.order = order; I.comb = true;
+            I.cx = cs->cx[lo]; I.cy = cs->cy[lo]; I.cq = cs->cq[lo];
+            keep = comb_node(P, B, path, I, t, k, g, v);
+          } else {
+            Walk w;
+            w.t = t; w.t1 = sh.t1[lo]; w.t2 = sh.t2[lo]; w.s = sh.seg[lo];
+            keep = gauss_node(P, B, path, w, k, v);
+          }
         }
         const unsigned mk = __ballot_sync(0xffffffffu, keep);
         if (lane == 0) sh.wsum[warp] = __popc(mk);
@@ -165,6 +201,51 @@ __device__ __forceinline__ void gen_list_block(const DevProblem& P, double t, bo
       }
       if (!sh.more) break;
     }
+  }
+}
+
+__device__ __forceinline__ void copy_node(const NodeBufView& nb, int dst, int src) {
+  nb.x[dst] = nb.x[src]; nb.y[dst] = nb.y[src]; nb.z[dst] = nb.z[src];
+  nb.ipx[dst] = nb.ipx[src]; nb.ipy[dst] = nb.ipy[src]; nb.ipz[dst] = nb.ipz[src];
+  nb.dtau[dst] = nb.dtau[src]; nb.amp[dst] = nb.amp[src];
+  nb.kx[dst] = nb.kx[src]; nb.ky[dst] = nb.ky[src]; nb.kz[dst] = nb.kz[src]; nb.w[dst] = nb.w[src];
+  nb.xh[dst] = nb.xh[src]; nb.xl[dst] = nb.xl[src]; nb.yh[dst] = nb.yh[src]; nb.yl[dst] = nb.yl[src];
+  nb.zh[dst] = nb.zh[src]; nb.zl[dst] = nb.zl[src];
+}
+
+// One thread block builds the whole node list at time t (Calc::Integrate_Serial,
+// src/Calc.cpp:48-65).  With path compression (P.compress; cs must then point at the
+// block's GenComp) the list is the compressed walk's, except at a non-solidification time
+// where the plain walk's list is kept when it is not longer (the reference builds both and
+// keeps the smaller, src/Calc.cpp:49-58): both are built, the plain one after the
+// compressed one, so the buffer must hold both (a count above nb.cap reports the need).
+__device__ __forceinline__ void gen_list_block(const DevProblem& P, double t, bool is_sol, const NodeBufView& nb,
+                                               int* count, int* err, GenShared& sh, GenComp* cs = nullptr) {
+  const int tid = threadIdx.x;
+  if (tid == 0) { sh.nout = 0; sh.err = 0; }
+  __syncthreads();
+  if (P.compress && cs) {
+    gen_walk_block(P, t, is_sol, nb, sh, cs);
+    if (!is_sol) {
+      __syncthreads();
+      const int n_c = sh.nout;
+      gen_walk_block(P, t, is_sol, nb, sh, nullptr);
+      __syncthreads();
+      const int n_r = sh.nout - n_c;
+      if (sh.nout <= nb.cap) {
+        if (n_r <= n_c) {                              // keep the plain list: move it down
+          for (int i = tid; i < n_r; i += kGenThreads) copy_node(nb, i, n_c + i);
+          __syncthreads();
+          if (tid == 0) sh.nout = n_r;
+        } else if (tid == 0) {
+          sh.nout = n_c;
+        }
+      }
+      __syncthreads();
+    }
+  } else {
+    if (P.compress && tid == 0) sh.err |= ERR_WALK_LIMIT;   // a compressing deck needs cs
+    gen_walk_block(P, t, is_sol, nb, sh, nullptr);
   }
   __syncthreads();
   const int n0 = sh.nout;

@@ -15,10 +15,12 @@ namespace {
 
 using namespace thdev;
 
+// Dynamic shared memory of the list-generating kernels: a GenComp for compressing decks.
 __global__ void __launch_bounds__(kGenThreads) k_nodes_block(DevProblem P, double t, int is_sol, NodeBufView nb,
                                                              int* count, int* err) {
   __shared__ GenShared sh;
-  gen_list_block(P, t, is_sol != 0, nb, count, err, sh);
+  extern __shared__ __align__(16) unsigned char gen_dyn[];
+  gen_list_block(P, t, is_sol != 0, nb, count, err, sh, P.compress ? (GenComp*)gen_dyn : nullptr);
 }
 
 // ---------------------------------------------------------------- whole-grid sums
@@ -182,8 +184,9 @@ __global__ void __launch_bounds__(kThreads) k_grid_fp64(DevProblem P, NodeBufVie
 __global__ void __launch_bounds__(kGenThreads) k_batch_nodes(const DevProblem* probs, const NodeBufView* views,
                                                              const double* times, int* counts, int* err) {
   __shared__ GenShared sh;
+  extern __shared__ __align__(16) unsigned char gen_dyn[];
   const int d = blockIdx.x;
-  gen_list_block(probs[d], times[d], false, views[d], counts + d, err, sh);
+  gen_list_block(probs[d], times[d], false, views[d], counts + d, err, sh, (GenComp*)gen_dyn);
 }
 
 // ...then a persistent grid drains one work list of (deck, tile) items, taken in order with
@@ -322,7 +325,7 @@ void launch_grid(const DevProblem& P, const NodeBufView& nb, const int* d_count,
 
 void th_launch_nodes(const DevProblem& P, double t, bool is_sol, const NodeBufView& nb, int* d_count, int* d_err,
                      cudaStream_t s) {
-  k_nodes_block<<<1, kGenThreads, 0, s>>>(P, t, is_sol ? 1 : 0, nb, d_count, d_err);
+  k_nodes_block<<<1, kGenThreads, P.compress ? sizeof(GenComp) : 0, s>>>(P, t, is_sol ? 1 : 0, nb, d_count, d_err);
 }
 
 bool th_tile_shape_supported(TileShape sh) {
@@ -356,7 +359,7 @@ int th_tile_count(const DevProblem& P, TileShape sh) {
 
 void th_launch_batch_nodes(int ndeck, const DevProblem* probs, const NodeBufView* views, const double* times,
                            int* counts, int* err, cudaStream_t s) {
-  k_batch_nodes<<<ndeck, kGenThreads, 0, s>>>(probs, views, times, counts, err);
+  k_batch_nodes<<<ndeck, kGenThreads, sizeof(GenComp), s>>>(probs, views, times, counts, err);
 }
 
 template <int KP, int KCH>

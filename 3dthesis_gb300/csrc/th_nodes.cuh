@@ -157,6 +157,174 @@ __device__ __forceinline__ bool instant_node(const DevProblem& P, const DevBeam&
   return true;
 }
 
+// ---------------------------------------------------------------- path compression
+// The walk of Calc::GaussCompressIntegrate (src/Calc.cpp:213-501): like the plain walk,
+// except that where an interval would reach into the previous segment, the segments whose
+// end points lie within the heat's diffusion distance r of the beam position at t2
+// (r^2 = ln2/8 ax^2 (12 a (t - t2) / ax^2 + 1)) and whose power matches are combined into
+// one interval whose Gauss nodes all sit at the power-and-time weighted centre of the
+// combined stretch, with its mean power.  Restated in the reference's operation order; the
+// combined nodes' power takes one more factor beta per node (src/Calc.cpp:453-464), and
+// their z - never set by the reference, an uninitialised int_seg (src/Calc.cpp:433), 0 in its
+// builds on paths at z = 0 - is the z of the segment the interval starts from.  A segment
+// end outside the r_max box, on which the reference's skip loop spins forever
+// (src/Calc.cpp:303-316), ends the walk with ERR_WALK_LIMIT.
+struct CWalk {
+  double t, t2, tpp, stepmax, step0;
+  int s, order;
+  bool more;
+};
+
+// One interval of the compressed walk: [t1, t2], its Gauss order, the segment whose beam
+// position gives its nodes (comb = false) or the combined centre and mean power (comb).
+struct CInterval {
+  double t1, t2, cx, cy, cq;
+  int s, order;
+  bool comb;
+};
+
+constexpr double kLn2 = 0.6931471805599453;    // ln 2, the double nearest to it
+
+__device__ __forceinline__ bool in_rmax(const DevProblem& P, double x, double y) {
+  return !((x > P.rx1) || (x < P.rx0) || (y > P.ry1) || (y < P.ry0));
+}
+
+static __device__ __noinline__ void cwalk_begin(const DevBeam& B, const DevSeg* path, double t, bool is_sol, CWalk& W) {
+  W.t = t;
+  W.s = find_seg(path, B.nseg, t);
+  W.step0 = is_sol ? rn_mul(B.nond, B.az) : B.nond;
+  W.stepmax = W.step0;
+  W.order = 16;
+  W.t2 = t; W.tpp = 0.0;
+  if (t > B.tlast) { W.tpp = rn_add(W.tpp, rn_sub(t, B.tlast)); W.t2 = B.tlast; }
+  int guard = 0;
+  while (W.tpp >= rn_sub(rn_mul(2.0, W.stepmax), W.step0) && guard++ < 4096) {
+    W.stepmax = rn_mul(W.stepmax, 2.0);
+    if (W.order != 2) W.order /= 2;
+  }
+  W.more = true;
+}
+
+// The next interval of the compressed walk into I; false when the walk has ended without
+// one.  err receives ERR_WALK_LIMIT for a segment end outside the r_max box.
+static __device__ __noinline__ bool cwalk_next(const DevProblem& P, const DevBeam& B, const DevSeg* path, CWalk& W,
+                                           CInterval& I, int& err) {
+  if (!W.more) return false;
+  if (path[W.s].tend <= 0.0) { W.more = false; return false; }
+  if (!in_rmax(P, path[W.s].x, path[W.s].y)) { err |= ERR_WALK_LIMIT; W.more = false; return false; }
+  int guard = 0;
+  while (W.tpp >= rn_sub(rn_mul(2.0, W.stepmax), W.step0) && guard++ < 4096) {
+    W.stepmax = rn_mul(W.stepmax, 2.0);
+    if (W.order != 2) W.order /= 2;
+  }
+  const double rt = ref_time(B, path, W.tpp, W.s);
+  const double use = (rt < W.stepmax) ? rt : W.stepmax;
+  const BeamLoc Lp = beam_loc(P, path, W.t2, W.s);
+  const double xp = Lp.x, yp = Lp.y;
+  const double r2 = rn_mul(rn_mul(kLn2 / 8.0, B.ax2),
+                           rn_add(rn_div(rn_mul(rn_mul(12.0, rn_sub(W.t, W.t2)), P.a), B.ax2), 1.0));
+  int s2 = W.s, ncomb = 0;
+  double t1 = path[W.s - 1].tend;
+  double sum_t = 0.0, sum_qt = 0.0, sum_qtx = 0.0, sum_qty = 0.0;
+  if (t1 < rn_sub(W.t2, use)) {
+    t1 = rn_sub(W.t2, use);
+  } else {
+    for (int it = 0;; ++it) {                              // combine segments (src/Calc.cpp:350-425)
+      if (it > kMaxWalkSteps) { err |= ERR_WALK_LIMIT; W.more = false; break; }
+      if (path[s2 - 1].tend <= 0.0) { W.more = false; break; }
+      double xs = path[s2 - 1].x, ys = path[s2 - 1].y;
+      const double dist2 = rn_add(rn_mul(rn_sub(xs, xp), rn_sub(xs, xp)), rn_mul(rn_sub(ys, yp), rn_sub(ys, yp)));
+      const double ts = path[s2 - 1].tend;
+      if (!in_rmax(P, xp, yp)) break;
+      const DevSeg cur = path[s2], prv = path[s2 - 1];
+      bool stop = false;
+      if ((dist2 > r2) ||
+          (cur.q != prv.q && (W.order > 2 || rn_sub(W.t2, ts) > rn_div(W.stepmax, 64.0)))) {
+        if (cur.mode) {
+          const double d = rn_sub(t1, ts);
+          sum_qtx = rn_add(sum_qtx, rn_mul(rn_mul(cur.x, cur.q), d));
+          sum_qty = rn_add(sum_qty, rn_mul(rn_mul(cur.y, cur.q), d));
+          sum_qt = rn_add(sum_qt, rn_mul(cur.q, d));
+          sum_t = rn_add(sum_t, d);
+          t1 = ts;
+        } else {
+          const double dx = rn_sub(cur.x, prv.x), dy = rn_sub(cur.y, prv.y), dt = rn_sub(cur.tend, ts);
+          const double den = rn_add(rn_mul(dx, dx), rn_mul(dy, dy));
+          const double num = rn_add(rn_mul(rn_sub(xp, xs), rn_sub(xp, xs)), rn_mul(rn_sub(yp, ys), rn_sub(yp, ys)));
+          double t_int = rn_add(ts, rn_mul(dt, rn_sub(rn_sqrt(rn_div(num, den)), rn_sqrt(rn_div(r2, den)))));
+          if (t_int < rn_sub(W.t2, W.stepmax)) t_int = rn_sub(W.t2, W.stepmax);
+          const double mid = rn_sub(rn_div(rn_add(t1, t_int), 2.0), ts);
+          const double px = rn_add(xs, rn_div(rn_mul(dx, mid), dt)), py = rn_add(ys, rn_div(rn_mul(dy, mid), dt));
+          const double d = rn_sub(t1, t_int);
+          sum_qtx = rn_add(sum_qtx, rn_mul(rn_mul(px, cur.q), d));
+          sum_qty = rn_add(sum_qty, rn_mul(rn_mul(py, cur.q), d));
+          sum_qt = rn_add(sum_qt, rn_mul(cur.q, d));
+          sum_t = rn_add(sum_t, d);
+          t1 = t_int;
+        }
+        stop = true;
+      } else {
+        if (ts < rn_sub(W.t2, W.stepmax)) { stop = true; t1 = rn_sub(W.t2, W.stepmax); }
+        else { t1 = ts; ++ncomb; }
+        const double dt = rn_sub(cur.tend, t1);
+        if (cur.mode) {
+          sum_qtx = rn_add(sum_qtx, rn_mul(rn_mul(cur.x, cur.q), dt));
+          sum_qty = rn_add(sum_qty, rn_mul(rn_mul(cur.y, cur.q), dt));
+        } else {
+          const double dx = rn_sub(cur.x, prv.x), dy = rn_sub(cur.y, prv.y);
+          const double mid = rn_sub(rn_div(rn_add(cur.tend, t1), 2.0), ts);
+          sum_qtx = rn_add(sum_qtx, rn_mul(rn_mul(rn_add(xs, rn_div(rn_mul(dx, mid), dt)), cur.q), dt));
+          sum_qty = rn_add(sum_qty, rn_mul(rn_mul(rn_add(ys, rn_div(rn_mul(dy, mid), dt)), cur.q), dt));
+        }
+        sum_qt = rn_add(sum_qt, rn_mul(cur.q, dt));
+        sum_t = rn_add(sum_t, dt);
+      }
+      if (t1 == path[s2 - 1].tend) {
+        xs = path[s2 - 1].x;
+        ys = path[s2 - 1].y;
+        --s2;
+        if (!in_rmax(P, xs, ys)) break;
+      }
+      if (stop) break;
+    }
+    if (!ncomb) { t1 = path[W.s - 1].tend; s2 = W.s - 1; }
+  }
+  I.t1 = t1; I.t2 = W.t2; I.s = W.s; I.order = W.order; I.comb = ncomb != 0;
+  I.cx = I.cy = I.cq = 0.0;
+  if (I.comb && sum_qt > 0.0) {
+    I.cx = rn_div(sum_qtx, sum_qt);
+    I.cy = rn_div(sum_qty, sum_qt);
+    I.cq = rn_div(sum_qt, sum_t);
+  }
+  W.tpp = rn_add(W.tpp, rn_sub(W.t2, t1));
+  W.t2 = t1;
+  if (W.tpp >= rn_sub(rn_mul(2.0, W.stepmax), W.step0)) {
+    W.stepmax = rn_mul(W.stepmax, 2.0);
+    if (W.order != 2) W.order /= 2;
+  }
+  W.s = s2;
+  if (t1 <= 0.0) W.more = false;
+  return true;
+}
+
+// Node k (absolute index into the packed Gauss tables) of a combined interval, emitted j-th
+// (0-based) in the interval's node order: at the combined centre, with the mean power times
+// beta^(j+1) (the reference multiplies by beta once per emitted node).
+static __device__ __noinline__ bool comb_node(const DevProblem& P, const DevBeam& B, const DevSeg* path,
+                                          const CInterval& I, double t, int k, int j, NodeVal& v) {
+  const double h = rn_sub(I.t2, I.t1);
+  const double tp = rn_mul(0.5, rn_add(rn_mul(h, P.gl_loc[k]), rn_add(I.t2, I.t1)));
+  const double ct = rn_mul(P.a12, rn_sub(t, tp));
+  double q = I.cq;
+  for (int i = 0; i <= j; ++i) q = rn_mul(q, B.beta);
+  const double dtau = rn_mul(rn_mul(0.5, h), P.gl_w[k]);
+  if (!(q > 0.0 && dtau > 0.0)) return false;
+  BeamLoc L;
+  L.x = I.cx; L.y = I.cy; L.z = path[I.s].z; L.q = q;
+  finish_node(B, ct, q, dtau, L, v);
+  return true;
+}
+
 // Method-of-images copy of a coordinate (src/Calc.cpp:588-603).
 __device__ __forceinline__ double image_coord(int c, double lo, double hi, double v) {
   const int n = abs(c % 2);

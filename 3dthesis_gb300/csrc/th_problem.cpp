@@ -338,7 +338,7 @@ bool th_load_deck(const std::string& param_input, HostProblem& hp, std::string& 
       hp.t_hist = s.num("Temperature", "Cutoff_Peak", 1e-9);
       hp.p_hist = s.num("Temperature", "Cutoff_T0TL", 1e-2);
       hp.r_max = s.num("Path", "Buffer", -1.0);
-      if (s.integer("Path", "Compression", 0)) { err = "path compression is not supported"; return false; }
+      hp.compress = s.integer("Path", "Compression", 0) != 0;
       hp.t_hist = 1.0 / hp.t_hist;
       if (hp.r_max < 0.0) {
         // as in the reference, the last beam's radius wins
@@ -390,6 +390,7 @@ void th_make_dev_problem(const HostProblem& hp, const DevSeg* d_segs, DevProblem
     off += D.nseg;
   }
   dp.T0 = hp.T0; dp.TL = hp.TL; dp.a = hp.a; dp.a12 = 12.0 * hp.a;
+  dp.compress = hp.compress ? 1 : 0;
   {  // TL - T0 = s + e exactly (TwoSum); s + e split into three floats
     const double s = hp.TL - hp.T0, bb = s - hp.TL;
     const double e = (hp.TL - (s - bb)) + (-hp.T0 - bb);

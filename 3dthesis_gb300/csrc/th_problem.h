@@ -58,6 +58,7 @@ struct DevProblem {
   double dt, sol_tol;
   int32_t sol_iter;
   int32_t tracking;
+  int32_t compress;         // path compression (GaussCompressIntegrate) on
   double rcheck;
   double end_time;
   // Gauss-Legendre tables for orders 2/4/8/16 packed at offset order - 2
@@ -77,6 +78,7 @@ struct HostProblem {
   int64_t pnum;
   double xmin, xmax, ymin, ymax, zmin, zmax, xres, yres, zres;
   bool use_bcs;
+  bool compress;                  // path compression (Settings: Path Compression)
   int bc_refl;
   double bcx0, bcx1, bcy0, bcy1, bcz0;
   // mode

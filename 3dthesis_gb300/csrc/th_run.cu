@@ -172,7 +172,9 @@ th_status init_run(th_ctx* ctx) {
   }
   ALLOC(r->rec[0], (size_t)kRecCap, 0);
   ALLOC(r->rec[1], (size_t)kRecCap, 0);
-  if (ctx->precision == TH_FP32_KAHAN) {       // the FP64 redo of FP32 solidification: queue, scratch lists
+  // the FP64 redo of FP32 solidification (queue, scratch lists); compressing decks
+  // solidify every record with the same kernel
+  if (ctx->precision == TH_FP32_KAHAN || hp.compress) {
     ALLOC(S.redo, (size_t)kRecCap, 0);
     ALLOC(S.redo_n, 1, 0);
     int dev = 0, sms = 0;
@@ -341,6 +343,7 @@ th_status read_counters(th_ctx* ctx, RunState* r, TrackCounters* h) {
   if (st != TH_OK) return st;
   // a capacity overflow first: a lost work item also leaves the step's waits to run out
   if (err & 32) return th_fail(ctx, TH_ERR_CAPACITY, "solidification record queue overflowed");
+  if (err & 1) return th_fail(ctx, TH_ERR_CAPACITY, "a solidification node list exceeded its buffer");
   if (err & 64) return th_fail(ctx, TH_ERR_CAPACITY, "a tracking list overflowed");
   if (err & 128) return th_fail(ctx, TH_ERR_CAPACITY, "the per-step work queue overflowed");
   if (err & 16) {

@@ -760,12 +760,13 @@ struct SeedSink {
 };
 
 // ------------------------------------------------------------------ node windows
-__global__ void __launch_bounds__(kGenThreads) k_nodes_window(DevProblem P, NodeWindow w, int first, int n, int is_sol,
+__global__ void __launch_bounds__(kGenThreads, 2) k_nodes_window(DevProblem P, NodeWindow w, int first, int n, int is_sol,
                                                               int* err) {
   __shared__ GenShared sh;
+  extern __shared__ __align__(16) unsigned char gen_dyn[];    // GenComp of a compressing deck
   const int slot = first + blockIdx.x;
   const NodeBufView nb = slot_view(w, slot);
-  gen_list_block(P, w.t[slot], is_sol != 0, nb, &w.count[slot], err, sh);
+  gen_list_block(P, w.t[slot], is_sol != 0, nb, &w.count[slot], err, sh, P.compress ? (GenComp*)gen_dyn : nullptr);
   if (P.tracking != TH_TRACK_NONE && threadIdx.x < 32) {   // the step's beam-trace candidates
     SeedSink sink{w.seeds + (size_t)slot * w.seed_cap, w.seed_cap, 0};
     beam_trace(P, w.t[slot], sink);
@@ -1706,12 +1707,9 @@ __device__ __noinline__ void point_sums_warp_call(const DevProblem* P, double x,
   point_sums_warp<GRAD>(*P, x, y, z, t, is_sol, *o, *pairs, *err);
 }
 
-// Sums at time t from a list generated by the block into its scratch buffer; a list longer
-// than the buffer is summed by warp 0 walking the path itself (point_sums_warp) instead.
-template <bool GRAD>
-__device__ void block_sums_at(const DevProblem& P, const TrackState& S, double t, bool is_sol, double x, double y,
-                              double z, PointSums& o, GenShared& sh, double (*red)[6], PointSums& bc,
-                              unsigned long long& pairs, int& err) {
+// The block's scratch list at time t (one out-of-line copy of the generator for both sums).
+__device__ __noinline__ void gen_scratch_list(const DevProblem& P, const TrackState& S, double t, bool is_sol,
+                                              GenShared& sh, GenComp* cs) {
   NodeBufView nb = S.redo_nb;
   const size_t off = (size_t)blockIdx.x * S.redo_cap;
   nb.x += off; nb.y += off; nb.z += off; nb.ipx += off; nb.ipy += off; nb.ipz += off; nb.dtau += off; nb.amp += off;
@@ -1721,12 +1719,35 @@ __device__ void block_sums_at(const DevProblem& P, const TrackState& S, double t
   int* cnt = S.redo_aux + 2 * blockIdx.x;
   if (threadIdx.x == 0) cnt[1] = 0;
   __syncthreads();
-  gen_list_block(P, t, is_sol, nb, cnt, cnt + 1, sh);
+  gen_list_block(P, t, is_sol, nb, cnt, cnt + 1, sh, cs);
   __syncthreads();
+}
+
+// Sums at time t from a list generated by the block into its scratch buffer; a list longer
+// than the buffer is summed by warp 0 walking the path itself (point_sums_warp) instead, or,
+// for a compressing deck (whose walk only the list generator restates), reported as
+// ERR_NODE_CAPACITY.
+template <bool GRAD>
+__device__ void block_sums_at(const DevProblem& P, const TrackState& S, double t, bool is_sol, double x, double y,
+                              double z, PointSums& o, GenShared& sh, GenComp* cs, double (*red)[6], PointSums& bc,
+                              unsigned long long& pairs, int& err) {
+  NodeBufView nb = S.redo_nb;
+  const size_t off = (size_t)blockIdx.x * S.redo_cap;
+  nb.x += off; nb.y += off; nb.z += off; nb.ipx += off; nb.ipy += off; nb.ipz += off; nb.dtau += off; nb.amp += off;
+  nb.kx += off; nb.ky += off; nb.kz += off; nb.w += off; nb.xh += off; nb.xl += off; nb.yh += off; nb.yl += off;
+  nb.zh += off; nb.zl += off;
+  nb.cap = S.redo_cap;
+  const int* cnt = S.redo_aux + 2 * blockIdx.x;
+  gen_scratch_list(P, S, t, is_sol, sh, cs);
   const int n = __ldcg(cnt), e = __ldcg(cnt + 1);
   err |= e & ERR_WALK_LIMIT;
   if (!(e & ERR_NODE_CAPACITY) && n <= nb.cap) {
     block_sums<GRAD>(nb, n, x, y, z, o, red, pairs);
+    return;
+  }
+  if (P.compress) {
+    err |= ERR_NODE_CAPACITY;
+    o.T = o.gx = o.gy = o.gz = o.lap = o.dtt = o.g_mag = o.lap_mag = 0.0;
     return;
   }
   if (threadIdx.x < 32) {
@@ -1747,16 +1768,23 @@ __device__ void block_sums_at(const DevProblem& P, const TrackState& S, double t
 // gradient sums at the solidification time from a list the block generates, all in FP64;
 // then the fields, overwriting the FP32 pass's values of the record.  The window is intact:
 // a window is rebuilt on the same stream only after its records' solidification.
+// all > 0: every one of the first `all` records instead of the queue (the solidification of
+// compressing decks, whose walk only the list generator restates; a later record of a
+// point wins, as in k_solidify).  A compressing deck's kernel takes a GenComp as dynamic
+// shared memory.
 __global__ void __launch_bounds__(kGenThreads, 2) k_solidify_redo(DevProblem P, TrackState S, NodeWindow W,
-                                                                  const SolRec* rec) {
+                                                                  const SolRec* rec, int all) {
   __shared__ GenShared sh;
   __shared__ double red[kGenThreads / 32][6];
   __shared__ PointSums bc;
-  const int n = min(__ldcg(S.redo_n), S.rec_cap);
+  extern __shared__ __align__(16) unsigned char gen_dyn[];
+  GenComp* cs = P.compress ? (GenComp*)gen_dyn : nullptr;
+  const int n = all > 0 ? all : min(__ldcg(S.redo_n), S.rec_cap);
   unsigned long long pairs = 0;
   int err = 0;
   for (int e = blockIdx.x; e < n; e += gridDim.x) {
-    const SolRec r = rec[S.redo[e].i];
+    const SolRec r = rec[all > 0 ? e : S.redo[e].i];
+    if (all > 0 && S.sol_step[r.p] != r.step) continue;    // block-uniform: a later record wins
     double x, y, z;
     point_xyz(P, r.p, x, y, z);
     const int slot = r.step - W.base + 1;
@@ -1770,16 +1798,16 @@ __global__ void __launch_bounds__(kGenThreads, 2) k_solidify_redo(DevProblem P, 
     for (int it = 1;; ++it) {
       const double m = rn_div(rn_sub(T2, T1), rn_sub(t2, t1));
       tsol = rn_add(t1, rn_div(rn_sub(P.TL, T1), m));
-      block_sums_at<false>(P, S, tsol, false, x, y, z, ps, sh, red, bc, pairs, err);
+      block_sums_at<false>(P, S, tsol, false, x, y, z, ps, sh, cs, red, bc, pairs, err);
       const double Tt = P.T0 + ps.T;
       const double e2 = int_abs(rn_sub(1.0, rn_div(Tt, P.TL)));
       if ((e2 < P.sol_tol) || (it >= P.sol_iter)) break;
       if (Tt > P.TL) { t1 = tsol; T1 = Tt; } else { t2 = tsol; T2 = Tt; }
     }
-    block_sums_at<true>(P, S, tsol, true, x, y, z, ps, sh, red, bc, pairs, err);
+    block_sums_at<true>(P, S, tsol, true, x, y, z, ps, sh, cs, red, bc, pairs, err);
     if (threadIdx.x == 0) {
       store_fields(P, S, r.p, tsol, ps);
-      atomicAdd(&S.C->redo_total, 1ull);
+      if (all == 0) atomicAdd(&S.C->redo_total, 1ull);
     }
   }
   if (threadIdx.x == 0) {
@@ -1818,7 +1846,8 @@ __global__ void k_final_field(DevProblem P, TrackState S, int f, double* out) {
 void th_launch_nodes_window(const DevProblem& P, const NodeWindow& w, int first_slot, int nslots, bool is_sol,
                             int* d_err, cudaStream_t s) {
   if (nslots <= 0) return;
-  k_nodes_window<<<nslots, kGenThreads, 0, s>>>(P, w, first_slot, nslots, is_sol ? 1 : 0, d_err);
+  k_nodes_window<<<nslots, kGenThreads, P.compress ? sizeof(GenComp) : 0, s>>>(P, w, first_slot, nslots, is_sol ? 1 : 0,
+                                                                              d_err);
 }
 
 // The layout SlotRef reads: every field one array of nb.cap entries, the fields nb.cap apart
@@ -1867,7 +1896,8 @@ static cudaError_t launch_track_t(const DevProblem& P, const TrackState& S, cons
   cudaFuncAttributes ta{}, na{};
   if ((e = cudaFuncGetAttributes(&ta, k_track<PREC, SURF>)) != cudaSuccess) return e;
   if ((e = cudaFuncGetAttributes(&na, k_nodes_window)) != cudaSuccess) return e;
-  const size_t need = smem + ta.sharedSizeBytes + na.sharedSizeBytes + 2 * 1024;   // + 1 KB reserved per block
+  const size_t need = smem + ta.sharedSizeBytes + na.sharedSizeBytes + (P.compress ? sizeof(GenComp) : 0) +
+                      2 * 1024;                                                   // + 1 KB reserved per block
   const int carve = std::min(100, (int)((need * 100 + 228 * 1024 - 1) / (228 * 1024)));
   e = cudaFuncSetAttribute(k_track<PREC, SURF>, cudaFuncAttributePreferredSharedMemoryCarveout, carve);
   if (e != cudaSuccess) return e;
@@ -1904,6 +1934,10 @@ void th_launch_solidify(const DevProblem& P, const TrackState& S, const NodeWind
   if (nrec <= 0) return;
   k_sol_latest<<<(nrec + 255) / 256, 256, 0, s>>>(S, rec, nrec);
   if (!do_sol) return;
+  if (P.compress) {               // every record by the list-based FP64 kernel
+    k_solidify_redo<<<S.redo_blocks, kGenThreads, sizeof(GenComp), s>>>(P, S, w, rec, nrec);
+    return;
+  }
   if (precision == 0) {
     k_solidify<0><<<(nrec + 127) / 128, 128, 0, s>>>(P, S, rec, nrec);
     return;
@@ -1911,7 +1945,7 @@ void th_launch_solidify(const DevProblem& P, const TrackState& S, const NodeWind
   k_solidify<1><<<(nrec + 127) / 128, 128, 0, s>>>(P, S, rec, nrec);
   // one to five percent of the records are redone, a block each: a persistent pass over the
   // queue, then the queue is emptied
-  k_solidify_redo<<<S.redo_blocks, kGenThreads, 0, s>>>(P, S, w, rec);
+  k_solidify_redo<<<S.redo_blocks, kGenThreads, 0, s>>>(P, S, w, rec, 0);
   cudaMemsetAsync(S.redo_n, 0, sizeof(int), s);
 }
 

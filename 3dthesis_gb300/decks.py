@@ -340,6 +340,16 @@ def small_spots() -> Deck:
         scan_fracs=[30, 70, 100], tracking="None")
 
 
+def small_zigzag() -> Deck:
+    """A fine serpentine of 20 short 60 um tracks with 30 um hatch moves (a thin-wall-like
+    path): successive segments lie within the heat's diffusion distance of each other."""
+    return Deck(
+        name="small_zigzag", mode="Snapshots", beams=[BeamSpec()],
+        paths=[serpentine_path(20, 0.06, 0.03, 0.5)],
+        axes=(AxisSpec(-0.1e-3, 0.19e-3, num=30), AxisSpec(-0.1e-3, 0.69e-3, num=40), AxisSpec(-0.05e-3, 0.0, num=6)),
+        scan_fracs=[30, 70, 100], tracking="None")
+
+
 def small_sweep(n: int = 10, seed: int = 3) -> List[Deck]:
     """Small uneven snapshot sweep: seeded power, speed, widths and track counts, grids
     from 8x8x3 to 40x30x10 points, snapshots at 50 % and 100 %; deck 1 scans spots and

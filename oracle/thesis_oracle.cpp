@@ -106,6 +106,7 @@ struct Problem {
   double sol_tol; int sol_iter; double t_hist, p_hist, r_max; int compress; int thnum;
   double end_time;
   bool do_sol;
+  mutable bool walk_error = false;   // a compressed walk met a segment end outside the r_max box
   // grid state
   std::vector<double> T, T_last, tSol, G, V, Gx, Gy, Gz, dTdt, eqFrac, depth;
   // per point, for the parity tests' explanations: the closest approach of an evaluated T
@@ -377,7 +378,7 @@ bool load_problem(Problem& P, const std::string& param_input, std::string& err) 
     P.t_hist = dval(s[0][2], 1e-9); P.p_hist = dval(s[0][3], 1e-2);
     P.r_max = dval(s[1][0], -1.0); P.compress = ival(s[1][1], 0);
     P.thnum = ival(s[2][0], 1);
-    if (P.compress) { err = "path compression is not supported"; return false; }
+
     P.t_hist = 1.0 / P.t_hist;
     if (P.r_max < 0.0) {
       for (const Beam& B : P.beams) {
@@ -505,6 +506,151 @@ void gauss_nodes(const Problem& P, double t, bool is_sol, Nodes& N, uint64_t* si
   }
 }
 
+// Path compression (GaussCompressIntegrate, src/Calc.cpp:213-501): the backward walk of
+// gauss_nodes, except that where an interval would reach into the previous segment, the
+// segments whose end points lie within the heat's diffusion distance r of the beam position
+// at t2 (r^2 = ln2/8 ax^2 (12 a (t - t2) / ax^2 + 1)) and whose power matches are combined
+// into one interval, integrated with the Gauss nodes of one point: the power-and-time
+// weighted centre of the combined stretch and its mean power.  Restated as the reference
+// computes it, including:
+//  - the node power is multiplied by beta once per node inside the node loop, so the k-th
+//    node of a combined interval carries beta^(k+1) (src/Calc.cpp:453-464);
+//  - the combined node's z is never set by the reference (an uninitialised int_seg,
+//    src/Calc.cpp:433); its builds give 0 on paths at z = 0.  Here it is the z of the
+//    segment the interval starts from;
+//  - a segment end outside the r_max box makes the reference's skip loop spin forever
+//    (src/Calc.cpp:303-316 never moves to another segment); here the walk stops and the
+//    node list is flagged (P.walk_error).
+void gauss_compress_nodes(const Problem& P, double t, bool is_sol, Nodes& N) {
+  const GaussTables& G = gauss();
+  for (size_t b = 0; b < P.paths.size(); ++b) {
+    const Beam& B = P.beams[b];
+    const std::vector<Seg>& path = P.paths[b];
+    int s = find_seg(path, t);
+    const double beta = std::pow(3.0 / kPi, 1.5) * B.q / (P.rho * P.cps);
+    const double t0 = 0.0;
+    double step0 = B.nond;
+    if (is_sol) step0 *= B.az;
+    double stepmax = step0;
+    int order = 16;
+    {
+      Loc L = beam_loc(P, path, t, s);
+      const double qb = L.q * beta;
+      if (t <= path.back().tend && qb > 0.0)
+        add_node(N, L.x, L.y, L.z, B.ax * B.ax + 0.0, B.ay * B.ay + 0.0, B.az * B.az + 0.0, 0.0, qb);
+    }
+    double t2 = t, t1 = t, tpp = 0.0;
+    if (t > path.back().tend) { tpp += t - path.back().tend; t2 = path.back().tend; }
+    while (tpp >= 2 * stepmax - step0) { stepmax *= 2.0; if (order != 2) order /= 2; }
+    bool more = true;
+    while (more) {
+      double sum_t = 0, sum_qt = 0, sum_qtx = 0, sum_qty = 0;
+      int s2, ncomb = 0;
+      // segment ends outside the r_max box are skipped (src/Calc.cpp:303-316)
+      {
+        const double ts = path[s].tend;
+        if (ts <= t0) break;
+        if (!in_rmax(P, path[s].x, path[s].y)) { P.walk_error = true; break; }
+      }
+      while (tpp >= 2 * stepmax - step0) { stepmax *= 2.0; if (order != 2) order /= 2; }
+      const double rt = ref_time(path, B, tpp, s);
+      const double use = (rt < stepmax) ? rt : stepmax;
+      const Loc Lp = beam_loc(P, path, t2, s);
+      const double xp = Lp.x, yp = Lp.y;
+      const double r2 = std::log(2.0) / 8.0 * (B.ax * B.ax) * (12.0 * (t - t2) * P.a / (B.ax * B.ax) + 1.0);
+      s2 = s;
+      t1 = path[s - 1].tend;
+      if (t1 < t2 - use) {
+        t1 = t2 - use;
+      } else {
+        while (true) {                                   // combine segments (src/Calc.cpp:350-425)
+          if (path[s2 - 1].tend <= t0) { more = false; break; }
+          double xs = path[s2 - 1].x, ys = path[s2 - 1].y;
+          const double dist2 = (xs - xp) * (xs - xp) + (ys - yp) * (ys - yp);
+          const double ts = path[s2 - 1].tend;
+          if (!in_rmax(P, xp, yp)) break;
+          bool stop = false;
+          if ((dist2 > r2) || (path[s2].q != path[s2 - 1].q && (order > 2 || (t2 - ts) > (stepmax / 64.0)))) {
+            if (path[s2].mode) {
+              sum_qtx += path[s2].x * path[s2].q * (t1 - ts);
+              sum_qty += path[s2].y * path[s2].q * (t1 - ts);
+              sum_qt += path[s2].q * (t1 - ts);
+              sum_t += (t1 - ts);
+              t1 = ts;
+            } else {
+              const double dx = path[s2].x - path[s2 - 1].x, dy = path[s2].y - path[s2 - 1].y;
+              const double dt = path[s2].tend - ts;
+              double t_int = ts + dt * (std::sqrt(((xp - xs) * (xp - xs) + (yp - ys) * (yp - ys)) / (dx * dx + dy * dy)) -
+                                        std::sqrt(r2 / (dx * dx + dy * dy)));
+              if (t_int < t2 - stepmax) t_int = t2 - stepmax;
+              sum_qtx += (xs + dx * ((t1 + t_int) / 2.0 - ts) / dt) * path[s2].q * (t1 - t_int);
+              sum_qty += (ys + dy * ((t1 + t_int) / 2.0 - ts) / dt) * path[s2].q * (t1 - t_int);
+              sum_qt += path[s2].q * (t1 - t_int);
+              sum_t += (t1 - t_int);
+              t1 = t_int;
+            }
+            stop = true;
+          } else {
+            if (ts < t2 - stepmax) { stop = true; t1 = t2 - stepmax; }
+            else { t1 = ts; ncomb++; }
+            const double dt = path[s2].tend - t1;
+            if (path[s2].mode) {
+              sum_qtx += path[s2].x * path[s2].q * dt;
+              sum_qty += path[s2].y * path[s2].q * dt;
+              sum_qt += path[s2].q * dt;
+              sum_t += dt;
+            } else {
+              const double dx = path[s2].x - path[s2 - 1].x, dy = path[s2].y - path[s2 - 1].y;
+              sum_qtx += (xs + dx * ((path[s2].tend + t1) / 2.0 - ts) / dt) * path[s2].q * dt;
+              sum_qty += (ys + dy * ((path[s2].tend + t1) / 2.0 - ts) / dt) * path[s2].q * dt;
+              sum_qt += path[s2].q * dt;
+              sum_t += dt;
+            }
+          }
+          if (t1 == path[s2 - 1].tend) {
+            xs = path[s2 - 1].x;
+            ys = path[s2 - 1].y;
+            s2--;
+            if (!in_rmax(P, xs, ys)) break;
+          }
+          if (stop) break;
+        }
+        if (!ncomb) { t1 = path[s - 1].tend; s2 = s - 1; }
+      }
+      const int base = order - 2;
+      if (ncomb) {
+        if (sum_qt > 0.0) {
+          const double cx = sum_qtx / sum_qt, cy = sum_qty / sum_qt, cz = path[s].z;
+          double q = sum_qt / sum_t;
+          for (int k = base + order - 1; k >= base; --k) {
+            const double tp = 0.5 * ((t2 - t1) * G.loc[k] + (t2 + t1));
+            const double ct = 12.0 * P.a * (t - tp);
+            q *= beta;
+            const double dtau = 0.5 * (t2 - t1) * G.w[k];
+            if ((q > 0.0) && (dtau > 0.0))
+              add_node(N, cx, cy, cz, B.ax * B.ax + ct, B.ay * B.ay + ct, B.az * B.az + ct, dtau, q);
+          }
+        }
+      } else {
+        for (int k = base + order - 1; k >= base; --k) {
+          const double tp = 0.5 * ((t2 - t1) * G.loc[k] + (t2 + t1));
+          const double ct = 12.0 * P.a * (t - tp);
+          Loc L = beam_loc(P, path, tp, s);
+          const double qb = L.q * beta;
+          const double dtau = 0.5 * (t2 - t1) * G.w[k];
+          if (qb > 0.0 && dtau > 0.0)
+            add_node(N, L.x, L.y, L.z, B.ax * B.ax + ct, B.ay * B.ay + ct, B.az * B.az + ct, dtau, qb);
+        }
+      }
+      tpp += t2 - t1;
+      t2 = t1;
+      if (tpp >= 2 * stepmax - step0) { stepmax *= 2.0; if (order != 2) order /= 2; }
+      s = s2;
+      if (t1 <= t0) more = false;
+    }
+  }
+}
+
 // Method-of-images copies of the node list (src/Calc.cpp:503-608).
 void add_bcs(const Problem& P, Nodes& N) {
   std::vector<std::array<int, 3>> all{{0, 0, 0}}, frontier{{0, 0, 0}};
@@ -540,7 +686,16 @@ void add_bcs(const Problem& P, Nodes& N) {
 
 void make_nodes(const Problem& P, double t, bool is_sol, Nodes& N) {        // src/Calc.cpp:48-65
   N.clear();
-  gauss_nodes(P, t, is_sol, N);
+  if (P.compress) {
+    gauss_compress_nodes(P, t, is_sol, N);
+    if (!is_sol) {                         // the smaller of the two lists (the plain one on a tie)
+      Nodes R;
+      gauss_nodes(P, t, is_sol, R);
+      if (R.size() <= N.size()) N = R;
+    }
+  } else {
+    gauss_nodes(P, t, is_sol, N);
+  }
   if (P.use_bcs) add_bcs(P, N);
 }
 

@@ -19,7 +19,8 @@ own process (the reference keeps function-static state).  The fixtures hold:
   a small Snapshots deck and a small Solidification deck, byte for byte: ``names`` and
   ``file<i>`` (the file's bytes).
 
-``python tests/golden/make_golden.py csv`` regenerates only the csv fixtures.
+``python tests/golden/make_golden.py csv`` (or ``comp``) regenerates only the csv (or the
+path-compression) fixtures.
 """
 from __future__ import annotations
 
@@ -123,9 +124,14 @@ NODE_TIMES = {
     "small_spots": [0.3e-3, 0.9e-3, 1.7e-3, 2.52e-3, 3.1e-3],
     "small_multibeam": [1e-4, 5e-4, 1.5e-3, 2.5e-3],
     "small_bcs": [0.4e-3, 1.2e-3, 3.0e-3],
+    # path compression (Settings: Path Compression 1, src/Calc.cpp:48-58,213-501)
+    "comp_spots": [0.3e-3, 0.9e-3, 1.7e-3, 2.52e-3, 3.1e-3, 4.0e-3],
+    "comp_lines": [0.4e-3, 1.1e-3, 1.9e-3, 2.6e-3],
+    "comp_zigzag": [0.2e-3, 0.7e-3, 1.3e-3, 2.2e-3, 3.0e-3],
 }
 RUNS = {"small_surface": ("small_surface", "Surface"), "small_volume": ("small_surface", "Volume"),
-        "small_none": ("small_surface", "None"), "small_multibeam": ("small_multibeam",)}
+        "small_none": ("small_surface", "None"), "small_multibeam": ("small_multibeam",),
+        "small_surface_comp": ("small_surface", "Surface")}
 
 
 CSV_DECKS = ("csv_snapshot", "small_multibeam")
@@ -151,6 +157,12 @@ def csv_fixture(deck, scratch):
 
 def node_deck(name):
     """The deck each nodes_<name>.npz fixture was made from."""
+    if name.startswith("comp_"):
+        d = {"comp_spots": decks.small_spots, "comp_lines": decks.small_snapshot,
+             "comp_zigzag": decks.small_zigzag}[name]()
+        d.name = name
+        d.settings_extra = {"Path": {"Compression": "1"}}
+        return d
     if name == "small_bcs":
         d = decks.small_snapshot()
         d.name = "small_bcs"
@@ -162,12 +174,24 @@ def node_deck(name):
 def run_deck(tag):
     """The deck each run_<tag>.npz fixture was made from."""
     fn, *args = RUNS[tag]
-    return getattr(decks, fn)(*args)
+    d = getattr(decks, fn)(*args)
+    if tag.endswith("_comp"):                  # path compression on
+        d.name = tag
+        d.settings_extra = {"Path": {"Compression": "1"}}
+    return d
 
 
 def main():
     if not os.path.exists(REF_LIB):
         sys.exit(f"missing {REF_LIB}: build it with `make -C oracle ref`")
+    if sys.argv[1:] == ["comp"]:               # only the path-compression fixtures
+        with tempfile.TemporaryDirectory() as scratch:
+            for name in [n for n in NODE_TIMES if n.startswith("comp_")]:
+                node_fixture(node_deck(name), NODE_TIMES[name], scratch)
+            for tag in [t for t in RUNS if t.endswith("_comp")]:
+                run_fixture(run_deck(tag), scratch, tag)
+        print("compression fixtures written to", HERE)
+        return
     if sys.argv[1:] == ["csv"]:
         with tempfile.TemporaryDirectory() as scratch:
             for name in CSV_DECKS:

@@ -44,7 +44,6 @@ def test_missing_deck_is_an_error(thesis, built_library, tmp_path):
 @pytest.mark.parametrize("edit,needle", [
     (lambda d: setattr(d, "mode", "Bogus"), "exactly one"),
     (lambda d: setattr(d, "tracking", "Geometry"), "tracking"),
-    (lambda d: d.settings_extra.update({"Path": {"Compression": "1"}}), "compression"),
     (lambda d: setattr(d.beams[0], "width_x", 0.0), "widths"),
 ])
 def test_bad_decks_are_rejected_before_any_launch(thesis, built_library, decks, tmp_path, edit, needle):

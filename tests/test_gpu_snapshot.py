@@ -122,3 +122,26 @@ def test_times_in_one_launch_match_single_snapshots(lib, deck_dir):
         got = out.cpu().numpy().reshape(len(times), sim.pnum)
         for i in range(len(times)):
             assert np.array_equal(got[i], sim.snapshot(i)), i
+
+
+@pytest.mark.parametrize("name", ["comp_spots", "comp_lines", "comp_zigzag"])
+@pytest.mark.parametrize("precision,tol", [("fp64", TOL_FP64), ("fp32", TOL_FP32)])
+def test_path_compression_snapshots_and_batch(lib, oracle, tmp_path, name, precision, tol):
+    """Decks with path compression (GaussCompressIntegrate, src/Calc.cpp:213-501): the
+    device's lists are the reference's (test_device_nodes_bit_identical_to_reference covers
+    these decks' goldens), the whole-grid snapshots match the oracle, and the same decks in
+    one batch match their single-deck snapshots."""
+    d = make_golden.node_deck(name)
+    path = d.write(str(tmp_path / name))
+    o = oracle(path)
+    singles = []
+    with lib.Simulation(path, precision) as sim:
+        for i in range(o.n_snapshots):
+            ref = o.snapshot(i)
+            got = sim.snapshot(i)
+            assert np.max(np.abs(got - ref)) <= tol, (name, i, np.max(np.abs(got - ref)))
+            singles.append(got)
+    with lib.Batch([path, path], precision) as b:
+        T = b.snapshot(o.n_snapshots - 1)
+    off = b.offsets
+    assert np.array_equal(T[off[0]:off[1]], singles[-1]) and np.array_equal(T[off[1]:off[2]], singles[-1])
