@@ -1467,10 +1467,16 @@ __device__ __forceinline__ void point_sums_warp(const DevProblem& P, double x, d
   o.g_mag = o.lap_mag = 0.0;
 }
 
-// The same sums in the FP32 form: the walk and each node's time, t - t', position and
-// offset from the point stay FP64; the inverse widths, amplitude, exponential and the six
-// sums (Kahan-compensated) are FP32.  The line position uses the segment's reciprocal
-// duration, formed once per interval.
+// The same sums in the FP32 form.  The walk stays FP64, and so do each node's time before
+// t (t - t') and its offset from the point; the inverse widths, amplitude, exponential and the
+// six sums (Kahan-compensated) are FP32.  FP64 arithmetic issues at about 1/64 of the FP32
+// rate on this GPU, so per node only the time and the three offsets are formed in FP64, each
+// one fused multiply-add from constants of its interval: t - t' = (t - m) - (h/2) x_k and
+// offset = (x - p0 - r0 D) - (h/2 D / duration) x_k for a line segment (m the interval's
+// midpoint, x_k the Gauss abscissa, p0 and D the segment's start and extent, r0 the
+// midpoint's fraction along it).  The power cut-off box is tested once per interval when
+// both ends of the segment lie inside it (the nodes lie between them), else per node exactly
+// as the reference computes the position; image copies mirror the node in FP64.
 template <bool GRAD>
 __device__ __forceinline__ void point_sums_f32(const DevProblem& P, double x, double y, double z, double t, bool is_sol,
                                PointSums& o, unsigned long long& pairs, int& err) {
@@ -1481,22 +1487,24 @@ __device__ __forceinline__ void point_sums_f32(const DevProblem& P, double x, do
     cj = (tt - sj) - yy;
     sj = tt;
   };
-  auto add = [&](double nx0, double ny0, double nz0, double ct, double qb, double dtau, const DevBeam& B) {
-    const float fx = (float)(B.ax2 + ct), fy = (float)(B.ay2 + ct), fz = (float)(B.az2 + ct);
+  const float a12f = (float)P.a12;
+  // a node at FP64 offset (ox, oy, oz) from the point, tau before t, with power q beta (qb)
+  // and weight dtau (0: the instantaneous node)
+  auto add = [&](double ox, double oy, double oz, float tau, float qb, float dtau, float ax2, float ay2, float az2) {
+    const float ct = a12f * tau;
+    const float fx = ax2 + ct, fy = ay2 + ct, fz = az2 + ct;
     const float ipx = __frcp_rn(fx), ipy = __frcp_rn(fy), ipz = __frcp_rn(fz);
-    const float amp = (float)qb * __frsqrt_rn(fx * fy * fz);
-    const float fdt = (float)dtau;
+    const float amp = qb * __frsqrt_rn(fx * fy * fz);
     for (int im = 0; im < P.n_images; ++im) {
-      double nx = nx0, ny = ny0, nz = nz0;
-      if (im) {
-        nx = image_coord(P.img[im][0], P.bcx0, P.bcx1, nx0);
-        ny = image_coord(P.img[im][1], P.bcy0, P.bcy1, ny0);
-        nz = image_coord(P.img[im][2], P.bcz0, P.bcz1, nz0);
+      float dx = (float)ox, dy = (float)oy, dz = (float)oz;
+      if (im) {                                  // the mirrored node, from its FP64 position
+        dx = (float)(x - image_coord(P.img[im][0], P.bcx0, P.bcx1, x - ox));
+        dy = (float)(y - image_coord(P.img[im][1], P.bcy0, P.bcy1, y - oy));
+        dz = (float)(z - image_coord(P.img[im][2], P.bcz0, P.bcz1, z - oz));
       }
-      const float dx = (float)(x - nx), dy = (float)(y - ny), dz = (float)(z - nz);
       const float e = (float)kNeg3Log2e * ((dx * dx * ipx + dy * dy * ipy) + dz * dz * ipz);
       const float phi = amp * ex2_approx(e);
-      const float seg = fdt * phi;
+      const float seg = dtau * phi;
       kahan(s0, c0, seg);
       if (GRAD) {
         const float ddx = -6.f * ipx, ddy = -6.f * ipy, ddz = -6.f * ipz;
@@ -1504,42 +1512,65 @@ __device__ __forceinline__ void point_sums_f32(const DevProblem& P, double x, do
         kahan(s1, c1, seg * dpx); kahan(s2, c2, seg * dpy); kahan(s3, c3, seg * dpz);
         const float dp2 = (dpx * dpx + dpy * dpy) + dpz * dpz, dd = (ddx + ddy) + ddz;
         kahan(s4, c4, seg * (dp2 + dd));
-        if (dtau == 0) kahan(s5, c5, phi);
+        if (dtau == 0.f) kahan(s5, c5, phi);
         m_g += seg * ((fabsf(dpx) + fabsf(dpy)) + fabsf(dpz));
         m_lap += seg * (dp2 - dd);
       }
       ++pairs;
     }
   };
+  auto inside = [&](double px, double py) {    // strictly inside the cut-off box, with a margin
+    const double mx = 1e-9 * (fabs(P.rx0) + fabs(P.rx1)), my = 1e-9 * (fabs(P.ry0) + fabs(P.ry1));
+    return px < P.rx1 - mx && px > P.rx0 + mx && py < P.ry1 - my && py > P.ry0 + my;
+  };
   for (int b = 0; b < P.nbeams; ++b) {
     const DevBeam B = P.beam[b];
     const DevSeg* path = P.segs + B.seg_off;
+    const float ax2 = (float)B.ax2, ay2 = (float)B.ay2, az2 = (float)B.az2;
     Walk W;
     walk_begin(B, path, t, is_sol, W);
     {
       const BeamLoc L = beam_loc(P, path, W.t, W.s);
       const double qb = L.q * B.beta;
-      if (W.t <= B.tlast && qb > 0.0) add(L.x, L.y, L.z, 0.0, qb, 0.0, B);
+      if (W.t <= B.tlast && qb > 0.0) add(x - L.x, y - L.y, z - L.z, 0.f, (float)qb, 0.f, ax2, ay2, az2);
     }
     int steps = 0;
     while (W.more) {
       if (++steps > kMaxWalkSteps) { err |= ERR_WALK_LIMIT; break; }
       walk_interval(B, path, W);
       const DevSeg cur = path[W.s], prv = path[W.s - 1];
-      const double inv = cur.mode ? 0.0 : 1.0 / (cur.tend - prv.tend);
-      const double h = W.t2 - W.t1;
+      const double h = W.t2 - W.t1, hh = 0.5 * h;
+      if (!(h > 0.0)) { walk_advance(W); continue; }      // zero weights: no node is kept
+      const double A = W.t - 0.5 * (W.t2 + W.t1);          // t minus the interval's midpoint
       const int base = W.order - 2;
+      const bool line = !cur.mode;
+      // the nodes' offsets: constant for a spot, linear in the abscissa along a line
+      double Bx = x - cur.x, By = y - cur.y, Bz = z - cur.z, Cx = 0.0, Cy = 0.0, Cz = 0.0, inv = 0.0;
+      if (line) {
+        inv = 1.0 / (cur.tend - prv.tend);
+        const double r0 = (0.5 * (W.t2 + W.t1) - prv.tend) * inv, r1 = hh * inv;
+        const double DX = cur.x - prv.x, DY = cur.y - prv.y, DZ = cur.z - prv.z;
+        Bx = (x - prv.x) - r0 * DX; By = (y - prv.y) - r0 * DY; Bz = (z - prv.z) - r0 * DZ;
+        Cx = r1 * DX; Cy = r1 * DY; Cz = r1 * DZ;
+      }
+      const bool all_in = line ? (inside(cur.x, cur.y) && inside(prv.x, prv.y)) : inside(cur.x, cur.y);
+      const float qb_in = (float)(cur.q * B.beta), hhf = (float)hh;
+      if (all_in && !(cur.q * B.beta > 0.0)) { walk_advance(W); continue; }
       for (int kk = base + W.order - 1; kk >= base; --kk) {
-        const double tp = 0.5 * (h * P.gl_loc[kk] + (W.t2 + W.t1));
-        double lx = cur.x, ly = cur.y, lz = cur.z;
-        if (!cur.mode) {
-          const double r = (tp - prv.tend) * inv;
-          lx = prv.x + r * (cur.x - prv.x); ly = prv.y + r * (cur.y - prv.y); lz = prv.z + r * (cur.z - prv.z);
+        const double loc = P.gl_loc[kk];
+        float qb = qb_in;
+        if (!all_in) {                                     // the reference's per-node test
+          const double tp = 0.5 * (h * loc + (W.t2 + W.t1));
+          double lx = cur.x, ly = cur.y;
+          if (line) {
+            const double r = (tp - prv.tend) * inv;
+            lx = prv.x + r * (cur.x - prv.x); ly = prv.y + r * (cur.y - prv.y);
+          }
+          const bool out = (lx > P.rx1) || (lx < P.rx0) || (ly > P.ry1) || (ly < P.ry0);
+          if (out || !(cur.q * B.beta > 0.0)) continue;
         }
-        const bool out = (lx > P.rx1) || (lx < P.rx0) || (ly > P.ry1) || (ly < P.ry0);
-        const double qb = (out ? 0.0 : cur.q) * B.beta;
-        const double dtau = 0.5 * h * P.gl_w[kk];
-        if (qb > 0.0 && dtau > 0.0) add(lx, ly, lz, P.a12 * (W.t - tp), qb, dtau, B);
+        add(fma(-Cx, loc, Bx), fma(-Cy, loc, By), fma(-Cz, loc, Bz), (float)fma(-hh, loc, A), qb,
+            hhf * (float)P.gl_w[kk], ax2, ay2, az2);
       }
       walk_advance(W);
     }
@@ -1586,6 +1617,26 @@ __device__ __forceinline__ double secant_tsol(const DevProblem& P, double x, dou
     if (Tt > P.TL) { t1 = tsol; T1 = Tt; } else { t2 = tsol; T2 = Tt; }
   }
   return tsol;
+}
+
+// The first estimate of the reference's secant (its only one in practice, see below).
+__device__ __forceinline__ double secant_first(const DevProblem& P, double T2, double T1, double t) {
+  const double t1 = rn_sub(t, P.dt);
+  const double m = rn_div(rn_sub(T2, T1), rn_sub(t, t1));
+  return rn_add(t1, rn_div(rn_sub(P.TL, T1), m));
+}
+
+// The reference's secant stops after its first estimate when its test value, int abs of
+// 1 - T(t_sol) / T_L with T from the plain node schedule (src/Grid.cpp:366-401), is below
+// Sol_Tol - which for a positive Sol_Tol happens exactly when 0 < T(t_sol) < 2 T_L - or when
+// Sol_Iter is 1.  The gradient sums at the same t_sol give T on the refined schedule, which
+// differs from the plain one by the quadrature error (~1e-3 relative); when that T lies
+// more than kStopMargin T_L inside (0, 2 T_L), the test's outcome is certain and the plain
+// schedule's sum is not formed.  Otherwise the secant runs as the reference's does.
+constexpr double kStopMargin = 0.05;
+__device__ __forceinline__ bool stop_test_decided(const DevProblem& P, double T_refined) {
+  if (P.sol_iter <= 1) return true;
+  return P.sol_tol > 0.0 && T_refined > kStopMargin * P.TL && T_refined < (2.0 - kStopMargin) * P.TL;
 }
 
 // G, the unit gradient, dT/dt (the reference's int abs), V and eqFrac of point p from the
@@ -1639,10 +1690,18 @@ __global__ void __launch_bounds__(128, 4) k_solidify(DevProblem P, TrackState S,
   unsigned long long pairs = 0;
   int err = 0;
   const double T2 = t_decode(S, P, r.T), T1 = t_decode(S, P, r.Tl);
-  const double tsol = secant_tsol<PREC>(P, x, y, z, T2, T1, r.t, pairs, err);
+  double tsol = secant_first(P, T2, T1, r.t);
   PointSums ps;
   if (PREC == 0) point_sums<true>(P, x, y, z, tsol, true, ps, pairs, err);
   else point_sums_f32<true>(P, x, y, z, tsol, true, ps, pairs, err);
+  if (!stop_test_decided(P, P.T0 + ps.T)) {          // the secant as the reference runs it
+    const double ts = secant_tsol<PREC>(P, x, y, z, T2, T1, r.t, pairs, err);
+    if (ts != tsol) {
+      tsol = ts;
+      if (PREC == 0) point_sums<true>(P, x, y, z, tsol, true, ps, pairs, err);
+      else point_sums_f32<true>(P, x, y, z, tsol, true, ps, pairs, err);
+    }
+  }
   if (PREC != 0) {
     const double G = sqrt(ps.gx * ps.gx + ps.gy * ps.gy + ps.gz * ps.gz);
     const double rate = fabs(rn_add(rn_mul(P.a, ps.lap), ps.dtt));
@@ -1793,18 +1852,22 @@ __global__ void __launch_bounds__(kGenThreads, 2) k_solidify_redo(DevProblem P, 
     double T2 = P.T0 + ps.T;
     block_sums<false>(slot_view(W, slot - 1), min(W.count[slot - 1], W.slot_cap), x, y, z, ps, red, pairs);
     double T1 = P.T0 + ps.T;
-    // the reference's secant (see secant_tsol), every sum by the block
-    double t2 = r.t, t1 = rn_sub(r.t, P.dt), tsol = 0.0;
-    for (int it = 1;; ++it) {
-      const double m = rn_div(rn_sub(T2, T1), rn_sub(t2, t1));
-      tsol = rn_add(t1, rn_div(rn_sub(P.TL, T1), m));
-      block_sums_at<false>(P, S, tsol, false, x, y, z, ps, sh, cs, red, bc, pairs, err);
-      const double Tt = P.T0 + ps.T;
-      const double e2 = int_abs(rn_sub(1.0, rn_div(Tt, P.TL)));
-      if ((e2 < P.sol_tol) || (it >= P.sol_iter)) break;
-      if (Tt > P.TL) { t1 = tsol; T1 = Tt; } else { t2 = tsol; T2 = Tt; }
-    }
+    // the reference's secant (see secant_tsol and stop_test_decided), every sum by the block
+    double tsol = secant_first(P, T2, T1, r.t);
     block_sums_at<true>(P, S, tsol, true, x, y, z, ps, sh, cs, red, bc, pairs, err);
+    if (!stop_test_decided(P, P.T0 + ps.T)) {
+      double t2 = r.t, t1 = rn_sub(r.t, P.dt);
+      for (int it = 1;; ++it) {
+        const double m = rn_div(rn_sub(T2, T1), rn_sub(t2, t1));
+        tsol = rn_add(t1, rn_div(rn_sub(P.TL, T1), m));
+        block_sums_at<false>(P, S, tsol, false, x, y, z, ps, sh, cs, red, bc, pairs, err);
+        const double Tt = P.T0 + ps.T;
+        const double e2 = int_abs(rn_sub(1.0, rn_div(Tt, P.TL)));
+        if ((e2 < P.sol_tol) || (it >= P.sol_iter)) break;
+        if (Tt > P.TL) { t1 = tsol; T1 = Tt; } else { t2 = tsol; T2 = Tt; }
+      }
+      block_sums_at<true>(P, S, tsol, true, x, y, z, ps, sh, cs, red, bc, pairs, err);
+    }
     if (threadIdx.x == 0) {
       store_fields(P, S, r.p, tsol, ps);
       if (all == 0) atomicAdd(&S.C->redo_total, 1ull);
