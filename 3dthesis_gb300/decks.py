@@ -322,6 +322,15 @@ def small_surface(tracking: str = "Surface", dt: float = 1e-5) -> Deck:
     return d
 
 
+def small_stork() -> Deck:
+    """Two 0.1 mm tracks on a 20x22x7 grid at 10 um, Stork tracking, dt = 2e-5 s: the pool
+    reaches the bottom layer, so the walk's bottom rule is exercised."""
+    d = small_surface("Stork", dt=2e-5)
+    d.paths = [serpentine_path(2, 0.1, 0.08, 0.8)]
+    d.axes = (AxisSpec(-0.05e-3, 0.14e-3, num=20), AxisSpec(-0.1e-3, 0.11e-3, num=22), AxisSpec(-0.06e-3, 0.0, num=7))
+    return d
+
+
 def small_multibeam(seed: int = 1) -> Deck:
     d = volume_multibeam(seed=seed, grid=(40, 40, 10), tracks=3, length_mm=0.25)
     d.name = "small_multibeam"

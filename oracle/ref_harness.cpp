@@ -7,8 +7,8 @@
  * Entry points call the reference's public interface:
  *   Init::GetFileNames / Init::ReadSimParams (src/Init.h), Grid (src/Grid.h),
  *   Calc::Integrate_Serial (src/Calc.h:23), Grid::Calc_T (src/Grid.h:290),
- *   Run::Simulate (src/Run.h), Grid::Output (src/Grid.h), and the Grid getters
- *   (src/Grid.h:299-370).
+ *   Run::Simulate (src/Run.h), Grid::Output and Grid::Output_RRDF_csv (src/Grid.h), and
+ *   the Grid getters (src/Grid.h:299-370).
  */
 #include <cstdint>
 #include <cstring>
@@ -81,6 +81,30 @@ void ref_simulate(void* h) {
 void ref_output(void* h, const char* name) {
   RefRun* r = (RefRun*)h;
   r->grid->Output(r->sim, name);
+}
+
+// The doubly reduced data a Stork run leaves in the grid (src/Grid.h:368-370): per row the
+// cell index (3), the two step times (2) and the 16 vertex temperatures, in the run's order.
+// Returns the row count; copies at most cap rows.
+int64_t ref_rrdf(void* h, uint32_t* idx, double* ts, double* Ts, int64_t cap) {
+  RefRun* r = (RefRun*)h;
+  const vector<uint32_t>& I = r->grid->get_RRDF_idxs();
+  const vector<double>& tt = r->grid->get_RRDF_ts();
+  const vector<double>& TT = r->grid->get_RRDF_Ts();
+  const int64_t n = (int64_t)tt.size() / 2;
+  for (int64_t q = 0; q < n && q < cap; ++q) {
+    for (int c = 0; c < 3; ++c) idx[3 * q + c] = I[3 * q + c];
+    for (int c = 0; c < 2; ++c) ts[2 * q + c] = tt[2 * q + c];
+    for (int c = 0; c < 16; ++c) Ts[16 * q + c] = TT[16 * q + c];
+  }
+  return n;
+}
+
+// The reference's RRDF writer (Grid::Output_RRDF_csv, src/Grid.cpp:203-238), as
+// bin/Main.cpp:109-111 calls it after a Stork run: Data/<Name>.<name>.csv.
+void ref_output_rrdf(void* h, const char* name) {
+  RefRun* r = (RefRun*)h;
+  r->grid->Output_RRDF_csv(r->sim, name);
 }
 
 int ref_field(void* h, const char* name, double* out) {

@@ -82,7 +82,7 @@ struct GaussTables {
 };
 const GaussTables& gauss() { static GaussTables g; return g; }
 
-enum { TRACK_NONE = 0, TRACK_VOLUME = 1, TRACK_SURFACE = 2 };
+enum { TRACK_NONE = 0, TRACK_VOLUME = 1, TRACK_SURFACE = 2, TRACK_STORK = 3 };
 
 struct Problem {
   std::string dir;
@@ -113,6 +113,11 @@ struct Problem {
   // to T_L (DBL_MAX: never evaluated) and the secant's T - T_last at its latest
   // solidification (0: never solidified)
   std::vector<double> band, sol_dT;
+  // Stork's doubly reduced data (src/Run.cpp:711-1079): per output cell its index (i, j, k),
+  // the two step times and the 16 vertex temperatures (8 at the earlier time, then 8 at the
+  // later one)
+  std::vector<uint32_t> rrdf_idx;
+  std::vector<double> rrdf_t, rrdf_T;
   std::vector<int> numMelt;
   std::vector<unsigned char> calc, outflag;
   std::atomic<long long> pairs{0};
@@ -298,8 +303,9 @@ bool load_problem(Problem& P, const std::string& param_input, std::string& err) 
       std::vector<std::vector<std::string>> m;
       read_blocks(f_mode, {"Solidification"}, {{"Tracking", "Timestep", "OutputFrequency", "CheckRadius", "Secondary"}}, m);
       const std::string tr = m[0][0].empty() ? "None" : m[0][0];
-      P.tracking = tr == "Volume" ? TRACK_VOLUME : tr == "Surface" ? TRACK_SURFACE : TRACK_NONE;
-      if (!(tr == "None" || tr == "Volume" || tr == "Surface")) { err = "unsupported tracking " + tr; return false; }
+      P.tracking = tr == "Volume" ? TRACK_VOLUME : tr == "Surface" ? TRACK_SURFACE : tr == "Stork" ? TRACK_STORK
+                                                                                                   : TRACK_NONE;
+      if (!(tr == "None" || tr == "Volume" || tr == "Surface" || tr == "Stork")) { err = "unsupported tracking " + tr; return false; }
       P.dt = dval(m[0][1], 1e-5); P.out_freq = ival(m[0][2], INT_MAX);
       P.rcheck = dval(m[0][3], 1.0); P.secondary = m[0][4].empty() ? false : (bool)std::stoi(m[0][4]);
       if (P.secondary) { err = "secondary solidification is not supported"; return false; }
@@ -1056,6 +1062,139 @@ int64_t run_tracking(Problem& P, int threads, int64_t max_steps, double budget_s
   return step + 1;
 }
 
+// Run::Stork (src/Run.cpp:711-1079): the Surface loop's frontier expansion over the top
+// layer, without solidification, then per liquid column a walk that finds its depth and
+// marks its layers liquid; every cell (8 grid points) whose count of liquid points changed
+// or is neither 0 nor 8 at this or the previous step gets a row: its index, the two step
+// times and the temperatures of its points at both.
+int64_t run_stork(Problem& P, int threads, int64_t max_steps, double budget_s) {
+  const double t_start = omp_get_wtime();
+  const int nx = P.nx, ny = P.ny, nz = P.nz;
+  const int cx = nx - 1, cy = ny - 1, cz = nz - 1;
+  const long cpnum = (long)cx * cy * cz;
+  std::vector<uint8_t> c_a(std::max(cpnum, 0L), 0), c_b(std::max(cpnum, 0L), 0);
+  std::vector<double> T_a(P.pnum, P.T0), T_b(P.pnum, P.T0);
+  std::vector<uint8_t> calc_a(P.pnum, 1), calc_b(P.pnum, 1), is_liq(P.pnum, 0);
+  std::vector<long> liq, reset;
+  std::vector<int> depths((size_t)nx * ny, 0);
+  Nodes N, Nlast;
+  double t = 0.0;
+  int64_t itert = 0;
+  while (true) {
+    std::vector<uint8_t>& c_prev = (itert % 2) ? c_a : c_b;
+    std::vector<uint8_t>& c_cur = (itert % 2) ? c_b : c_a;
+    std::vector<double>& T_prev = (itert % 2) ? T_a : T_b;
+    std::vector<double>& T_cur = (itert % 2) ? T_b : T_a;
+    std::vector<uint8_t>& calc_prev = (itert % 2) ? calc_a : calc_b;
+    std::vector<uint8_t>& calc_cur = (itert % 2) ? calc_b : calc_a;
+    std::fill(c_cur.begin(), c_cur.end(), 0);
+    std::fill(calc_cur.begin(), calc_cur.end(), 0);
+    std::fill(is_liq.begin(), is_liq.end(), 0);
+    for (long p : reset) { P.T_last[p] = P.T[p]; P.calc[p] = 0; }
+    reset.clear();
+    const std::vector<long> last_liq = liq;
+    liq.clear();
+    make_nodes(P, t, false, N);
+    for (long p : last_liq) {                                   // re-test last step's liquid points
+      T_cur[p] = eval_set(P, N, p);
+      calc_cur[p] = 1;
+      reset.push_back(p);
+      if (T_cur[p] >= P.TL) liq.push_back(p);
+      else depths[(size_t)pi_(P, p) * ny + pj_(P, p)] = 0;
+    }
+    std::vector<long> test = liq;
+    if (itert && t < P.end_time + P.dt) {
+      std::vector<long> seeds;
+      beam_trace(P, t - P.dt, t, seeds);
+      for (long p : seeds) {
+        reset.push_back(p);
+        if (calc_cur[p] == 0) {
+          T_cur[p] = eval_set(P, N, p);
+          calc_cur[p] = 1;
+          if (T_cur[p] >= P.TL) { test.push_back(p); liq.push_back(p); }
+        }
+      }
+    }
+    while (!test.empty()) {                                     // frontier expansion, top layer
+      std::vector<long> next;
+      for (long p : test) {
+        const int i = pi_(P, p), j = pj_(P, p), k = pk_(P, p);
+        for (int di = 0; di < 3; ++di) for (int dj = 0; dj < 3; ++dj) {
+          const int ni = i + di - 1, nj = j + dj - 1;
+          if (ni < 0 || ni > nx - 1 || nj < 0 || nj > ny - 1) continue;
+          const long q = pid(P, ni, nj, k);
+          if (P.calc[q]) continue;
+          T_cur[q] = eval_set(P, N, q);
+          calc_cur[q] = 1;
+          if (T_cur[q] >= P.TL) { liq.push_back(q); next.push_back(q); }
+          reset.push_back(q);
+        }
+      }
+      test.swap(next);
+    }
+    for (long p : liq) {                                        // depths (src/Run.cpp:909-956)
+      const int i = pi_(P, p), j = pj_(P, p);
+      const size_t dn = (size_t)i * ny + j;
+      int depth = depths[dn];
+      bool deeper = false;
+      while (true) {
+        depth++;
+        if (depth == nz) break;
+        const long q = pid(P, i, j, nz - 1 - depth);
+        T_cur[q] = sum_T(P, N, q);
+        calc_cur[q] = 1;
+        if (!(T_cur[q] >= P.TL)) break;
+        deeper = true;
+      }
+      while (true) {
+        depth--;
+        if (depth == 0 || deeper) break;
+        const long q = pid(P, i, j, nz - 1 - depth);
+        T_cur[q] = sum_T(P, N, q);
+        calc_cur[q] = 1;
+        if (T_cur[q] >= P.TL) break;
+      }
+      if (depth == nz - 1) depth--;
+      depths[dn] = depth;
+      for (int d = 0; d <= depth; ++d) is_liq[pid(P, i, j, nz - 1 - d)] = 1;
+    }
+    std::vector<long> relevant;
+    if (!last_liq.empty() || !liq.empty()) {
+      for (long c = 0; c < cpnum; ++c) {
+        const int ci = (int)((c / cy) / cz), cj = (int)((c / cz) % cy), ck = (int)(c % cz);
+        int n = 0;
+        for (int di = 0; di < 2; ++di) for (int dj = 0; dj < 2; ++dj) for (int dk = 0; dk < 2; ++dk)
+          n += is_liq[pid(P, ci + di, cj + dj, ck + dk)];
+        c_cur[c] = (uint8_t)n;
+        if (c_cur[c] != c_prev[c] || c_prev[c] % 8 || c_cur[c] % 8) relevant.push_back(c);
+      }
+    }
+    for (long c : relevant) {
+      const int ci = (int)((c / cy) / cz), cj = (int)((c / cz) % cy), ck = (int)(c % cz);
+      P.rrdf_idx.push_back((uint32_t)ci); P.rrdf_idx.push_back((uint32_t)cj); P.rrdf_idx.push_back((uint32_t)ck);
+      P.rrdf_t.push_back(t - P.dt); P.rrdf_t.push_back(t);
+      double Ts[16];
+      int n = 0;
+      for (int di = 0; di < 2; ++di) for (int dj = 0; dj < 2; ++dj) for (int dk = 0; dk < 2; ++dk) {
+        const long p = pid(P, ci + di, cj + dj, ck + dk);
+        if (calc_prev[p] == 0) { calc_prev[p] = 1; T_prev[p] = sum_T(P, Nlast, p); }
+        if (calc_cur[p] == 0) { calc_cur[p] = 1; T_cur[p] = sum_T(P, N, p); }
+        Ts[n] = T_prev[p];
+        Ts[n + 8] = T_cur[p];
+        ++n;
+      }
+      P.rrdf_T.insert(P.rrdf_T.end(), Ts, Ts + 16);
+    }
+    if (finished(P, t, (long)liq.size())) break;
+    t += P.dt; ++itert;
+    Nlast = N;
+    if (max_steps > 0 && itert >= max_steps) return itert;
+    if (budget_s > 0 && omp_get_wtime() - t_start > budget_s) return itert;
+  }
+  (void)threads;
+  return itert + 1;
+}
+
 }  // namespace
 
 // ====================================================================== C API
@@ -1120,6 +1259,7 @@ int64_t or_solidify_budget(void* h, int threads, int64_t max_steps, double budge
   if (threads <= 0) threads = omp_get_max_threads();
   if (P.mode != 1) return -1;
   if (P.tracking == TRACK_NONE) return run_notracking(P, threads, max_steps, budget_s);
+  if (P.tracking == TRACK_STORK) return run_stork(P, threads, max_steps, budget_s);
   return run_tracking(P, threads, max_steps, budget_s);
 }
 
@@ -1150,6 +1290,17 @@ int or_field(void* h, const char* name, double* out) {
 }
 
 int64_t or_pairs(void* h) { return ((Problem*)h)->pairs.load(); }
+
+int64_t or_rrdf(void* h, uint32_t* idx, double* ts, double* Ts, int64_t cap) {
+  const Problem& P = *(Problem*)h;
+  const int64_t n = (int64_t)P.rrdf_t.size() / 2;
+  for (int64_t r = 0; r < std::min(n, cap); ++r) {
+    for (int c = 0; c < 3; ++c) idx[3 * r + c] = P.rrdf_idx[3 * r + c];
+    for (int c = 0; c < 2; ++c) ts[2 * r + c] = P.rrdf_t[2 * r + c];
+    for (int c = 0; c < 16; ++c) Ts[16 * r + c] = P.rrdf_T[16 * r + c];
+  }
+  return n;
+}
 
 void or_solid_fields(void* h, int64_t p, double tsol, double* out) { solid_fields(*(Problem*)h, (long)p, tsol, out); }
 

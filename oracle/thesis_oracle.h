@@ -69,6 +69,11 @@ void  or_solid_fields_many(void* h, const int64_t* pts, const double* tsol, int6
 uint64_t or_schedule(void* h, double t, int is_sol);
 void  or_schedule_many(void* h, const double* t, int64_t n, int is_sol, uint64_t* out, int threads);
 
+/* After a Stork run (Tracking Stork): the doubly reduced data, rows in the reference's
+ * single-thread order (step, then cell): per row the cell index (3), the two step times (2)
+ * and the 16 vertex temperatures.  Returns the row count; copies at most cap rows. */
+int64_t or_rrdf(void* h, uint32_t* idx, double* ts, double* Ts, int64_t cap);
+
 /* Point x node pairs evaluated since load (temperature sums + gradient sums). */
 int64_t or_pairs(void* h);
 

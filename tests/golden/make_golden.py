@@ -19,8 +19,14 @@ own process (the reference keeps function-static state).  The fixtures hold:
   a small Snapshots deck and a small Solidification deck, byte for byte: ``names`` and
   ``file<i>`` (the file's bytes).
 
-``python tests/golden/make_golden.py csv`` (or ``comp``) regenerates only the csv (or the
-path-compression) fixtures.
+* ``rrdf_<deck>.npz`` - a whole Stork run (Tracking Stork): the row count, the number of
+  steps with rows and a SHA-256 digest of the doubly reduced data (cell indices, step
+  times, vertex temperatures; the reference run with one thread, so rows come in cell
+  order within a step); the first deck's fixture also holds the reference's own
+  ``<name>.RRDF.csv`` (Grid::Output_RRDF_csv) byte for byte.
+
+``python tests/golden/make_golden.py csv`` (or ``comp``, ``rrdf``) regenerates only the csv
+(or the path-compression, the Stork) fixtures.
 """
 from __future__ import annotations
 
@@ -68,6 +74,21 @@ if "csv" in job:
     L.ref_simulate(h)
     if str(job["csv"]) == "Solidification":
         L.ref_output(h, b"Solidification.Final")
+    names = sorted(os.listdir("Data"))
+    out["names"] = np.array(names)
+    for i, nm in enumerate(names):
+        with open(os.path.join("Data", nm), "rb") as f:
+            out[f"file{i}"] = np.frombuffer(f.read(), dtype=np.uint8)
+if "rrdf" in job:
+    import os
+    L.ref_rrdf.restype = ctypes.c_int64
+    L.ref_simulate(h)
+    n = L.ref_rrdf(h, None, None, None, ctypes.c_int64(0))
+    idx = np.zeros((n, 3), dtype=np.uint32); ts = np.zeros((n, 2)); Ts = np.zeros((n, 16))
+    L.ref_rrdf(h, idx.ctypes.data_as(ctypes.c_void_p), ts.ctypes.data_as(ctypes.c_void_p),
+               Ts.ctypes.data_as(ctypes.c_void_p), ctypes.c_int64(n))
+    out.update(idx=idx, ts=ts, Ts=Ts)
+    L.ref_output_rrdf(h, b"RRDF")
     names = sorted(os.listdir("Data"))
     out["names"] = np.array(names)
     for i, nm in enumerate(names):
@@ -135,6 +156,38 @@ RUNS = {"small_surface": ("small_surface", "Surface"), "small_volume": ("small_s
 
 
 CSV_DECKS = ("csv_snapshot", "small_multibeam")
+# Stork runs (Tracking Stork, src/Run.cpp:711-1079): the doubly reduced data; the first deck's
+# fixture also holds the reference's RRDF file
+RRDF_DECKS = ("small_stork", "surface_stork")
+
+
+def rrdf_deck(name):
+    """The deck each rrdf_<name>.npz fixture was made from."""
+    if name == "surface_stork":
+        d = decks.small_surface("Stork")
+        d.name = "surface_stork"
+        return d
+    return decks.small_stork()
+
+
+def rrdf_digest(idx, ts, Ts):
+    """SHA-256 of the rows: the index, time and temperature arrays' little-endian bytes."""
+    import hashlib
+    h = hashlib.sha256()
+    for a, dt in ((idx, "<u4"), (ts, "<f8"), (Ts, "<f8")):
+        h.update(np.ascontiguousarray(a, dtype=dt).tobytes())
+    return h.hexdigest()
+
+
+def rrdf_fixture(deck, scratch, with_file):
+    r = run_ref(deck, {"rrdf": np.asarray(1)}, scratch)
+    out = {"rows": np.int64(r["idx"].shape[0]), "digest": np.asarray(rrdf_digest(r["idx"], r["ts"], r["Ts"])),
+           "steps": np.int64(np.unique(r["ts"][:, 1]).size)}
+    if with_file:
+        out["names"] = r["names"]
+        out.update({k: v for k, v in r.items() if k.startswith("file")})
+    np.savez_compressed(os.path.join(HERE, f"rrdf_{deck.name}.npz"), **out)
+    return out
 
 
 def csv_deck(name):
@@ -192,6 +245,12 @@ def main():
                 run_fixture(run_deck(tag), scratch, tag)
         print("compression fixtures written to", HERE)
         return
+    if sys.argv[1:] == ["rrdf"]:
+        with tempfile.TemporaryDirectory() as scratch:
+            for i, name in enumerate(RRDF_DECKS):
+                rrdf_fixture(rrdf_deck(name), scratch, i == 0)
+        print("rrdf fixtures written to", HERE)
+        return
     if sys.argv[1:] == ["csv"]:
         with tempfile.TemporaryDirectory() as scratch:
             for name in CSV_DECKS:
@@ -209,6 +268,8 @@ def main():
             run_fixture(run_deck(tag), scratch, tag)
         for name in CSV_DECKS:
             csv_fixture(csv_deck(name), scratch)
+        for i, name in enumerate(RRDF_DECKS):
+            rrdf_fixture(rrdf_deck(name), scratch, i == 0)
     print("golden fixtures written to", HERE)
 
 

@@ -38,6 +38,8 @@ def load():
         L.or_schedule.argtypes = [vp, ctypes.c_double, ctypes.c_int]
         L.or_schedule.restype = ctypes.c_uint64
         L.or_schedule_many.argtypes = [vp, vp, ctypes.c_int64, ctypes.c_int, vp, ctypes.c_int]
+        L.or_rrdf.argtypes = [vp, vp, vp, vp, ctypes.c_int64]
+        L.or_rrdf.restype = ctypes.c_int64
         L.or_pairs.argtypes = [vp]
         L.or_pairs.restype = ctypes.c_int64
         _lib = L
@@ -124,6 +126,16 @@ class Oracle:
         _lib.or_schedule_many(self.h, tt.ctypes.data_as(ctypes.c_void_p), tt.size, int(is_sol),
                               out.ctypes.data_as(ctypes.c_void_p), threads)
         return out
+
+    def rrdf(self):
+        """After a Stork run: (idx (n, 3) uint32, ts (n, 2), Ts (n, 16)), the rows in the
+        reference's single-thread order."""
+        n = _lib.or_rrdf(self.h, None, None, None, 0)
+        idx = np.zeros((n, 3), dtype=np.uint32)
+        ts, Ts = np.zeros((n, 2)), np.zeros((n, 16))
+        _lib.or_rrdf(self.h, idx.ctypes.data_as(ctypes.c_void_p), ts.ctypes.data_as(ctypes.c_void_p),
+                     Ts.ctypes.data_as(ctypes.c_void_p), n)
+        return idx, ts, Ts
 
     @property
     def pairs(self):

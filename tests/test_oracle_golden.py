@@ -71,3 +71,20 @@ def test_oracle_solidification_time_budget(oracle, tmp_path):
     ref = oracle(path)
     ref.solidify(threads=2)
     assert np.array_equal(ample.field("tSol"), ref.field("tSol"))
+
+
+@pytest.mark.parametrize("name", make_golden.RRDF_DECKS)
+def test_oracle_stork_rows_match_reference(name, oracle, tmp_path):
+    """A whole Stork run (Run::Stork, src/Run.cpp:711-1079): the oracle's doubly reduced data
+    equals the reference's bit for bit (same rows in the same order, same index, time and
+    temperature words)."""
+    g = _load(f"rrdf_{name}.npz")
+    deck = make_golden.rrdf_deck(name)
+    o = oracle(deck.write(str(tmp_path / name)))
+    o.solidify(threads=4)
+    idx, ts, Ts = o.rrdf()
+    assert idx.shape[0] == int(g["rows"])
+    assert np.unique(ts[:, 1]).size == int(g["steps"])
+    assert make_golden.rrdf_digest(idx, ts, Ts) == str(g["digest"])
+    if name == "small_stork":                      # the pool reaches the bottom cell layer
+        assert idx[:, 2].min() == 0
