@@ -45,7 +45,7 @@ EXPORTED = ("th_ctx_create_from_deck", "th_ctx_destroy", "th_last_error", "th_ge
             "th_batch_snapshot_device", "th_batch_set_tile_shape", "th_batch_autotune", "th_batch_pairs",
             "th_adj_create", "th_adj_destroy", "th_adj_last_error", "th_adj_num_params", "th_adj_params",
             "th_adj_host_nodes", "th_adj_forward", "th_adj_backward", "th_calc_T_times_device",
-            "th_device_rates")
+            "th_device_rates", "th_rrdf")
 
 
 class ThesisError(RuntimeError):
@@ -124,6 +124,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.th_adj_forward.argtypes = [vp, vp, vp]
     L.th_adj_backward.argtypes = [vp, vp, vp]
     L.th_device_rates.argtypes = [vp]
+    L.th_rrdf.argtypes = [vp, vp, vp, vp, c_i64, ctypes.POINTER(c_i64)]
     _lib = L
     return L
 
@@ -253,15 +254,26 @@ class Simulation:
 
     def run_stats(self) -> Dict[str, float]:
         """Device time (ms) and counters of the solidification loop so far."""
-        out = np.zeros(31)
-        self._check(self._lib.th_run_stats(self._ctx, _ptr(out), 31))
+        out = np.zeros(33)
+        self._check(self._lib.th_run_stats(self._ctx, _ptr(out), 33))
         keys = ("ms_nodes", "ms_track", "ms_solidify", "windows", "records", "max_items", "steps", "slot_cap",
                 "ms_device", "pairs_solidify", "pairs_total", "loop_ms_work", "loop_ms_barrier", "loop_items",
                 "loop_item_clocks", "loop_wait_clocks", "loop_depth_sum", "loop_steps", "loop_evals",
                 "loop_eval_clocks", "loop_ms_start0", "loop_ms_start1", "loop_ms_start2", "loop_ms_start3",
                 "loop_ms_end0", "loop_ms_end1", "loop_ms_end2", "loop_ms_end3", "loop_eval_nodes",
-                "records_redone_fp64", "guarded_decisions")
+                "records_redone_fp64", "guarded_decisions", "ms_rrdf", "rrdf_rows")
         return dict(zip(keys, out.tolist()))
+
+    def rrdf(self):
+        """After solidify() on a Stork deck: the doubly reduced data, (idx (n, 3) uint32,
+        ts (n, 2), Ts (n, 16)) - per row the cell index, the previous and current step time
+        and the 8 vertex temperatures at each (Grid::get_RRDF_*, src/Grid.h:368-370)."""
+        n = ctypes.c_int64()
+        self._check(self._lib.th_rrdf(self._ctx, None, None, None, 0, ctypes.byref(n)))
+        idx = np.zeros((n.value, 3), dtype=np.uint32)
+        ts, Ts = np.zeros((n.value, 2)), np.zeros((n.value, 16))
+        self._check(self._lib.th_rrdf(self._ctx, _ptr(idx), _ptr(ts), _ptr(Ts), n.value, ctypes.byref(n)))
+        return idx, ts, Ts
 
     def field(self, name: str) -> np.ndarray:
         out = np.empty(self.pnum)

@@ -35,6 +35,31 @@ bool th_write_csv(const HostProblem& hp, const std::string& tag, const std::vect
   return ok;
 }
 
+// Stork's doubly reduced data (Grid::Output_RRDF_csv, src/Grid.cpp:203-238): the header,
+// then per row the cell index, the two step times and the 8 + 8 vertex temperatures.
+bool th_write_rrdf_csv(const HostProblem& hp, const std::string& tag, const uint32_t* idx, const double* ts,
+                       const double* Ts, int64_t rows, std::string& err) {
+  const std::string dir = th_data_dir(hp);
+  mkdir(dir.c_str(), 0777);
+  const std::string path = dir + "/" + hp.name + "." + tag + ".csv";
+  FILE* f = std::fopen(path.c_str(), "w");
+  if (!f) { err = "cannot write " + path; return false; }
+  std::vector<char> buf(1 << 20);
+  std::setvbuf(f, buf.data(), _IOFBF, buf.size());
+  std::fputs("x,y,z,t_prev,t_cur", f);
+  for (int t = 0; t < 2; ++t)
+    for (int v = 0; v < 8; ++v) std::fprintf(f, ",T%d%d%d_%s", v >> 2, (v >> 1) & 1, v & 1, t ? "cur" : "prev");
+  std::fputc('\n', f);
+  for (int64_t r = 0; r < rows; ++r) {
+    std::fprintf(f, "%u,%u,%u,%g,%g", idx[3 * r], idx[3 * r + 1], idx[3 * r + 2], ts[2 * r], ts[2 * r + 1]);
+    for (int v = 0; v < 16; ++v) std::fprintf(f, ",%g", Ts[16 * r + v]);
+    std::fputc('\n', f);
+  }
+  const bool ok = std::fclose(f) == 0;
+  if (!ok) err = "error writing " + path;
+  return ok;
+}
+
 void th_grid_coords(const HostProblem& hp, std::vector<double>& x, std::vector<double>& y, std::vector<double>& z) {
   const int gx = (uint16_t)hp.nx, gy = (uint16_t)hp.ny, gz = (uint16_t)hp.nz;
   const double hx = gx > 1 ? (hp.xmax - hp.xmin) / (gx - 1) : 0.0;

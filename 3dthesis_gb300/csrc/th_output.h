@@ -1,4 +1,5 @@
 #pragma once
+#include <cstdint>
 #include <string>
 #include <vector>
 
@@ -8,6 +9,10 @@ std::string th_data_dir(const HostProblem& hp);
 // Writes <deck dir>/Data/<name>.<tag>.csv; rows only where flag[p] (all rows if flag is null).
 bool th_write_csv(const HostProblem& hp, const std::string& tag, const std::vector<std::string>& names,
                   const std::vector<const double*>& cols, const unsigned char* flag, std::string& err);
+// Writes <deck dir>/Data/<name>.<tag>.csv with Stork's rows (3 indices, 2 times, 16
+// temperatures each).
+bool th_write_rrdf_csv(const HostProblem& hp, const std::string& tag, const uint32_t* idx, const double* ts,
+                       const double* Ts, int64_t rows, std::string& err);
 // Point coordinates exactly as the reference's Grid getters compute them.
 void th_grid_coords(const HostProblem& hp, std::vector<double>& x, std::vector<double>& y, std::vector<double>& z);
 std::string th_zero_pad(int v, int width);

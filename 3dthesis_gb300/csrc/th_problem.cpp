@@ -141,6 +141,7 @@ int parse_tracking(const std::string& s, bool& ok) {
   if (s.empty() || s == "None") return TH_TRACK_NONE;
   if (s == "Volume") return TH_TRACK_VOLUME;
   if (s == "Surface") return TH_TRACK_SURFACE;
+  if (s == "Stork") return TH_TRACK_STORK;
   ok = false;
   return TH_TRACK_NONE;
 }

@@ -10,7 +10,7 @@
 #define TH_MAX_BEAMS 16
 #define TH_MAX_IMAGES 64
 
-enum { TH_TRACK_NONE = 0, TH_TRACK_VOLUME = 1, TH_TRACK_SURFACE = 2 };
+enum { TH_TRACK_NONE = 0, TH_TRACK_VOLUME = 1, TH_TRACK_SURFACE = 2, TH_TRACK_STORK = 3 };
 
 // One path segment (src/DataStructs.h:42-48): end point, power modulation, speed or dwell,
 // end time.  mode 0 = line, 1 = spot.

@@ -7,7 +7,9 @@
 // queued liquid -> solid records are solidified in bulk.  For the tracking modes the three
 // overlap: while the tracking kernel runs window w on the context's stream, a second
 // stream builds the node lists of window w + 1 and solidifies the records of window w - 1
-// (two node windows and two record buffers, ordered by events).
+// (two node windows and two record buffers, ordered by events).  Stork logs each launch's
+// liquid lists instead of records; the aux stream turns a finished launch's log into the
+// doubly reduced data while the next launch runs.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -68,6 +70,28 @@ struct RunState {
   cudaEvent_t ev_run[2] = {nullptr, nullptr};
   double ms_nodes = 0, ms_track = 0, ms_solid = 0, ms_device = 0;
   long long windows = 0, records = 0;
+  // Stork: per buffer the launch's log of liquid lists and their offsets, the launch's first
+  // step and steps run (0: nothing pending); the rows on the device and their capacity
+  int2* rlog[2] = {nullptr, nullptr};
+  int* rlog_off[2] = {nullptr, nullptr};
+  int rr_k0[2] = {0, 0}, rr_n[2] = {0, 0};
+  int* h_off = nullptr;          // pinned: one log's offsets
+  int* h_counts = nullptr;       // pinned: per step rows, vertex values
+  long long* h_row_base = nullptr;   // pinned
+  int* d_counts = nullptr;
+  long long* d_row_base = nullptr;
+  int* d_rerr = nullptr;
+  int* d_rscratch = nullptr;
+  size_t rscratch_ints = 0;
+  double* d_rvals = nullptr;
+  size_t rvals_doubles = 0;
+  uint32_t* r_idx = nullptr;
+  double* r_ts = nullptr;
+  double* r_Ts = nullptr;
+  long long rows = 0, rows_cap = 0;
+  cudaEvent_t ev_rr[2] = {nullptr, nullptr};   // around the latest pass
+  bool rr_timed = true;
+  double ms_rrdf = 0;
 };
 
 void th_release_run_state(th_ctx* ctx) {
@@ -83,6 +107,12 @@ void th_release_run_state(th_ctx* ctx) {
   cudaFree(r->d_field);
   cudaFree(r->d_axis);
   if (r->h_err) cudaFreeHost(r->h_err);
+  if (r->h_off) cudaFreeHost(r->h_off);
+  if (r->h_counts) cudaFreeHost(r->h_counts);
+  if (r->h_row_base) cudaFreeHost(r->h_row_base);
+  cudaFree(r->d_rscratch); cudaFree(r->d_rvals);
+  cudaFree(r->r_idx); cudaFree(r->r_ts); cudaFree(r->r_Ts);
+  for (int e = 0; e < 2; ++e) if (r->ev_rr[e]) cudaEventDestroy(r->ev_rr[e]);
   for (int b = 0; b < 2; ++b)
     for (int e = 0; e < 2; ++e) {
       if (r->ev_trk[b][e]) cudaEventDestroy(r->ev_trk[b][e]);
@@ -148,8 +178,22 @@ th_status init_run(th_ctx* ctx) {
   if (hp.o_eqFrac) ALLOC(S.eqFrac, n, 0);
   if (hp.tracking == TH_TRACK_SURFACE) {
     if (hp.o_depth) ALLOC(S.depth, n, 0);
-    ALLOC(S.depths, ncol, 0);
     ALLOC(S.depth_max, ncol, 0);
+  }
+  if (hp.tracking == TH_TRACK_SURFACE || hp.tracking == TH_TRACK_STORK) ALLOC(S.depths, ncol, 0);
+  const bool stork = hp.tracking == TH_TRACK_STORK;
+  if (stork) {
+    // a log holds the lists of one launch (a list has at most one entry per column); the
+    // launch stops before less than one list's room is left
+    S.rlog_step_max = (int)std::min<size_t>(ncol, (size_t)INT_MAX / 4);
+    S.rlog_cap = (int)std::min<size_t>(std::max<size_t>((size_t)1 << 20, 4 * ncol), (size_t)INT_MAX / 2);
+    for (int b = 0; b < 2; ++b) {
+      ALLOC(r->rlog[b], (size_t)S.rlog_cap, 0);
+      ALLOC(r->rlog_off[b], (size_t)kWindowTrack + 2, 0);
+    }
+    ALLOC(r->d_counts, 2 * (size_t)kWindowTrack, 0);
+    ALLOC(r->d_row_base, (size_t)kWindowTrack, 0);
+    ALLOC(r->d_rerr, 1, 0);
   }
   if (hp.tracking != TH_TRACK_NONE) {
     S.list_cap = (int)n;
@@ -164,14 +208,16 @@ th_status init_run(th_ctx* ctx) {
     }
     ALLOC(S.queue, (size_t)S.queue_cap, 0);
   }
-  S.rec_cap = kRecCap;
+  // Stork queues no records: its buffers stay token-sized
+  const int rec_alloc = stork ? 64 : kRecCap;
+  S.rec_cap = rec_alloc;
   // test knob of the failure path: record buffers this small overflow in one step (ERR_RECORDS)
   if (const char* env = std::getenv("THESIS_GB300_REC_CAP")) {
     const int v = std::atoi(env);
     if (v > 0) S.rec_cap = std::min(S.rec_cap, v);
   }
-  ALLOC(r->rec[0], (size_t)kRecCap, 0);
-  ALLOC(r->rec[1], (size_t)kRecCap, 0);
+  ALLOC(r->rec[0], (size_t)rec_alloc, 0);
+  ALLOC(r->rec[1], (size_t)rec_alloc, 0);
   // the FP64 redo of FP32 solidification (queue, scratch lists); compressing decks
   // solidify every record with the same kernel
   if (ctx->precision == TH_FP32_KAHAN || hp.compress) {
@@ -228,6 +274,19 @@ th_status init_run(th_ctx* ctx) {
   if ((st = th_cuda_check(ctx, cudaStreamCreateWithFlags(&r->aux, cudaStreamNonBlocking), "stream")) != TH_OK) return st;
   if ((st = th_cuda_check(ctx, cudaHostAlloc((void**)&r->h_err, 4 * sizeof(int), cudaHostAllocDefault), "host")) != TH_OK)
     return st;
+  if (stork) {
+    if ((st = th_cuda_check(ctx, cudaHostAlloc((void**)&r->h_off, (kWindowTrack + 2) * sizeof(int), cudaHostAllocDefault),
+                            "host")) != TH_OK)
+      return st;
+    if ((st = th_cuda_check(ctx, cudaHostAlloc((void**)&r->h_counts, 2 * kWindowTrack * sizeof(int), cudaHostAllocDefault),
+                            "host")) != TH_OK)
+      return st;
+    if ((st = th_cuda_check(ctx, cudaHostAlloc((void**)&r->h_row_base, kWindowTrack * sizeof(long long),
+                                               cudaHostAllocDefault), "host")) != TH_OK)
+      return st;
+    cudaEventCreate(&r->ev_rr[0]);
+    cudaEventCreate(&r->ev_rr[1]);
+  }
   for (int b = 0; b < 2; ++b) {
     cudaEventCreate(&r->win[b].gen0); cudaEventCreate(&r->win[b].gen1);
     for (int e = 0; e < 2; ++e) { cudaEventCreate(&r->ev_trk[b][e]); cudaEventCreate(&r->ev_sol[b][e]); }
@@ -359,6 +418,92 @@ th_status read_counters(th_ctx* ctx, RunState* r, TrackCounters* h) {
 
 void add_elapsed(double& acc, cudaEvent_t a, cudaEvent_t b);
 
+// Grows a device array to hold `need` elements, keeping the first `keep` (stream-ordered
+// copy on s; the old array is freed after it).
+template <class T>
+th_status grow(th_ctx* ctx, T** p, size_t need, size_t keep, cudaStream_t s) {
+  T* q = nullptr;
+  th_status st = th_cuda_check(ctx, cudaMalloc(&q, std::max<size_t>(need, 1) * sizeof(T)), "cudaMalloc");
+  if (st != TH_OK) return st;
+  if (*p && keep) {
+    st = th_cuda_check(ctx, cudaMemcpyAsync(q, *p, keep * sizeof(T), cudaMemcpyDeviceToDevice, s), "cudaMemcpyAsync");
+    if (st != TH_OK) { cudaFree(q); return st; }
+    cudaStreamSynchronize(s);
+  }
+  cudaFree(*p);
+  *p = q;
+  return TH_OK;
+}
+
+// Stork: the doubly reduced data of the launch that filled log b (its steps, the node lists
+// of window b), appended to the rows on stream s.  The host reads the log's offsets and then
+// the per-step counts on the way (s holds only this pass), so the rows land at offsets laid
+// out in step order and the buffers grow before the fill.
+th_status rrdf_buffer(th_ctx* ctx, RunState* r, int b, cudaStream_t s) {
+  const int n = r->rr_n[b];
+  r->rr_n[b] = 0;
+  if (n <= 0) return TH_OK;
+  th_status st = th_cuda_check(ctx, cudaMemcpyAsync(r->h_off, r->rlog_off[b], (n + 2) * sizeof(int), cudaMemcpyDeviceToHost,
+                                                    s), "copy");
+  if (st != TH_OK) return st;
+  if ((st = th_cuda_check(ctx, cudaStreamSynchronize(s), "rrdf")) != TH_OK) return st;
+  if (!r->rr_timed) { add_elapsed(r->ms_rrdf, r->ev_rr[0], r->ev_rr[1]); r->rr_timed = true; }
+  if (r->h_off[n + 1] == 0) return TH_OK;                          // no liquid in these steps
+  if (r->h_off[n + 1] > r->S.rlog_cap) return th_fail(ctx, TH_ERR_CAPACITY, "the Stork liquid-list log overflowed");
+  int nmax = 1;
+  for (int j = 0; j < n; ++j) nmax = std::max(nmax, r->h_off[j + 2] - r->h_off[j]);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = std::min(n, 2 * std::max(sms, 1));
+  const size_t per = th_rrdf_scratch_ints(nmax);
+  if ((size_t)blocks * per > r->rscratch_ints) {
+    if ((st = grow(ctx, &r->d_rscratch, (size_t)blocks * per, 0, s)) != TH_OK) return st;
+    r->rscratch_ints = (size_t)blocks * per;
+  }
+  RrdfBatch B{};
+  B.log = r->rlog[b]; B.off = r->rlog_off[b]; B.k0 = r->rr_k0[b]; B.nsteps = n; B.nmax = nmax;
+  B.counts = r->d_counts; B.row_base = r->d_row_base; B.scratch = r->d_rscratch; B.err = r->d_rerr;
+  cudaEventRecord(r->ev_rr[0], s);
+  th_launch_rrdf(ctx->dp, r->win[b].W, B, false, ctx->precision, blocks, s);
+  if ((st = th_cuda_check(ctx, cudaGetLastError(), "rrdf count")) != TH_OK) return st;
+  st = th_cuda_check(ctx, cudaMemcpyAsync(r->h_counts, r->d_counts, 2 * n * sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
+  if (st != TH_OK) return st;
+  if ((st = th_cuda_check(ctx, cudaStreamSynchronize(s), "rrdf count")) != TH_OK) return st;
+  long long total = 0;
+  int nv = 1;
+  for (int j = 0; j < n; ++j) {
+    r->h_row_base[j] = r->rows + total;
+    total += r->h_counts[2 * j];
+    nv = std::max(nv, r->h_counts[2 * j + 1]);
+  }
+  if (total == 0) { cudaEventRecord(r->ev_rr[1], s); r->rr_timed = false; return TH_OK; }
+  if (r->rows + total > r->rows_cap) {
+    const long long cap = std::max<long long>(r->rows + total, std::max<long long>(2 * r->rows_cap, 1 << 16));
+    if ((st = grow(ctx, &r->r_idx, 3 * (size_t)cap, 3 * (size_t)r->rows, s)) != TH_OK) return st;
+    if ((st = grow(ctx, &r->r_ts, 2 * (size_t)cap, 2 * (size_t)r->rows, s)) != TH_OK) return st;
+    if ((st = grow(ctx, &r->r_Ts, 16 * (size_t)cap, 16 * (size_t)r->rows, s)) != TH_OK) return st;
+    r->rows_cap = cap;
+  }
+  if ((size_t)blocks * 3 * nv > r->rvals_doubles) {
+    const size_t need = (size_t)blocks * 3 * std::max(nv, 4096);
+    if ((st = grow(ctx, &r->d_rvals, need, 0, s)) != TH_OK) return st;
+    r->rvals_doubles = need;
+  }
+  B.vals = r->d_rvals;
+  B.vals_cap = (int)(r->rvals_doubles / (3 * (size_t)blocks));
+  B.idx = r->r_idx; B.ts = r->r_ts; B.Ts = r->r_Ts;
+  st = th_cuda_check(ctx, cudaMemcpyAsync(r->d_row_base, r->h_row_base, n * sizeof(long long), cudaMemcpyHostToDevice, s),
+                     "copy");
+  if (st != TH_OK) return st;
+  th_launch_rrdf(ctx->dp, r->win[b].W, B, true, ctx->precision, blocks, s);
+  if ((st = th_cuda_check(ctx, cudaGetLastError(), "rrdf fill")) != TH_OK) return st;
+  cudaEventRecord(r->ev_rr[1], s);
+  r->rr_timed = false;
+  r->rows += total;
+  return TH_OK;
+}
+
 // Solidifies record buffer b (nrec records) on stream s, then empties it.  The previous
 // use of the buffer's events has completed by then (the tracking launch in between waited
 // for it), so its time is added first.
@@ -373,6 +518,7 @@ th_status solidify_buffer(th_ctx* ctx, RunState* r, int b, int nrec, cudaStream_
     if (st != TH_OK) return st;
   }
   th_status st = th_cuda_check(ctx, cudaMemsetAsync(&r->S.C->rec_n[b], 0, sizeof(int), s), "cudaMemsetAsync");
+  if (st == TH_OK && ctx->hp.tracking == TH_TRACK_STORK) st = rrdf_buffer(ctx, r, b, s);
   cudaEventRecord(r->ev_sol[b][1], s);
   r->records += nrec;
   return st;
@@ -404,6 +550,8 @@ th_status advance_tracking(th_ctx* ctx, int64_t stop_at) {
     TrackState S = r->S;
     S.rec = r->rec[b];
     S.rec_n = &r->S.C->rec_n[b];
+    S.rlog = r->rlog[b];
+    S.rlog_off = r->rlog_off[b];
     cudaEventRecord(r->ev_trk[b][0], ts);
     st = th_cuda_check(ctx, th_launch_track(ctx->dp, S, w.W, w.base, w.base + w.n, ctx->precision, r->S.rec_cap / 2, ts),
                        "cooperative launch");
@@ -433,6 +581,8 @@ th_status advance_tracking(th_ctx* ctx, int64_t stop_at) {
     r->max_items = std::max(r->max_items, h.max_items);
     const int k_new = h.step;
     if (k_new <= r->k && !h.done) return th_fail(ctx, TH_ERR_INVALID, "solidification loop made no progress");
+    r->rr_k0[b] = w.base;
+    r->rr_n[b] = ctx->hp.tracking == TH_TRACK_STORK ? k_new - w.base : 0;
     r->k = k_new;
     r->done = h.done != 0;
     if (r->done || r->k >= stop_at) break;
@@ -447,7 +597,7 @@ th_status advance_tracking(th_ctx* ctx, int64_t stop_at) {
   // drain: both record buffers, then wait for both streams
   for (int i = 0; i < 2; ++i) {
     const int bb = b ^ 1 ^ i;       // the older buffer first
-    if (pending_rec[bb] > 0) {
+    if (pending_rec[bb] > 0 || r->rr_n[bb] > 0) {
       cudaStreamWaitEvent(as, r->ev_trk[bb][1], 0);
       if ((st = solidify_buffer(ctx, r, bb, pending_rec[bb], as)) != TH_OK) return st;
       pending_rec[bb] = 0;
@@ -456,6 +606,12 @@ th_status advance_tracking(th_ctx* ctx, int64_t stop_at) {
   if ((st = th_cuda_check(ctx, cudaStreamSynchronize(as), "solidify")) != TH_OK) return st;
   for (int i = 0; i < 2; ++i)
     if (!r->sol_timed[i]) { add_elapsed(r->ms_solid, r->ev_sol[i][0], r->ev_sol[i][1]); r->sol_timed[i] = true; }
+  if (!r->rr_timed) { add_elapsed(r->ms_rrdf, r->ev_rr[0], r->ev_rr[1]); r->rr_timed = true; }
+  if (r->d_rerr) {
+    int e = 0;
+    if ((st = th_cuda_check(ctx, cudaMemcpy(&e, r->d_rerr, sizeof(int), cudaMemcpyDeviceToHost), "copy")) != TH_OK) return st;
+    if (e) return th_fail(ctx, TH_ERR_CAPACITY, "a Stork step needed more vertex values than laid out");
+  }
   return th_cuda_check(ctx, cudaStreamSynchronize(ts), "solidification");
 }
 
@@ -597,6 +753,7 @@ th_status th_run_reset(th_ctx* ctx) {
   r->k = 0; r->done = false; r->max_items = 0;
   r->sol_timed[0] = r->sol_timed[1] = true;
   r->ms_nodes = r->ms_track = r->ms_solid = r->ms_device = 0;
+  r->rows = 0; r->rr_n[0] = r->rr_n[1] = 0; r->rr_timed = true; r->ms_rrdf = 0;
   r->windows = r->records = 0;
   st = th_cuda_check(ctx, cudaMemsetAsync(ctx->d_pairs, 0, 2 * sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
   if (st != TH_OK) return st;
@@ -614,15 +771,16 @@ th_status th_run_stats(th_ctx* ctx, double* out, int32_t n) {
     st = th_cuda_check(ctx, cudaMemcpy(prof, r->S.C->prof, sizeof(prof), cudaMemcpyDeviceToHost), "cudaMemcpy");
     if (st != TH_OK) return st;
   }
-  const double v[31] = {r ? r->ms_nodes : 0, r ? r->ms_track : 0, r ? r->ms_solid : 0, r ? (double)r->windows : 0,
+  const double v[33] = {r ? r->ms_nodes : 0, r ? r->ms_track : 0, r ? r->ms_solid : 0, r ? (double)r->windows : 0,
                         r ? (double)r->records : 0, r ? (double)r->max_items : 0, r ? (double)r->k : 0,
                         r ? (double)r->slot_cap : 0, r ? r->ms_device : 0, (double)pairs[1],
                         (double)pairs[0], prof[0] * 1e-6, prof[1] * 1e-6, (double)prof[2], (double)prof[3],
                         (double)prof[4], (double)prof[5], (double)prof[6], (double)prof[7], (double)prof[8],
                         prof[10] * 1e-6, prof[11] * 1e-6, prof[12] * 1e-6, prof[13] * 1e-6,
                         prof[14] * 1e-6, prof[15] * 1e-6, prof[16] * 1e-6, prof[17] * 1e-6,
-                        (double)prof[9], (double)prof[18], (double)prof[19]};
-  for (int i = 0; i < n && i < 31; ++i) out[i] = v[i];
+                        (double)prof[9], (double)prof[18], (double)prof[19],
+                        r ? r->ms_rrdf : 0, r ? (double)r->rows : 0};
+  for (int i = 0; i < n && i < 33; ++i) out[i] = v[i];
   return TH_OK;
 }
 
@@ -647,6 +805,28 @@ th_status th_field(th_ctx* ctx, const char* name, double* out) {
   const int id = field_id(f);
   if (id < 0) return th_fail(ctx, TH_ERR_INVALID, "unknown field " + f);
   return fetch_field(ctx, id, out);
+}
+
+th_status th_rrdf(th_ctx* ctx, uint32_t* idx, double* ts, double* Ts, int64_t cap, int64_t* rows) {
+  if (!ctx) return th_fail(ctx, TH_ERR_INVALID, "null context");
+  if (ctx->hp.tracking != TH_TRACK_STORK) return th_fail(ctx, TH_ERR_INVALID, "the deck does not use Stork tracking");
+  th_status st = th_cuda_check(ctx, cudaSetDevice(ctx->device), "cudaSetDevice");
+  if (st != TH_OK) return st;
+  const RunState* r = ctx->run;
+  const int64_t n = r ? r->rows : 0;
+  if (rows) *rows = n;
+  const int64_t m = std::min<int64_t>(std::max<int64_t>(cap, 0), n);
+  if (m == 0) return TH_OK;
+  if (idx && (st = th_cuda_check(ctx, cudaMemcpy(idx, r->r_idx, 3 * m * sizeof(uint32_t), cudaMemcpyDeviceToHost),
+                                 "cudaMemcpy")) != TH_OK)
+    return st;
+  if (ts && (st = th_cuda_check(ctx, cudaMemcpy(ts, r->r_ts, 2 * m * sizeof(double), cudaMemcpyDeviceToHost),
+                                "cudaMemcpy")) != TH_OK)
+    return st;
+  if (Ts && (st = th_cuda_check(ctx, cudaMemcpy(Ts, r->r_Ts, 16 * m * sizeof(double), cudaMemcpyDeviceToHost),
+                                "cudaMemcpy")) != TH_OK)
+    return st;
+  return TH_OK;
 }
 
 th_status th_simulate(th_ctx* ctx) {
@@ -674,6 +854,20 @@ th_status th_simulate(th_ctx* ctx) {
   th_status st = th_cuda_check(ctx, cudaSetDevice(ctx->device), "cudaSetDevice");
   if (st != TH_OK) return st;
   if (!ctx->run && (st = init_run(ctx)) != TH_OK) return st;
+  if (hp.tracking == TH_TRACK_STORK) {
+    // Stork writes its doubly reduced data in place of Solidification.Final and no
+    // intermediate files (bin/Main.cpp:104-111, src/Run.cpp:711-1079)
+    while (!ctx->run->done)
+      if ((st = advance(ctx, (int64_t)INT_MAX - 1)) != TH_OK) return st;
+    const int64_t n = ctx->run->rows;
+    std::vector<uint32_t> idx(3 * (size_t)n);
+    std::vector<double> ts(2 * (size_t)n), Ts(16 * (size_t)n);
+    int64_t got = 0;
+    if ((st = th_rrdf(ctx, idx.data(), ts.data(), Ts.data(), n, &got)) != TH_OK) return st;
+    std::string err;
+    if (!th_write_rrdf_csv(hp, "RRDF", idx.data(), ts.data(), Ts.data(), n, err)) return th_fail(ctx, TH_ERR_IO, err);
+    return TH_OK;
+  }
   // intermediate outputs every OutputFrequency steps (src/Run.cpp:446-458, 553-565, 689-701)
   const std::string prefix = hp.tracking == TH_TRACK_SURFACE ? "Solidification." : "";
   const int64_t freq = hp.out_freq;

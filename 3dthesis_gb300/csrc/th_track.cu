@@ -27,16 +27,6 @@ using namespace thdev;
 
 namespace {
 
-__device__ __forceinline__ NodeBufView slot_view(const NodeWindow& w, int slot) {
-  NodeBufView v = w.nb;
-  const size_t off = (size_t)slot * w.slot_cap;
-  v.x += off; v.y += off; v.z += off; v.ipx += off; v.ipy += off; v.ipz += off; v.dtau += off; v.amp += off;
-  v.kx += off; v.ky += off; v.kz += off; v.w += off; v.xh += off; v.xl += off; v.yh += off; v.yl += off;
-  v.zh += off; v.zl += off;
-  v.cap = w.slot_cap;
-  return v;
-}
-
 // One slot's node arrays as two base pointers: a window keeps each of its eight double
 // fields (x, y, z, ipx, ipy, ipz, dtau, amp) and ten float fields (kx, ky, kz, w, xh, xl, yh,
 // yl, zh, zl) in one array of `stride` entries, those arrays `stride` apart, slots one after
@@ -415,6 +405,8 @@ struct StepCtx {
   int* lo_n;
   QueueCounters* qc;
   const float2* ax;        // grid axis table (hi, lo) (shared memory when it fits)
+  int log_out;             // Stork: where this step's liquid list starts in the launch's log
+  int log_j;               // and which of the launch's lists it is
 };
 
 __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
@@ -575,6 +567,13 @@ __device__ __forceinline__ void push_liquid(const TrackState& S, const StepCtx& 
   if (i < S.list_cap) X.Lo[i] = make_int2(p, depth); else atomicOr(S.err, ERR_LISTS);
 }
 
+// Stork: the liquid point also joins the launch's log of liquid lists (the doubly reduced
+// data is built from it after the launch), at the same index as in the next step's list.
+__device__ __forceinline__ void log_liquid(const TrackState& S, const StepCtx& X, int i, int p, int depth) {
+  const int j = X.log_out + i;
+  if (j < S.rlog_cap) S.rlog[j] = make_int2(p, depth); else atomicOr(S.err, ERR_LISTS);
+}
+
 __device__ __forceinline__ bool step_over(unsigned long long v, int n_init, unsigned blocks) {
   return (v >> 48) == blocks && (v & kField) == (unsigned long long)n_init + ((v >> 24) & kField);
 }
@@ -599,8 +598,12 @@ __device__ void finish_step(const DevProblem& P, const TrackState& S, const Step
   if (items > C->max_items) C->max_items = items;
   const int n_next = __ldcg(X.lo_n), n_rec = __ldcg(S.rec_n);
   unsigned long long flags = 0;
+  // Stork: the end of the step's list in the launch's log; a log that could not take another
+  // whole list ends the launch like a full record buffer
+  const bool log_full = S.rlog != nullptr && X.log_out + n_next > S.rlog_cap - S.rlog_step_max;
+  if (S.rlog != nullptr) S.rlog_off[X.log_j + 1] = X.log_out + n_next;
   if (X.t > P.end_time && n_next == 0) { flags |= 1u; C->done = 1; }
-  else if (n_rec > high_water) { flags |= 2u; C->stop = 1; }
+  else if (n_rec > high_water || log_full) { flags |= 2u; C->stop = 1; }
   __threadfence();
   st_release_u64(&C->fin, ((unsigned long long)n_next << 34) | (flags << 32) | X.stamp);
 }
@@ -884,14 +887,92 @@ __device__ int depth_walk(const DevProblem& P, const TrackState& S, const StepCt
   return d;
 }
 
+// Stork's depth walk (src/Run.cpp:909-956): down while liquid, else up until liquid, on T at
+// t alone; only the column's depth is kept.  A walk that ends on the bottom layer keeps the
+// layer above it (the reference's bottom rule).  Layers are evaluated ahead as in
+// depth_walk.
+template <int PREC>
+__device__ int stork_walk(const DevProblem& P, const TrackState& S, const StepCtx& X, int p, int D,
+                          const EvalT& first_down, const EvalT& first_up, unsigned long long& pairs) {
+  const int lane = threadIdx.x & 31;
+  const int col = p / P.nz;
+  const int top = col * P.nz + (P.nz - 1);
+  constexpr int NB = PREC == 0 ? 1 : 4;
+  EvalT Tc[4], Tu[4];
+  int cb = D + 1, cn = (PREC != 0 && D + 1 <= P.nz - 1) ? 1 : 0;
+  int ub = D, un = (PREC != 0 && D >= 1) ? 1 : 0;
+  Tc[0] = first_down; Tu[0] = first_up;
+  int d = D;
+  bool none_deeper = true;
+  while (true) {
+    ++d;
+    if (d == P.nz) break;
+    if (d >= cb + cn) {
+      int pts[NB];
+      cn = 0;
+#pragma unroll
+      for (int q = 0; q < NB; ++q) {
+        const bool ok = d + q <= P.nz - 1;
+        pts[q] = ok ? top - (d + q) : p;
+        cn += ok ? 1 : 0;
+      }
+      cb = d;
+      EvalT tmp[NB];
+      eval_Tn<PREC, NB>(P, S, X, pts, tmp);
+#pragma unroll
+      for (int q = 0; q < NB; ++q) Tc[q] = tmp[q];
+    }
+    EvalT T = pick4(Tc, d - cb);
+    guard_T<PREC>(P, S, X, T, top - d);
+    pairs += X.nn;
+    if (!T.liquid) break;
+    none_deeper = false;
+  }
+  while (true) {
+    --d;
+    if (d == 0 || !none_deeper) break;
+    if (!(d <= ub && d > ub - un)) {
+      int pts[NB];
+      un = 0;
+#pragma unroll
+      for (int q = 0; q < NB; ++q) {
+        const bool ok = d - q >= 1;
+        pts[q] = ok ? top - (d - q) : p;
+        un += ok ? 1 : 0;
+      }
+      ub = d;
+      EvalT tmp[NB];
+      eval_Tn<PREC, NB>(P, S, X, pts, tmp);
+#pragma unroll
+      for (int q = 0; q < NB; ++q) Tu[q] = tmp[q];
+    }
+    EvalT T = pick4(Tu, ub - d);
+    guard_T<PREC>(P, S, X, T, top - d);
+    pairs += X.nn;
+    if (T.liquid) break;
+  }
+  if (d == P.nz - 1) --d;
+  if (lane == 0) S.depths[col] = d;
+  return d;
+}
+
+// Tracking forms of the loop: Volume, Surface and Stork (Surface's search without
+// solidification, which logs the liquid columns for the doubly reduced data).
+enum { TM_VOLUME = 0, TM_SURFACE = 1, TM_STORK = 2 };
+
 // One work item; returns the number of child items it published (already counted).
 // A beam-trace candidate arrives with its claim still in flight (the lane-0 result of the
 // atomic, `got`): the point is evaluated meanwhile and the item stops before any effect if
 // another item took the point.
 // A re-test brings its column's depth from the liquid list (Dk); other items read it.
-template <int PREC, bool SURF>
+// Stork re-tests (src/Run.cpp:796-830) expand only when still liquid, and one that cooled
+// only resets its column's depth.
+template <int PREC, int TM>
 __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx& X, int type, int p, int aux,
                         int Dk, bool seed, bool got, unsigned long long& pairs, Kept& kept) {
+  constexpr bool SURF = TM != TM_VOLUME;
+  constexpr bool STORK = TM == TM_STORK;
+  constexpr bool RETEST_EXPANDS = SURF && !STORK;     // Surface: test_pts = last_liq_pts
   const int lane = threadIdx.x & 31;
   int nchild = 0;
   const double Told = ldcg_d(S.T + p);
@@ -909,7 +990,7 @@ __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx&
   // issued first and run while this point is evaluated; the claimed neighbours are
   // published after the pass.
   Claims rc{0, 0, 0xffffffffu};
-  if (SURF && type == IT_RETEST) rc = claim_neighbours<SURF>(P, S, X, p);
+  if (RETEST_EXPANDS && type == IT_RETEST) rc = claim_neighbours<SURF>(P, S, X, p);
   EvalT T3[3];
   int D = 0;
   if (SURF && PREC != 0) {                 // the point and the layers its depth walk starts with
@@ -929,7 +1010,7 @@ __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx&
     if (SURF) D = type == IT_RETEST ? Dk : (seed ? ldcg_i(S.depths + p / P.nz) : aux);
     T3[0] = eval_T<PREC>(P, S, X, X.nb, X.nn, p, X.st);
   }
-  if (SURF && type == IT_RETEST) emit_claimed(S, X, rc, nchild, nullptr);
+  if (RETEST_EXPANDS && type == IT_RETEST) emit_claimed(S, X, rc, nchild, nullptr);
   if (seed && !__shfl_sync(0xffffffffu, got, 0)) return 0;
   EvalT T = T3[0];
   guard_T<PREC>(P, S, X, T, p);
@@ -942,11 +1023,15 @@ __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx&
     // Volume items keep one claimed neighbour to run next in the same warp; Surface items
     // publish all of them (a kept child would wait for the rest of a long re-test or depth
     // walk, longer than the queue takes to hand it to another warp)
-    if (!(SURF && type == IT_RETEST)) expand<SURF>(P, S, X, p, nchild, SURF ? nullptr : &kept);
+    if (!(RETEST_EXPANDS && type == IT_RETEST)) expand<SURF>(P, S, X, p, nchild, SURF ? nullptr : &kept);
     // the depth walk under a liquid surface point needs nothing else from this step
     int Dn = 0;
-    if (SURF) Dn = depth_walk<PREC>(P, S, X, p, D, T3[1], T3[2], pairs);
+    if (STORK) Dn = stork_walk<PREC>(P, S, X, p, D, T3[1], T3[2], pairs);
+    else if (SURF) Dn = depth_walk<PREC>(P, S, X, p, D, T3[1], T3[2], pairs);
     if (lane == 0) push_liquid(S, X, slot, p, Dn);
+    if (STORK && lane == 0) log_liquid(S, X, slot, p, Dn);
+  } else if (STORK) {
+    if (type == IT_RETEST && lane == 0) S.depths[p / P.nz] = 0;
   } else if (type == IT_RETEST) {          // cooled below T_L since the last step
     if (lane == 0) push_rec(S, X, p, T.T, Told);
     if (SURF) {
@@ -1002,10 +1087,11 @@ __host__ __device__ __forceinline__ bool axis_in_smem(const DevProblem& P) {
 // spin_limit bounds every wait (kSpinLimit unless a test lowers it); hold (a test knob, 0
 // otherwise) counts items into every step that are never dealt, so no step can end and the
 // waits run out: the path of a lost item.
-template <int PREC, bool SURF>
-__global__ void __launch_bounds__(track_bound<SURF>(), 1) k_track(DevProblem P, TrackState S, NodeWindow W, int k_begin,
-                                                            int k_end, int high_water, int stage_cap,
-                                                            long long spin_limit, int hold) {
+template <int PREC, int TM>
+__global__ void __launch_bounds__(track_bound<TM != TM_VOLUME>(), 1) k_track(DevProblem P, TrackState S, NodeWindow W,
+                                                                        int k_begin, int k_end, int high_water,
+                                                                        int stage_cap, long long spin_limit, int hold) {
+  constexpr bool SURF = TM != TM_VOLUME;
   extern __shared__ __align__(16) unsigned char stage_mem[];
   __shared__ BlockBuf bbuf;
   const int lane = threadIdx.x & 31;
@@ -1046,6 +1132,14 @@ __global__ void __launch_bounds__(track_bound<SURF>(), 1) k_track(DevProblem P, 
   // step k's live-list length and this warp's first re-test entry, read when step k - 1
   // ended (for the first step, from memory)
   int nL_next = k_begin < k_end ? ldcg_i(&C->liq_n[k_begin % 3]) : 0;
+  // Stork: the launch's log starts with the liquid list of step k_begin - 1 (list 0); the
+  // list each step fills follows the one before it
+  int log_pos = nL_next;
+  if (TM == TM_STORK && blockIdx.x == 0 && k_begin < k_end) {
+    const int2* L0 = S.liq[k_begin % 3];
+    for (int i = threadIdx.x; i < nL_next && i < S.rlog_cap; i += blockDim.x) S.rlog[i] = __ldcg(L0 + i);
+    if (threadIdx.x == 0) { S.rlog_off[0] = 0; S.rlog_off[1] = nL_next; }
+  }
   int2 first_next = make_int2(0, 0);
   if (k_begin < k_end && (tid >> 5) < S.list_cap) first_next = __ldcg(S.liq[k_begin % 3] + (tid >> 5));
   // the window's per-step scalars, read one step ahead
@@ -1099,6 +1193,8 @@ __global__ void __launch_bounds__(track_bound<SURF>(), 1) k_track(DevProblem P, 
     X.Lo = S.liq[b1];
     X.lo_n = &C->liq_n[b1];
     X.ax = ax;
+    X.log_out = log_pos;
+    X.log_j = k - k_begin + 1;
     unsigned long long arrival = 0;         // this block enters the step (thread 0)
     bool arrival_pending = threadIdx.x == 0;
     if (arrival_pending) arrival = atomicAdd(&X.qc->state, kArrive);
@@ -1201,7 +1297,7 @@ __global__ void __launch_bounds__(track_bound<SURF>(), 1) k_track(DevProblem P, 
       unsigned long long g_item = globaltimer();
       Kept kept{0, 0, false};
       while (true) {
-        run_item<PREC, SURF>(P, S, X, type, p, aux, Dk, is_seed, got, pairs, kept);
+        run_item<PREC, TM>(P, S, X, type, p, aux, Dk, is_seed, got, pairs, kept);
         if (lane == 0) {
           const int l = min(X.depth, 3);
           atomicMax(&X.qc->lvl_start[l], (unsigned)(g_item - g0));
@@ -1237,6 +1333,7 @@ __global__ void __launch_bounds__(track_bound<SURF>(), 1) k_track(DevProblem P, 
     const bool aborted = (unsigned)fin_seen == 0xffffffffu;
     const unsigned verdict = (unsigned)(fin_seen >> 32) & 3u;
     nL_next = (int)(fin_seen >> 34);
+    log_pos += nL_next;
     if (!aborted && (tid >> 5) < S.list_cap) first_next = __ldcg(X.Lo + (tid >> 5));
     cp_async_wait_all();
     if (threadIdx.x == 0) s_flush[k & 1] = bbuf.nrec >= kBlkRec / 2;
@@ -1923,7 +2020,7 @@ static bool window_layout_ok(const NodeBufView& nb) {
   return true;
 }
 
-template <int PREC, bool SURF>
+template <int PREC, int TM>
 static cudaError_t launch_track_t(const DevProblem& P, const TrackState& S, const NodeWindow& w, int k_begin, int k_end,
                                   int hw, cudaStream_t s) {
   if (!window_layout_ok(w.nb)) return cudaErrorInvalidValue;
@@ -1950,38 +2047,43 @@ static cudaError_t launch_track_t(const DevProblem& P, const TrackState& S, cons
   cap = std::max(kListPad, cap & ~(kListPad - 1));
   const size_t smem = (size_t)3 * cap * staged_bytes_per_node<PREC>() +
                       (axis_in_smem<PREC>(P) ? (size_t)(P.nx + P.ny + P.nz) * sizeof(float2) : 0);
-  cudaError_t e = cudaFuncSetAttribute(k_track<PREC, SURF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(k_track<PREC, TM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   // Shared memory for this block and one k_nodes_window block beside it (the next window's
   // lists are built on the other stream while this one is tracked; without the room that
   // launch waits for the tracking launch to end), the rest of the SM's 256 KB to the L1
   // cache.  A carveout picks the smallest configuration at or above the request.
   cudaFuncAttributes ta{}, na{};
-  if ((e = cudaFuncGetAttributes(&ta, k_track<PREC, SURF>)) != cudaSuccess) return e;
+  if ((e = cudaFuncGetAttributes(&ta, k_track<PREC, TM>)) != cudaSuccess) return e;
   if ((e = cudaFuncGetAttributes(&na, k_nodes_window)) != cudaSuccess) return e;
   const size_t need = smem + ta.sharedSizeBytes + na.sharedSizeBytes + (P.compress ? sizeof(GenComp) : 0) +
                       2 * 1024;                                                   // + 1 KB reserved per block
   const int carve = std::min(100, (int)((need * 100 + 228 * 1024 - 1) / (228 * 1024)));
-  e = cudaFuncSetAttribute(k_track<PREC, SURF>, cudaFuncAttributePreferredSharedMemoryCarveout, carve);
+  e = cudaFuncSetAttribute(k_track<PREC, TM>, cudaFuncAttributePreferredSharedMemoryCarveout, carve);
   if (e != cudaSuccess) return e;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_track<PREC, SURF>, track_threads<SURF>(), smem);
+  constexpr bool SURF = TM != TM_VOLUME;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_track<PREC, TM>, track_threads<SURF>(), smem);
   const int blocks = sms * (occ < 1 ? occ : 1);
   if (blocks <= 0) return cudaErrorInvalidConfiguration;
   DevProblem Pc = P;
   TrackState Sc = S;
   NodeWindow Wc = w;
   void* args[] = {&Pc, &Sc, &Wc, &k_begin, &k_end, &hw, &cap, &spin_limit, &hold};
-  return cudaLaunchCooperativeKernel((const void*)k_track<PREC, SURF>, dim3(blocks), dim3(track_threads<SURF>()), args, smem,
+  return cudaLaunchCooperativeKernel((const void*)k_track<PREC, TM>, dim3(blocks), dim3(track_threads<SURF>()), args, smem,
                                      s);
 }
 
 cudaError_t th_launch_track(const DevProblem& P, const TrackState& S, const NodeWindow& w, int k_begin, int k_end,
                             int precision, int rec_high_water, cudaStream_t s) {
-  const bool surf = P.tracking == TH_TRACK_SURFACE;
-  if (precision == 0) return surf ? launch_track_t<0, true>(P, S, w, k_begin, k_end, rec_high_water, s)
-                                  : launch_track_t<0, false>(P, S, w, k_begin, k_end, rec_high_water, s);
-  return surf ? launch_track_t<1, true>(P, S, w, k_begin, k_end, rec_high_water, s)
-              : launch_track_t<1, false>(P, S, w, k_begin, k_end, rec_high_water, s);
+  const int tm = P.tracking == TH_TRACK_STORK ? TM_STORK : P.tracking == TH_TRACK_SURFACE ? TM_SURFACE : TM_VOLUME;
+  if (precision == 0) {
+    if (tm == TM_STORK) return launch_track_t<0, TM_STORK>(P, S, w, k_begin, k_end, rec_high_water, s);
+    if (tm == TM_SURFACE) return launch_track_t<0, TM_SURFACE>(P, S, w, k_begin, k_end, rec_high_water, s);
+    return launch_track_t<0, TM_VOLUME>(P, S, w, k_begin, k_end, rec_high_water, s);
+  }
+  if (tm == TM_STORK) return launch_track_t<1, TM_STORK>(P, S, w, k_begin, k_end, rec_high_water, s);
+  if (tm == TM_SURFACE) return launch_track_t<1, TM_SURFACE>(P, S, w, k_begin, k_end, rec_high_water, s);
+  return launch_track_t<1, TM_VOLUME>(P, S, w, k_begin, k_end, rec_high_water, s);
 }
 
 void th_launch_notrack_step(const DevProblem& P, const TrackState& S, const NodeWindow& w, int k, int precision,

@@ -1,4 +1,4 @@
-// Solidification-mode device state and kernels (NoTracking, Volume, Surface).
+// Solidification-mode device state and kernels (NoTracking, Volume, Surface, Stork).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -93,6 +93,14 @@ struct TrackState {
   int redo_cap;            // (block b's at b * redo_cap), and per block its list's count and
   int redo_blocks;         // error bits (redo_aux[2 b], redo_aux[2 b + 1])
   int* redo_aux;
+  // Stork: the launch's log of liquid lists (entries as in liq: point, column depth); list j
+  // (j = 0: the liquid points of step k_begin - 1, then one per step run) spans
+  // [rlog_off[j], rlog_off[j + 1]); null for the other forms
+  int2* rlog;
+  int* rlog_off;
+  int rlog_cap;
+  int rlog_step_max;       // the longest list one step can add (a launch stops before the log
+                           // has less room than that)
   TrackCounters* C;
   const float2* axis;      // grid coordinates as (hi, lo) floats: x[0, nx), y[nx, nx + ny), z after
   int t_fixed;             // T and the records' T, T_last hold FP32 tracking's fixed point (see t_decode)
@@ -114,6 +122,19 @@ struct NodeWindow {
   int* nseed;
   int seed_cap;
 };
+
+#ifdef __CUDACC__
+// Slot `slot` of a window as a node-list view.
+__device__ __forceinline__ NodeBufView slot_view(const NodeWindow& w, int slot) {
+  NodeBufView v = w.nb;
+  const size_t off = (size_t)slot * w.slot_cap;
+  v.x += off; v.y += off; v.z += off; v.ipx += off; v.ipy += off; v.ipz += off; v.dtau += off; v.amp += off;
+  v.kx += off; v.ky += off; v.kz += off; v.w += off; v.xh += off; v.xl += off; v.yh += off; v.yl += off;
+  v.zh += off; v.zl += off;
+  v.cap = w.slot_cap;
+  return v;
+}
+#endif
 
 // Error bits of a window build (with the node bits 1 = node capacity, 2 = walk limit).
 enum { ERR_SEED_CAPACITY = 4 };
@@ -137,6 +158,29 @@ void th_launch_notrack_step(const DevProblem& P, const TrackState& S, const Node
 // record's step and of the step before it).
 void th_launch_solidify(const DevProblem& P, const TrackState& S, const NodeWindow& w, const SolRec* rec, int nrec,
                         int precision, bool do_sol, cudaStream_t s);
+
+// Stork's doubly reduced data for the steps of one tracking launch (th_rrdf.cu): a count
+// pass gives each step's rows and vertex values, then a fill pass writes the rows at the
+// offsets the host lays out (cell index: 3 values, step times: 2, vertex temperatures: 16
+// per row, as Grid::get_RRDF_idxs / _ts / _Ts hold them, src/Grid.h:368-370).
+struct RrdfBatch {
+  const int2* log;           // the launch's log of liquid lists (TrackState::rlog)
+  const int* off;            // list j spans [off[j], off[j + 1]), j = 0 .. nsteps
+  int k0, nsteps;            // step k0 + j has lists j (liquid at k - 1) and j + 1 (liquid at k)
+  int nmax;                  // most entries of two consecutive lists
+  int* counts;               // per step: rows, vertex values
+  const long long* row_base; // fill: per step, its first row
+  int* scratch;              // per block: th_rrdf_scratch_ints(nmax) ints
+  double* vals;              // fill, per block: 3 * vals_cap doubles (vertex values, vertex ids)
+  int vals_cap;
+  uint32_t* idx;             // fill: the rows
+  double* ts;
+  double* Ts;
+  int* err;                  // bit 0: a step had more vertex values than vals_cap
+};
+size_t th_rrdf_scratch_ints(int nmax);
+void th_launch_rrdf(const DevProblem& P, const NodeWindow& w, const RrdfBatch& b, bool fill, int precision, int blocks,
+                    cudaStream_t s);
 
 // Final per-point field with the reference's liquid markers applied.
 void th_launch_final_field(const DevProblem& P, const TrackState& S, int field, double* out, cudaStream_t s);

@@ -55,7 +55,7 @@ typedef struct th_info {
   int32_t n_beams;
   int32_t n_snapshots;
   int32_t mode;                /* 0 Snapshots, 1 Solidification */
-  int32_t tracking;            /* 0 None, 1 Volume, 2 Surface */
+  int32_t tracking;            /* 0 None, 1 Volume, 2 Surface, 3 Stork */
   double dt;                   /* solidification timestep (s) */
   double end_time;             /* end of the last scan path (s) */
   double T0, TL;               /* initial and liquidus temperature (K) */
@@ -152,12 +152,24 @@ th_status th_run_reset(th_ctx* ctx);
  * and their SM clocks summed over warps, then per chain depth 0, 1, 2, >= 3 the latest
  * item start and the latest item end after the step began, in ms summed over steps, the
  * nodes of the evaluation passes summed over passes, the records of an FP32 run whose
- * solidification was redone in FP64, and the liquid decisions of an FP32 run taken on an
- * FP64 sum (31 values). */
+ * solidification was redone in FP64, the liquid decisions of an FP32 run taken on an
+ * FP64 sum, and for Stork tracking the ms building the doubly reduced data and its rows
+ * (33 values). */
 th_status th_run_stats(th_ctx* ctx, double* out, int32_t n);
 
+/* After th_solidify / th_simulate of a Stork deck (Tracking Stork): the doubly reduced data
+ * of the run so far, the rows in step order and within a step in ascending cell index
+ * (the reference's single-thread order).  Per row: idx the cell's (i, j, k) (3 values),
+ * ts the previous and the current step time (2), Ts the temperatures of the cell's 8
+ * vertices at the previous step, then at the current one, vertex (di, dj, dk) at
+ * di*4 + dj*2 + dk (16).  Copies min(cap, rows) rows into each non-null array; *rows
+ * receives the row count.  Replaces Grid::get_RRDF_idxs / get_RRDF_ts / get_RRDF_Ts
+ * (src/Grid.h:368-370), filled by Run::Stork (src/Run.cpp:711-1079). */
+th_status th_rrdf(th_ctx* ctx, uint32_t* idx, double* ts, double* Ts, int64_t cap, int64_t* rows);
+
 /* Whole run as the reference CLI does it: the mode loop, then the CSV files under
- * <deck dir>/Data (same names, columns and number format). */
+ * <deck dir>/Data (same names, columns and number format; a Stork deck writes
+ * <name>.RRDF.csv in place of <name>.Solidification.Final.csv). */
 th_status th_simulate(th_ctx* ctx);
 
 /* Point x node pairs evaluated by this context so far (temperature and gradient sums). */
