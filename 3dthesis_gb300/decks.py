@@ -150,7 +150,8 @@ class Deck:
         grid = [("x", 1), ("y", 1), ("z", 1)]
         temp = [("T", self.outputs.get("T", 1)), ("T_hist", 0)]
         sol_keys = ["tSol", "G", "Gx", "Gy", "Gz", "V", "dTdt", "eqFrac", "depth", "numMelt"]
-        sol = [(k, self.outputs.get(k, 0)) for k in sol_keys] + [("RDF", 0), ("MP_Stats", 0)]
+        sol = [(k, self.outputs.get(k, 0)) for k in sol_keys] + [("RDF", self.outputs.get("RDF", 0)),
+                                                                  ("MP_Stats", 0)]
         return (_block("Grid", [(k, str(v)) for k, v in grid])
                 + _block("Temperature", [(k, str(v)) for k, v in temp])
                 + _block("Solidification", [(k, str(v)) for k, v in sol]))

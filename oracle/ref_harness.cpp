@@ -107,6 +107,31 @@ void ref_output_rrdf(void* h, const char* name) {
   r->grid->Output_RRDF_csv(r->sim, name);
 }
 
+// The reduced data a run with Output RDF 1 leaves in the grid (Grid::get_RDF_tm / _tl /
+// _cr, src/Grid.h:360-362): per point the three counts, then all values in point order
+// (per point its tm, then tl, then cr values).  Returns the number of values; copies at most
+// cap.
+int64_t ref_rdf(void* h, int32_t* counts, double* vals, int64_t cap) {
+  RefRun* r = (RefRun*)h;
+  Grid& g = *r->grid;
+  int64_t n = 0;
+  for (int p = 0; p < r->sim.domain.pnum; ++p) {
+    const vector<double> v[3] = {g.get_RDF_tm(p), g.get_RDF_tl(p), g.get_RDF_cr(p)};
+    for (int c = 0; c < 3; ++c) {
+      if (counts) counts[3 * p + c] = (int32_t)v[c].size();
+      for (double x : v[c]) { if (vals && n < cap) vals[n] = x; ++n; }
+    }
+  }
+  return n;
+}
+
+// The reference's RDF writer (Grid::Output_RDF, src/Grid.cpp:176-201), as bin/Main.cpp:117
+// calls it: Data/<Name>.<name>.csv.
+void ref_output_rdf(void* h, const char* name) {
+  RefRun* r = (RefRun*)h;
+  r->grid->Output_RDF(r->sim, name);
+}
+
 int ref_field(void* h, const char* name, double* out) {
   RefRun* r = (RefRun*)h;
   Grid& g = *r->grid;

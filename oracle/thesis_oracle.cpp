@@ -102,6 +102,7 @@ struct Problem {
   int tracking; double dt; int out_freq; double rcheck; bool secondary;
   // outputs
   bool o_T, o_tSol, o_G, o_Gx, o_Gy, o_Gz, o_V, o_dTdt, o_eqFrac, o_depth, o_numMelt;
+  bool o_rdf = false;       // the reduced data format: per point its melt events (src/Grid.h:103-105)
   // settings
   double sol_tol; int sol_iter; double t_hist, p_hist, r_max; int compress; int thnum;
   double end_time;
@@ -113,6 +114,10 @@ struct Problem {
   // to T_L (DBL_MAX: never evaluated) and the secant's T - T_last at its latest
   // solidification (0: never solidified)
   std::vector<double> band, sol_dT;
+  // RDF (Output RDF 1): per point the melting times (pushed by Surface tracking's reset
+  // sweep, src/Run.cpp:604-609), solidification times and cooling rates (Grid::Solidify,
+  // src/Grid.cpp:322,547), and per solidification its secant's T - T_last (for tests)
+  std::vector<std::vector<double>> rdf_tm, rdf_tl, rdf_cr, rdf_dT;
   // Stork's doubly reduced data (src/Run.cpp:711-1079): per output cell its index (i, j, k),
   // the two step times and the 16 vertex temperatures (8 at the earlier time, then 8 at the
   // later one)
@@ -372,8 +377,10 @@ bool load_problem(Problem& P, const std::string& param_input, std::string& err) 
     P.o_T = b(o[1][0], true);
     P.o_tSol = b(o[2][0], false); P.o_G = b(o[2][1], false); P.o_Gx = b(o[2][2], false); P.o_Gy = b(o[2][3], false);
     P.o_Gz = b(o[2][4], false); P.o_V = b(o[2][5], false); P.o_dTdt = b(o[2][6], false); P.o_eqFrac = b(o[2][7], false);
-    P.o_depth = b(o[2][8], false); P.o_numMelt = b(o[2][9], false);
-    P.do_sol = P.mode == 1 && (P.o_tSol || P.o_G || P.o_V || P.o_Gx || P.o_Gy || P.o_Gz || P.o_dTdt || P.o_eqFrac);
+    P.o_depth = b(o[2][8], false); P.o_numMelt = b(o[2][9], false); P.o_rdf = b(o[2][10], false);
+    // every solidification output, RDF too, turns the solidification fields on (src/Grid.h:180-241)
+    P.do_sol = P.mode == 1 && (P.o_tSol || P.o_G || P.o_V || P.o_Gx || P.o_Gy || P.o_Gz || P.o_dTdt || P.o_eqFrac ||
+                               P.o_rdf);
   }
   // settings (src/Init.cpp:772-814) and r_max (src/Util.cpp:145-166)
   {
@@ -774,8 +781,10 @@ void solidify(Problem& P, double t, long p) {                                 //
     if (Tt > T0) { t1 = tsol; T1 = Tt; } else { t2 = tsol; T2 = Tt; }
   }
   P.tSol[p] = tsol;
+  if (P.o_rdf) { P.rdf_tl[p].push_back(tsol); P.rdf_dT[p].push_back(P.sol_dT[p]); }
   double out[10];
   solid_fields(P, p, tsol, out);
+  if (P.o_rdf) P.rdf_cr[p].push_back(out[4]);
   P.G[p] = out[0]; P.Gx[p] = out[1]; P.Gy[p] = out[2]; P.Gz[p] = out[3];
   P.dTdt[p] = out[4]; P.V[p] = out[5]; P.eqFrac[p] = out[6];
 }
@@ -915,6 +924,7 @@ void alloc_state(Problem& P) {
     P.Gz.assign(n, 0.0); P.dTdt.assign(n, 0.0); P.eqFrac.assign(n, 0.0); P.depth.assign(n, 0.0);
     P.numMelt.assign(n, 0);
     P.sol_dT.assign(n, 0.0);
+    if (P.o_rdf) { P.rdf_tm.assign(n, {}); P.rdf_tl.assign(n, {}); P.rdf_cr.assign(n, {}); P.rdf_dT.assign(n, {}); }
   }
 }
 
@@ -957,7 +967,13 @@ int64_t run_tracking(Problem& P, int threads, int64_t max_steps, double budget_s
   int64_t step = 0;
   while (true) {
     make_nodes(P, t, false, N);
-    for (long p : reset) { P.T_last[p] = P.T[p]; P.calc[p] = 0; }
+    for (long p : reset) {
+      // a point still liquid when its step ended opens a melt event (Surface only; one
+      // open event at a time: pushed while as many melting as solidification times)
+      if (surface && P.o_rdf && P.T[p] >= P.TL && P.rdf_tm[p].size() == P.rdf_tl[p].size())
+        P.rdf_tm[p].push_back(t - P.dt);
+      P.T_last[p] = P.T[p]; P.calc[p] = 0;
+    }
     std::vector<long> last_liq = liq;
     reset = liq;
     liq.clear();
@@ -1281,7 +1297,12 @@ int or_field(void* h, const char* name, double* out) {
     return 0;
   }
   if (v) { if (v->empty()) return 1; std::memcpy(out, v->data(), sizeof(double) * P.pnum); return 0; }
-  if (f == "numMelt") { if (P.numMelt.empty()) return 1; for (long p = 0; p < P.pnum; ++p) out[p] = P.numMelt[p]; return 0; }
+  if (f == "numMelt") {
+    if (P.numMelt.empty()) return 1;
+    // with RDF the count is the number of melting times (src/Grid.h:232,343-350)
+    for (long p = 0; p < P.pnum; ++p) out[p] = P.o_rdf ? (double)P.rdf_tm[p].size() : P.numMelt[p];
+    return 0;
+  }
   if (f == "output_flag") {
     for (long p = 0; p < P.pnum; ++p) out[p] = P.outflag.empty() ? 1.0 : (double)P.outflag[p];
     return 0;
@@ -1290,6 +1311,21 @@ int or_field(void* h, const char* name, double* out) {
 }
 
 int64_t or_pairs(void* h) { return ((Problem*)h)->pairs.load(); }
+
+int64_t or_rdf(void* h, int32_t* counts, double* vals, double* dT, int64_t cap) {
+  const Problem& P = *(Problem*)h;
+  if (!P.o_rdf) return -1;
+  int64_t n = 0, m = 0;
+  for (long p = 0; p < P.pnum; ++p) {
+    const std::vector<double>* v[3] = {&P.rdf_tm[p], &P.rdf_tl[p], &P.rdf_cr[p]};
+    for (int c = 0; c < 3; ++c) {
+      if (counts) counts[3 * p + c] = (int32_t)v[c]->size();
+      for (double x : *v[c]) { if (vals && n < cap) vals[n] = x; ++n; }
+    }
+    for (double x : P.rdf_dT[p]) { if (dT && m < cap) dT[m] = x; ++m; }
+  }
+  return n;
+}
 
 int64_t or_rrdf(void* h, uint32_t* idx, double* ts, double* Ts, int64_t cap) {
   const Problem& P = *(Problem*)h;

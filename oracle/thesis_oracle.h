@@ -69,6 +69,13 @@ void  or_solid_fields_many(void* h, const int64_t* pts, const double* tsol, int6
 uint64_t or_schedule(void* h, double t, int is_sol);
 void  or_schedule_many(void* h, const double* t, int64_t n, int is_sol, uint64_t* out, int threads);
 
+/* After a run with Output RDF 1: per point (in point order) the numbers of melting times,
+ * solidification times and cooling rates (counts[3p .. 3p+2]), and all values in that order
+ * (per point its melting times, then solidification times, then cooling rates); dT gets
+ * per solidification time its secant's T - T_last.  Returns the number of values (-1
+ * without RDF); copies at most cap into each array. */
+int64_t or_rdf(void* h, int32_t* counts, double* vals, double* dT, int64_t cap);
+
 /* After a Stork run (Tracking Stork): the doubly reduced data, rows in the reference's
  * single-thread order (step, then cell): per row the cell index (3), the two step times (2)
  * and the 16 vertex temperatures.  Returns the row count; copies at most cap rows. */

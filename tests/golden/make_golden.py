@@ -15,6 +15,8 @@ own process (the reference keeps function-static state).  The fixtures hold:
 * ``run_<deck>.npz`` - a full Run::Simulate on a small solidification deck: the packed
   molten-point mask, per-field checksums over all output points, and every output
   field at a seeded subset of 1500 output points.
+  The ``*_rdf`` runs (Output RDF 1) also hold every melting time, solidification time and
+  cooling rate of every point (Grid::get_RDF_*) and the reference's ``RDF.Final`` file.
 * ``csv_<deck>.npz`` - the reference's own output files (Grid::Output) of a whole run of
   a small Snapshots deck and a small Solidification deck, byte for byte: ``names`` and
   ``file<i>`` (the file's bytes).
@@ -25,8 +27,8 @@ own process (the reference keeps function-static state).  The fixtures hold:
   order within a step); the first deck's fixture also holds the reference's own
   ``<name>.RRDF.csv`` (Grid::Output_RRDF_csv) byte for byte.
 
-``python tests/golden/make_golden.py csv`` (or ``comp``, ``rrdf``) regenerates only the csv
-(or the path-compression, the Stork) fixtures.
+``python tests/golden/make_golden.py csv`` (or ``comp``, ``rdf``, ``rrdf``) regenerates only
+the csv (or the path-compression, the RDF, the Stork) fixtures.
 """
 from __future__ import annotations
 
@@ -96,6 +98,16 @@ if "rrdf" in job:
             out[f"file{i}"] = np.frombuffer(f.read(), dtype=np.uint8)
 if "fields" in job:
     L.ref_simulate(h)
+    if "rdf" in job:
+        import os
+        L.ref_rdf.restype = ctypes.c_int64
+        n = L.ref_rdf(h, None, None, ctypes.c_int64(0))
+        counts = np.zeros(3 * int(info[3]), dtype=np.int32); vals = np.zeros(n)
+        L.ref_rdf(h, counts.ctypes.data_as(ctypes.c_void_p), vals.ctypes.data_as(ctypes.c_void_p), ctypes.c_int64(n))
+        out.update(rdf_counts=counts, rdf_vals=vals)
+        L.ref_output_rdf(h, b"RDF.Final")
+        with open(os.path.join("Data", os.listdir("Data")[0]), "rb") as f:
+            out["rdf_file"] = np.frombuffer(f.read(), dtype=np.uint8)
     for f in job["fields"]:
         a = np.zeros(int(info[3])); L.ref_field(h, str(f).encode(), a.ctypes.data_as(ctypes.c_void_p)); out[str(f)] = a
 np.savez(sys.argv[4], **out)
@@ -121,12 +133,17 @@ def node_fixture(deck, times, scratch):
 def run_fixture(deck, scratch, tag):
     fields = ["T", "output_flag"] + [f for f in ("tSol", "G", "V", "Gx", "Gy", "Gz", "dTdt", "eqFrac",
                                                  "numMelt", "depth") if deck.outputs.get(f)]
-    r = run_ref(deck, {"fields": np.asarray(fields)}, scratch)
+    job = {"fields": np.asarray(fields)}
+    if deck.outputs.get("RDF"):
+        job["rdf"] = np.asarray(1)
+    r = run_ref(deck, job, scratch)
     flag = r["output_flag"] > 0
     idx = np.flatnonzero(flag)
     rng = np.random.default_rng(1234)
     sub = np.sort(rng.choice(idx, min(1500, idx.size), replace=False)) if idx.size else idx
     out = {"info": r["info"], "mask": np.packbits(flag), "n_points": np.int64(flag.size), "sample": sub}
+    if "rdf_counts" in r:                          # the reduced data: every value, and the file
+        out.update(rdf_counts=r["rdf_counts"], rdf_vals=r["rdf_vals"], rdf_file=r["rdf_file"])
     for f in fields:
         if f == "output_flag":
             continue
@@ -152,7 +169,8 @@ NODE_TIMES = {
 }
 RUNS = {"small_surface": ("small_surface", "Surface"), "small_volume": ("small_surface", "Volume"),
         "small_none": ("small_surface", "None"), "small_multibeam": ("small_multibeam",),
-        "small_surface_comp": ("small_surface", "Surface")}
+        "small_surface_comp": ("small_surface", "Surface"), "small_surface_rdf": ("small_surface", "Surface"),
+        "small_volume_rdf": ("small_surface", "Volume")}
 
 
 CSV_DECKS = ("csv_snapshot", "small_multibeam")
@@ -231,6 +249,9 @@ def run_deck(tag):
     if tag.endswith("_comp"):                  # path compression on
         d.name = tag
         d.settings_extra = {"Path": {"Compression": "1"}}
+    if tag.endswith("_rdf"):                   # the reduced data format (Output RDF 1)
+        d.name = tag
+        d.outputs = dict(d.outputs, RDF=1, numMelt=1)
     return d
 
 
@@ -244,6 +265,12 @@ def main():
             for tag in [t for t in RUNS if t.endswith("_comp")]:
                 run_fixture(run_deck(tag), scratch, tag)
         print("compression fixtures written to", HERE)
+        return
+    if sys.argv[1:] == ["rdf"]:
+        with tempfile.TemporaryDirectory() as scratch:
+            for tag in [t for t in RUNS if t.endswith("_rdf")]:
+                run_fixture(run_deck(tag), scratch, tag)
+        print("rdf fixtures written to", HERE)
         return
     if sys.argv[1:] == ["rrdf"]:
         with tempfile.TemporaryDirectory() as scratch:

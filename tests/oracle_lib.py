@@ -38,6 +38,8 @@ def load():
         L.or_schedule.argtypes = [vp, ctypes.c_double, ctypes.c_int]
         L.or_schedule.restype = ctypes.c_uint64
         L.or_schedule_many.argtypes = [vp, vp, ctypes.c_int64, ctypes.c_int, vp, ctypes.c_int]
+        L.or_rdf.argtypes = [vp, vp, vp, vp, ctypes.c_int64]
+        L.or_rdf.restype = ctypes.c_int64
         L.or_rrdf.argtypes = [vp, vp, vp, vp, ctypes.c_int64]
         L.or_rrdf.restype = ctypes.c_int64
         L.or_pairs.argtypes = [vp]
@@ -126,6 +128,19 @@ class Oracle:
         _lib.or_schedule_many(self.h, tt.ctypes.data_as(ctypes.c_void_p), tt.size, int(is_sol),
                               out.ctypes.data_as(ctypes.c_void_p), threads)
         return out
+
+    def rdf(self):
+        """After a run with Output RDF 1: (counts (pnum, 3) int32 - per point the numbers of
+        melting times, solidification times and cooling rates -, vals - all values, per point
+        its melting times, then solidification times, then cooling rates -, dT - per
+        solidification time its secant's T - T_last)."""
+        n = _lib.or_rdf(self.h, None, None, None, 0)
+        counts = np.zeros((self.pnum, 3), dtype=np.int32)
+        vals = np.zeros(max(n, 0))
+        dT = np.zeros(max(n, 0))
+        _lib.or_rdf(self.h, counts.ctypes.data_as(ctypes.c_void_p), vals.ctypes.data_as(ctypes.c_void_p),
+                    dT.ctypes.data_as(ctypes.c_void_p), n)
+        return counts, vals, dT[:int(counts[:, 1].sum())]
 
     def rrdf(self):
         """After a Stork run: (idx (n, 3) uint32, ts (n, 2), Ts (n, 16)), the rows in the

@@ -55,6 +55,10 @@ def test_oracle_solidification_matches_reference(tag, oracle, tmp_path):
         v = o.field(f)
         np.testing.assert_allclose(v[sub], g[key], rtol=1e-12, atol=1e-12, err_msg=f)
         np.testing.assert_allclose(np.sum(v[flag]), g[f + "_sum"], rtol=1e-11, err_msg=f)
+    if "rdf_counts" in g:                          # the reduced data format: every event
+        counts, vals, _ = o.rdf()
+        assert np.array_equal(counts.ravel(), g["rdf_counts"]), "RDF event counts differ"
+        np.testing.assert_allclose(vals, g["rdf_vals"], rtol=1e-12, atol=0, err_msg="RDF values")
 
 
 def test_oracle_solidification_time_budget(oracle, tmp_path):
