@@ -45,7 +45,7 @@ EXPORTED = ("th_ctx_create_from_deck", "th_ctx_destroy", "th_last_error", "th_ge
             "th_batch_snapshot_device", "th_batch_set_tile_shape", "th_batch_autotune", "th_batch_pairs",
             "th_adj_create", "th_adj_destroy", "th_adj_last_error", "th_adj_num_params", "th_adj_params",
             "th_adj_host_nodes", "th_adj_forward", "th_adj_backward", "th_calc_T_times_device",
-            "th_device_rates", "th_rrdf")
+            "th_device_rates", "th_rrdf", "th_rdf")
 
 
 class ThesisError(RuntimeError):
@@ -125,6 +125,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.th_adj_backward.argtypes = [vp, vp, vp]
     L.th_device_rates.argtypes = [vp]
     L.th_rrdf.argtypes = [vp, vp, vp, vp, c_i64, ctypes.POINTER(c_i64)]
+    L.th_rdf.argtypes = [vp, vp, vp, c_i64, ctypes.POINTER(c_i64)]
     _lib = L
     return L
 
@@ -263,6 +264,18 @@ class Simulation:
                 "loop_ms_end0", "loop_ms_end1", "loop_ms_end2", "loop_ms_end3", "loop_eval_nodes",
                 "records_redone_fp64", "guarded_decisions", "ms_rrdf", "rrdf_rows")
         return dict(zip(keys, out.tolist()))
+
+    def rdf(self):
+        """After solidify() on a deck with Output RDF 1: (counts (pnum, 3) int32 - per point its
+        numbers of melting times, solidification times and cooling rates -, vals - point by
+        point its melting times, then solidification times, then cooling rates)
+        (Grid::get_RDF_tm / _tl / _cr, src/Grid.h:360-362)."""
+        n = ctypes.c_int64()
+        counts = np.zeros((self.pnum, 3), dtype=np.int32)
+        self._check(self._lib.th_rdf(self._ctx, _ptr(counts), None, 0, ctypes.byref(n)))
+        vals = np.zeros(n.value)
+        self._check(self._lib.th_rdf(self._ctx, None, _ptr(vals), n.value, ctypes.byref(n)))
+        return counts, vals
 
     def rrdf(self):
         """After solidify() on a Stork deck: the doubly reduced data, (idx (n, 3) uint32,

@@ -60,6 +60,37 @@ bool th_write_rrdf_csv(const HostProblem& hp, const std::string& tag, const uint
   return ok;
 }
 
+// The reference's reduced data (Grid::Output_RDF, src/Grid.cpp:176-201): the header, then per
+// row the point's coordinates, melting time, solidification time and cooling rate.
+bool th_write_rdf_csv(const HostProblem& hp, const std::string& tag, const int64_t* pts, const double* tm,
+                      const double* tl, const double* cr, int64_t rows, std::string& err) {
+  const std::string dir = th_data_dir(hp);
+  mkdir(dir.c_str(), 0777);
+  const std::string path = dir + "/" + hp.name + "." + tag + ".csv";
+  FILE* f = std::fopen(path.c_str(), "w");
+  if (!f) { err = "cannot write " + path; return false; }
+  std::vector<char> buf(1 << 20);
+  std::setvbuf(f, buf.data(), _IOFBF, buf.size());
+  std::fputs("x,y,z,tm,tl,cr\n", f);
+  for (int64_t r = 0; r < rows; ++r) {
+    double x, y, z;
+    th_point_coord(hp, pts[r], x, y, z);
+    std::fprintf(f, "%g,%g,%g,%g,%g,%g\n", x, y, z, tm[r], tl[r], cr[r]);
+  }
+  const bool ok = std::fclose(f) == 0;
+  if (!ok) err = "error writing " + path;
+  return ok;
+}
+
+void th_point_coord(const HostProblem& hp, int64_t p, double& x, double& y, double& z) {
+  const int gx = (uint16_t)hp.nx, gy = (uint16_t)hp.ny, gz = (uint16_t)hp.nz;
+  const int64_t nyz = (int64_t)hp.ny * hp.nz;
+  const int i = (int)(p / nyz), j = (int)((p / hp.nz) % hp.ny), k = (int)(p % hp.nz);
+  x = (gx - 1) ? hp.xmin + (double(i) * ((hp.xmax - hp.xmin) / (gx - 1))) : hp.xmax;
+  y = (gy - 1) ? hp.ymin + (double(j) * ((hp.ymax - hp.ymin) / (gy - 1))) : hp.ymax;
+  z = (gz - 1) ? hp.zmin + (double(k) * ((hp.zmax - hp.zmin) / (gz - 1))) : hp.zmax;
+}
+
 void th_grid_coords(const HostProblem& hp, std::vector<double>& x, std::vector<double>& y, std::vector<double>& z) {
   const int gx = (uint16_t)hp.nx, gy = (uint16_t)hp.ny, gz = (uint16_t)hp.nz;
   const double hx = gx > 1 ? (hp.xmax - hp.xmin) / (gx - 1) : 0.0;

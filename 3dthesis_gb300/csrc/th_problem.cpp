@@ -324,10 +324,11 @@ bool th_load_deck(const std::string& param_input, HostProblem& hp, std::string& 
       hp.o_Gz = o.flag("Solidification", "Gz", false); hp.o_V = o.flag("Solidification", "V", false);
       hp.o_dTdt = o.flag("Solidification", "dTdt", false); hp.o_eqFrac = o.flag("Solidification", "eqFrac", false);
       hp.o_depth = o.flag("Solidification", "depth", false); hp.o_numMelt = o.flag("Solidification", "numMelt", false);
-      if (o.flag("Solidification", "RDF", false) || o.flag("Solidification", "MP_Stats", false)) {
-        err = "RDF and MP_Stats outputs are not supported"; return false;
-      }
-      hp.do_sol = hp.mode == 1 && (hp.o_tSol || hp.o_G || hp.o_V || hp.o_Gx || hp.o_Gy || hp.o_Gz || hp.o_dTdt || hp.o_eqFrac);
+      hp.o_rdf = o.flag("Solidification", "RDF", false);
+      if (o.flag("Solidification", "MP_Stats", false)) { err = "MP_Stats output is not supported"; return false; }
+      // every solidification output, RDF too, turns the solidification fields on (src/Grid.h:180-241)
+      hp.do_sol = hp.mode == 1 && (hp.o_tSol || hp.o_G || hp.o_V || hp.o_Gx || hp.o_Gy || hp.o_Gz || hp.o_dTdt ||
+                                   hp.o_eqFrac || hp.o_rdf);
     }
     // settings (src/Init.cpp:772-814) and r_max (src/Util.cpp:145-166)
     {

@@ -92,6 +92,14 @@ struct RunState {
   cudaEvent_t ev_rr[2] = {nullptr, nullptr};   // around the latest pass
   bool rr_timed = true;
   double ms_rrdf = 0;
+  // RDF: the melt-event logs of the two launch buffers (Surface runs) and the events of the
+  // run so far, every record's solidification time and cooling rate, all on the device
+  int2* tm_log[2] = {nullptr, nullptr};
+  int pending_tm[2] = {0, 0};
+  int2* tm_all = nullptr;
+  long long tm_total = 0, tm_all_cap = 0;
+  RdfSol* rdf_sol = nullptr;
+  long long rdf_total = 0, rdf_sol_cap = 0;
 };
 
 void th_release_run_state(th_ctx* ctx) {
@@ -112,6 +120,7 @@ void th_release_run_state(th_ctx* ctx) {
   if (r->h_row_base) cudaFreeHost(r->h_row_base);
   cudaFree(r->d_rscratch); cudaFree(r->d_rvals);
   cudaFree(r->r_idx); cudaFree(r->r_ts); cudaFree(r->r_Ts);
+  cudaFree(r->tm_all); cudaFree(r->rdf_sol);
   for (int e = 0; e < 2; ++e) if (r->ev_rr[e]) cudaEventDestroy(r->ev_rr[e]);
   for (int b = 0; b < 2; ++b)
     for (int e = 0; e < 2; ++e) {
@@ -207,6 +216,12 @@ th_status init_run(th_ctx* ctx) {
       if (v > 0) S.queue_cap = std::min(S.queue_cap, v);
     }
     ALLOC(S.queue, (size_t)S.queue_cap, 0);
+  }
+  if (hp.o_rdf && hp.tracking == TH_TRACK_SURFACE) {   // melt events (only Surface's reset sweep opens them)
+    ALLOC(S.rdf_open, n, 0);
+    S.tm_cap = 1 << 20;
+    ALLOC(r->tm_log[0], (size_t)S.tm_cap, 0);
+    ALLOC(r->tm_log[1], (size_t)S.tm_cap, 0);
   }
   // Stork queues no records: its buffers stay token-sized
   const int rec_alloc = stork ? 64 : kRecCap;
@@ -404,6 +419,7 @@ th_status read_counters(th_ctx* ctx, RunState* r, TrackCounters* h) {
   if (err & 32) return th_fail(ctx, TH_ERR_CAPACITY, "solidification record queue overflowed");
   if (err & 1) return th_fail(ctx, TH_ERR_CAPACITY, "a solidification node list exceeded its buffer");
   if (err & 64) return th_fail(ctx, TH_ERR_CAPACITY, "a tracking list overflowed");
+  if (err & 256) return th_fail(ctx, TH_ERR_CAPACITY, "the RDF melt-event log overflowed");
   if (err & 128) return th_fail(ctx, TH_ERR_CAPACITY, "the per-step work queue overflowed");
   if (err & 16) {
     char b[256];
@@ -511,13 +527,39 @@ th_status solidify_buffer(th_ctx* ctx, RunState* r, int b, int nrec, cudaStream_
   if (!r->sol_timed[b]) { add_elapsed(r->ms_solid, r->ev_sol[b][0], r->ev_sol[b][1]); r->sol_timed[b] = true; }
   r->sol_timed[b] = false;
   cudaEventRecord(r->ev_sol[b][0], s);
+  nrec = std::min(nrec, r->S.rec_cap);
   if (nrec > 0) {
-    th_launch_solidify(ctx->dp, r->S, r->win[b].W, r->rec[b], std::min(nrec, r->S.rec_cap), ctx->precision,
-                       ctx->hp.do_sol, s);
+    TrackState S = r->S;
+    if (ctx->hp.o_rdf) {                  // RDF: every record's time and rate, at the run's record count
+      if (r->rdf_total + nrec > r->rdf_sol_cap) {
+        const long long cap = std::max<long long>(r->rdf_total + nrec, std::max<long long>(2 * r->rdf_sol_cap, 1 << 16));
+        th_status st = grow(ctx, &r->rdf_sol, (size_t)cap, (size_t)r->rdf_total, s);
+        if (st != TH_OK) return st;
+        r->rdf_sol_cap = cap;
+      }
+      S.rdf_sol = r->rdf_sol;
+      S.rdf_base = r->rdf_total;
+      r->rdf_total += nrec;
+    }
+    th_launch_solidify(ctx->dp, S, r->win[b].W, r->rec[b], nrec, ctx->precision, ctx->hp.do_sol, s);
     th_status st = th_cuda_check(ctx, cudaGetLastError(), "solidify");
     if (st != TH_OK) return st;
   }
   th_status st = th_cuda_check(ctx, cudaMemsetAsync(&r->S.C->rec_n[b], 0, sizeof(int), s), "cudaMemsetAsync");
+  if (st == TH_OK && r->tm_log[b] && r->pending_tm[b] > 0) {     // RDF: this launch's melt events
+    const int m = std::min(r->pending_tm[b], r->S.tm_cap);
+    if (r->tm_total + m > r->tm_all_cap) {
+      const long long cap = std::max<long long>(r->tm_total + m, std::max<long long>(2 * r->tm_all_cap, 1 << 16));
+      if ((st = grow(ctx, &r->tm_all, (size_t)cap, (size_t)r->tm_total, s)) != TH_OK) return st;
+      r->tm_all_cap = cap;
+    }
+    st = th_cuda_check(ctx, cudaMemcpyAsync(r->tm_all + r->tm_total, r->tm_log[b], m * sizeof(int2), cudaMemcpyDeviceToDevice,
+                                            s), "cudaMemcpyAsync");
+    if (st != TH_OK) return st;
+    r->tm_total += m;
+    r->pending_tm[b] = 0;
+    st = th_cuda_check(ctx, cudaMemsetAsync(&r->S.C->tm_n[b], 0, sizeof(int), s), "cudaMemsetAsync");
+  }
   if (st == TH_OK && ctx->hp.tracking == TH_TRACK_STORK) st = rrdf_buffer(ctx, r, b, s);
   cudaEventRecord(r->ev_sol[b][1], s);
   r->records += nrec;
@@ -552,6 +594,7 @@ th_status advance_tracking(th_ctx* ctx, int64_t stop_at) {
     S.rec_n = &r->S.C->rec_n[b];
     S.rlog = r->rlog[b];
     S.rlog_off = r->rlog_off[b];
+    if (r->tm_log[b]) { S.tm_log = r->tm_log[b]; S.tm_n = &r->S.C->tm_n[b]; }
     cudaEventRecord(r->ev_trk[b][0], ts);
     st = th_cuda_check(ctx, th_launch_track(ctx->dp, S, w.W, w.base, w.base + w.n, ctx->precision, r->S.rec_cap / 2, ts),
                        "cooperative launch");
@@ -582,6 +625,7 @@ th_status advance_tracking(th_ctx* ctx, int64_t stop_at) {
     const int k_new = h.step;
     if (k_new <= r->k && !h.done) return th_fail(ctx, TH_ERR_INVALID, "solidification loop made no progress");
     r->rr_k0[b] = w.base;
+    r->pending_tm[b] = h.tm_n[b];
     r->rr_n[b] = ctx->hp.tracking == TH_TRACK_STORK ? k_new - w.base : 0;
     r->k = k_new;
     r->done = h.done != 0;
@@ -597,7 +641,7 @@ th_status advance_tracking(th_ctx* ctx, int64_t stop_at) {
   // drain: both record buffers, then wait for both streams
   for (int i = 0; i < 2; ++i) {
     const int bb = b ^ 1 ^ i;       // the older buffer first
-    if (pending_rec[bb] > 0 || r->rr_n[bb] > 0) {
+    if (pending_rec[bb] > 0 || r->rr_n[bb] > 0 || r->pending_tm[bb] > 0) {
       cudaStreamWaitEvent(as, r->ev_trk[bb][1], 0);
       if ((st = solidify_buffer(ctx, r, bb, pending_rec[bb], as)) != TH_OK) return st;
       pending_rec[bb] = 0;
@@ -652,9 +696,46 @@ int field_id(const std::string& f) {
   return -1;
 }
 
+// RDF: every point's melt events as the reference's Grid holds them (src/Grid.h:103-105,
+// 360-362), sorted by point, then step: the melting times - events logged before the last
+// step run, as t - dt of the step after them (the reference pushes them at the start of
+// that step) - and every solidification's time and cooling rate.
+struct RdfHost {
+  std::vector<std::pair<int, double>> tm;   // (point, melting time)
+  std::vector<RdfSol> sol;                  // (point, step, solidification time, cooling rate)
+};
+
+th_status gather_rdf(th_ctx* ctx, RdfHost& h) {
+  RunState* r = ctx->run;
+  std::vector<int2> ev((size_t)r->tm_total);
+  h.sol.assign((size_t)r->rdf_total, RdfSol{});
+  th_status st = TH_OK;
+  if (!ev.empty() && (st = th_cuda_check(ctx, cudaMemcpy(ev.data(), r->tm_all, ev.size() * sizeof(int2),
+                                                         cudaMemcpyDeviceToHost), "cudaMemcpy")) != TH_OK)
+    return st;
+  if (!h.sol.empty() && (st = th_cuda_check(ctx, cudaMemcpy(h.sol.data(), r->rdf_sol, h.sol.size() * sizeof(RdfSol),
+                                                            cudaMemcpyDeviceToHost), "cudaMemcpy")) != TH_OK)
+    return st;
+  const int last = r->k - 1;
+  std::sort(ev.begin(), ev.end(), [](const int2& a, const int2& b) { return a.x != b.x ? a.x < b.x : a.y < b.y; });
+  h.tm.clear();
+  for (const int2& e : ev)
+    if (e.y < last) h.tm.push_back({e.x, time_of(r, ctx->hp.dt, e.y + 1) - ctx->hp.dt});
+  std::sort(h.sol.begin(), h.sol.end(),
+            [](const RdfSol& a, const RdfSol& b) { return a.p != b.p ? a.p < b.p : a.step < b.step; });
+  return TH_OK;
+}
+
 th_status fetch_field(th_ctx* ctx, int id, double* out) {
   RunState* r = ctx->run;
   th_status st = TH_OK;
+  if (id == F_NUMMELT && ctx->hp.o_rdf) {    // with RDF the count is the number of melting times (src/Grid.h:343-350)
+    RdfHost h;
+    if ((st = gather_rdf(ctx, h)) != TH_OK) return st;
+    std::fill(out, out + ctx->hp.pnum, 0.0);
+    for (const auto& e : h.tm) out[e.first] += 1.0;
+    return TH_OK;
+  }
   if (!r->d_field) {
     st = th_cuda_check(ctx, cudaMalloc(&r->d_field, ctx->hp.pnum * sizeof(double)), "cudaMalloc");
     if (st != TH_OK) return st;
@@ -666,6 +747,38 @@ th_status fetch_field(th_ctx* ctx, int id, double* out) {
                                           ctx->stream), "cudaMemcpyAsync");
   if (st != TH_OK) return st;
   return th_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "field");
+}
+
+// Grid::Output_RDF (src/Grid.cpp:176-201): per output point, per melting time, the point's
+// coordinates, the melting time, and the solidification time and cooling rate of the same
+// index.  Where a point has more melting than solidification times the reference reads past
+// the end of its vectors; those rows get 0 here.
+th_status write_rdf_csv(th_ctx* ctx, const std::string& tag) {
+  RdfHost h;
+  th_status st = gather_rdf(ctx, h);
+  if (st != TH_OK) return st;
+  std::vector<double> flagd(ctx->hp.pnum);
+  if ((st = fetch_field(ctx, F_FLAG, flagd.data())) != TH_OK) return st;
+  std::vector<int64_t> pts;
+  std::vector<double> tm, tl, cr;
+  size_t a = 0, b = 0;
+  while (a < h.tm.size()) {
+    const int p = h.tm[a].first;
+    while (b < h.sol.size() && h.sol[b].p < p) ++b;
+    size_t e = 0;
+    for (; a < h.tm.size() && h.tm[a].first == p; ++a, ++e) {
+      if (flagd[p] == 0.0) continue;
+      const bool has = b + e < h.sol.size() && h.sol[b + e].p == p;
+      pts.push_back(p);
+      tm.push_back(h.tm[a].second);
+      tl.push_back(has ? h.sol[b + e].tsol : 0.0);
+      cr.push_back(has ? h.sol[b + e].cr : 0.0);
+    }
+  }
+  std::string err;
+  if (!th_write_rdf_csv(ctx->hp, tag, pts.data(), tm.data(), tl.data(), cr.data(), (int64_t)pts.size(), err))
+    return th_fail(ctx, TH_ERR_IO, err);
+  return TH_OK;
 }
 
 th_status write_solidification_csv(th_ctx* ctx, const std::string& tag) {
@@ -754,6 +867,7 @@ th_status th_run_reset(th_ctx* ctx) {
   r->sol_timed[0] = r->sol_timed[1] = true;
   r->ms_nodes = r->ms_track = r->ms_solid = r->ms_device = 0;
   r->rows = 0; r->rr_n[0] = r->rr_n[1] = 0; r->rr_timed = true; r->ms_rrdf = 0;
+  r->tm_total = 0; r->rdf_total = 0; r->pending_tm[0] = r->pending_tm[1] = 0;
   r->windows = r->records = 0;
   st = th_cuda_check(ctx, cudaMemsetAsync(ctx->d_pairs, 0, 2 * sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
   if (st != TH_OK) return st;
@@ -829,6 +943,38 @@ th_status th_rrdf(th_ctx* ctx, uint32_t* idx, double* ts, double* Ts, int64_t ca
   return TH_OK;
 }
 
+th_status th_rdf(th_ctx* ctx, int32_t* counts, double* vals, int64_t cap, int64_t* nvals) {
+  if (!ctx) return th_fail(ctx, TH_ERR_INVALID, "null context");
+  if (!ctx->hp.o_rdf) return th_fail(ctx, TH_ERR_INVALID, "the deck does not ask for RDF output");
+  if (!ctx->run) return th_fail(ctx, TH_ERR_INVALID, "run th_solidify first");
+  th_status st = th_cuda_check(ctx, cudaSetDevice(ctx->device), "cudaSetDevice");
+  if (st != TH_OK) return st;
+  RdfHost h;
+  if ((st = gather_rdf(ctx, h)) != TH_OK) return st;
+  const int64_t n = (int64_t)(h.tm.size() + 2 * h.sol.size());
+  if (nvals) *nvals = n;
+  if (counts) {
+    std::fill(counts, counts + 3 * ctx->hp.pnum, 0);
+    for (const auto& e : h.tm) counts[3 * (int64_t)e.first] += 1;
+    for (const RdfSol& e : h.sol) { counts[3 * (int64_t)e.p + 1] += 1; counts[3 * (int64_t)e.p + 2] += 1; }
+  }
+  if (vals) {
+    int64_t o = 0;
+    size_t a = 0, b = 0;
+    while ((a < h.tm.size() || b < h.sol.size()) && o < cap) {
+      const int p = std::min(a < h.tm.size() ? h.tm[a].first : INT_MAX, b < h.sol.size() ? h.sol[b].p : INT_MAX);
+      size_t a1 = a, b1 = b;
+      while (a1 < h.tm.size() && h.tm[a1].first == p) ++a1;
+      while (b1 < h.sol.size() && h.sol[b1].p == p) ++b1;
+      for (size_t i = a; i < a1 && o < cap; ++i) vals[o++] = h.tm[i].second;
+      for (size_t i = b; i < b1 && o < cap; ++i) vals[o++] = h.sol[i].tsol;
+      for (size_t i = b; i < b1 && o < cap; ++i) vals[o++] = h.sol[i].cr;
+      a = a1; b = b1;
+    }
+  }
+  return TH_OK;
+}
+
 th_status th_simulate(th_ctx* ctx) {
   if (!ctx) return th_fail(ctx, TH_ERR_INVALID, "null context");
   const HostProblem& hp = ctx->hp;
@@ -866,7 +1012,7 @@ th_status th_simulate(th_ctx* ctx) {
     if ((st = th_rrdf(ctx, idx.data(), ts.data(), Ts.data(), n, &got)) != TH_OK) return st;
     std::string err;
     if (!th_write_rrdf_csv(hp, "RRDF", idx.data(), ts.data(), Ts.data(), n, err)) return th_fail(ctx, TH_ERR_IO, err);
-    return TH_OK;
+    return hp.o_rdf ? write_rdf_csv(ctx, "RDF.Final") : TH_OK;
   }
   // intermediate outputs every OutputFrequency steps (src/Run.cpp:446-458, 553-565, 689-701)
   const std::string prefix = hp.tracking == TH_TRACK_SURFACE ? "Solidification." : "";
@@ -888,7 +1034,9 @@ th_status th_simulate(th_ctx* ctx) {
     if (freq != INT_MAX && freq > 0 && last > 0 && last % freq == 0)
       if ((st = write_solidification_csv(ctx, prefix + th_zero_pad((int)last, 7))) != TH_OK) return st;
   }
-  return write_solidification_csv(ctx, "Solidification.Final");
+  if ((st = write_solidification_csv(ctx, "Solidification.Final")) != TH_OK) return st;
+  // the reduced data after the grid's fields (bin/Main.cpp:104-119)
+  return hp.o_rdf ? write_rdf_csv(ctx, "RDF.Final") : TH_OK;
 }
 
 }  // extern "C"

@@ -597,18 +597,20 @@ __device__ void finish_step(const DevProblem& P, const TrackState& S, const Step
   const int items = X.n_init + (int)((v >> 24) & kField);
   if (items > C->max_items) C->max_items = items;
   const int n_next = __ldcg(X.lo_n), n_rec = __ldcg(S.rec_n);
+  const bool tm_full = S.tm_n != nullptr && __ldcg(S.tm_n) > S.tm_cap / 2;   // RDF melt events
   unsigned long long flags = 0;
   // Stork: the end of the step's list in the launch's log; a log that could not take another
   // whole list ends the launch like a full record buffer
   const bool log_full = S.rlog != nullptr && X.log_out + n_next > S.rlog_cap - S.rlog_step_max;
   if (S.rlog != nullptr) S.rlog_off[X.log_j + 1] = X.log_out + n_next;
   if (X.t > P.end_time && n_next == 0) { flags |= 1u; C->done = 1; }
-  else if (n_rec > high_water || log_full) { flags |= 2u; C->stop = 1; }
+  else if (n_rec > high_water || log_full || tm_full) { flags |= 2u; C->stop = 1; }
   __threadfence();
   st_release_u64(&C->fin, ((unsigned long long)n_next << 34) | (flags << 32) | X.stamp);
 }
 
 __device__ __forceinline__ void push_rec(const TrackState& S, const StepCtx& X, int p, double T, double Tl) {
+  if (S.rdf_open) S.rdf_open[p] -= 1;               // RDF: a solidification time follows
   const int b = atomicAdd(&X.bb->nrec, 1);
   if (b < kBlkRec) {
     SolRec& r = X.bb->rec[b];
@@ -617,6 +619,18 @@ __device__ __forceinline__ void push_rec(const TrackState& S, const StepCtx& X, 
   } else {
     push_record(S, p, X.k, X.t, T, Tl);
   }
+}
+
+// RDF of Surface runs: point q, evaluated liquid in this step, opens a melt event unless
+// one is open - the next step's reset sweep pushes t - dt while the point has as many
+// melting as solidification times (src/Run.cpp:604-609, src/Grid.h:400-404).  Called by the
+// lane that stores q's T, after any solidification of q in the same item (an item is the
+// only one to touch its point in a step, so the step's order is kept).
+__device__ __forceinline__ void rdf_melt(const TrackState& S, const StepCtx& X, int q) {
+  if (S.rdf_open == nullptr || S.rdf_open[q] != 0) return;
+  S.rdf_open[q] = 1;
+  const int j = atomicAdd(S.tm_n, 1);
+  if (j < S.tm_cap) S.tm_log[j] = make_int2(q, X.k); else atomicOr(S.err, ERR_RDF);
 }
 
 // Appends the block's buffered records to the launch's record buffer (all threads of the
@@ -824,6 +838,7 @@ __device__ int depth_walk(const DevProblem& P, const TrackState& S, const StepCt
     pairs += X.nn;
     if (lane == 0) set_T(S, top - d, T, X.k);
     if (!T.liquid) break;
+    if (lane == 0) rdf_melt(S, X, top - d);
     none_deeper = false;
   }
   EvalT Tl4[4];                                       // the up layers' T at t - dt (below D)
@@ -864,6 +879,7 @@ __device__ int depth_walk(const DevProblem& P, const TrackState& S, const StepCt
       if (d != D) { Tl = pick4(Tl4, ub - d).T; pairs += X.nnl; }
       if (lane == 0) push_rec(S, X, q, T.T, Tl);
     } else {
+      if (lane == 0) rdf_melt(S, X, q);
       break;
     }
   }
@@ -984,6 +1000,7 @@ __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx&
     double Tl = Told;
     if (aux) { Tl = eval_T<PREC>(P, S, X, X.nbl, X.nnl, p, X.stl).T; pairs += X.nnl; }
     if (lane == 0) push_rec(S, X, p, T.T, Tl);
+    if (lane == 0 && T.liquid) rdf_melt(S, X, p);      // solidified while still liquid
     return 0;
   }
   // Surface re-tests expand whatever their temperature (src/Run.cpp:655): the claims are
@@ -1019,6 +1036,7 @@ __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx&
   if (T.liquid) {
     int slot = 0;
     if (lane == 0) slot = atomicAdd(X.lo_n, 1);
+    if (TM == TM_SURFACE && lane == 0) rdf_melt(S, X, p);
     // Volume expands the liquid points; Surface the liquid visits (re-tests did above)
     // Volume items keep one claimed neighbour to run next in the same warp; Surface items
     // publish all of them (a kept child would wait for the rest of a long re-test or depth
@@ -1738,10 +1756,14 @@ __device__ __forceinline__ bool stop_test_decided(const DevProblem& P, double T_
 
 // G, the unit gradient, dT/dt (the reference's int abs), V and eqFrac of point p from the
 // gradient sums at tsol (src/Grid.cpp:522-548), stored in the output fields.
+__device__ __forceinline__ double cool_rate(const DevProblem& P, const PointSums& ps) {
+  return int_abs(rn_add(rn_mul(P.a, ps.lap), ps.dtt));
+}
+
 __device__ __forceinline__ void store_fields(const DevProblem& P, const TrackState& S, int p, double tsol,
                                              const PointSums& ps) {
   const double G = sqrt(ps.gx * ps.gx + ps.gy * ps.gy + ps.gz * ps.gz);
-  const double dTdt = int_abs(rn_add(rn_mul(P.a, ps.lap), ps.dtt));
+  const double dTdt = cool_rate(P, ps);
   const double V = dTdt / G;
   const double kPi = 3.14159265358979323846;
   const double eq = 1.0 - exp((-4 * kPi * P.cetN0 / 3) * pow(G * (P.cetn + 1) / (pow(P.ceta * V, 1 / P.cetn)), -3.0));
@@ -1781,7 +1803,9 @@ __global__ void __launch_bounds__(128, 4) k_solidify(DevProblem P, TrackState S,
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nrec) return;
   const SolRec r = rec[i];
-  if (S.sol_step[r.p] != r.step) return;            // a later record of this point wins
+  // a later record of this point sets its fields; RDF keeps every record's time and rate
+  const bool latest = S.sol_step[r.p] == r.step;
+  if (!latest && S.rdf_sol == nullptr) return;
   double x, y, z;
   point_xyz(P, r.p, x, y, z);
   unsigned long long pairs = 0;
@@ -1811,7 +1835,8 @@ __global__ void __launch_bounds__(128, 4) k_solidify(DevProblem P, TrackState S,
       if (j < S.rec_cap) S.redo[j] = RedoRec{i, why};
     }
   }
-  store_fields(P, S, r.p, tsol, ps);
+  if (latest) store_fields(P, S, r.p, tsol, ps);
+  if (S.rdf_sol) S.rdf_sol[S.rdf_base + i] = RdfSol{r.p, r.step, tsol, cool_rate(P, ps)};
   atomicAdd(S.pairs, pairs);
   atomicAdd(S.pairs + 1, pairs);
   if (err) atomicOr(S.err, err);
@@ -1939,8 +1964,10 @@ __global__ void __launch_bounds__(kGenThreads, 2) k_solidify_redo(DevProblem P, 
   unsigned long long pairs = 0;
   int err = 0;
   for (int e = blockIdx.x; e < n; e += gridDim.x) {
-    const SolRec r = rec[all > 0 ? e : S.redo[e].i];
-    if (all > 0 && S.sol_step[r.p] != r.step) continue;    // block-uniform: a later record wins
+    const int ri = all > 0 ? e : S.redo[e].i;
+    const SolRec r = rec[ri];
+    const bool latest = S.sol_step[r.p] == r.step;
+    if (all > 0 && !latest && S.rdf_sol == nullptr) continue;   // block-uniform: a later record wins
     double x, y, z;
     point_xyz(P, r.p, x, y, z);
     const int slot = r.step - W.base + 1;
@@ -1966,7 +1993,8 @@ __global__ void __launch_bounds__(kGenThreads, 2) k_solidify_redo(DevProblem P, 
       block_sums_at<true>(P, S, tsol, true, x, y, z, ps, sh, cs, red, bc, pairs, err);
     }
     if (threadIdx.x == 0) {
-      store_fields(P, S, r.p, tsol, ps);
+      if (latest) store_fields(P, S, r.p, tsol, ps);
+      if (S.rdf_sol) S.rdf_sol[S.rdf_base + ri] = RdfSol{r.p, r.step, tsol, cool_rate(P, ps)};
       if (all == 0) atomicAdd(&S.C->redo_total, 1ull);
     }
   }

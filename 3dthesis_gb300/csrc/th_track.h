@@ -18,6 +18,15 @@ struct SolRec {
   double Tl;       // temperature at the previous step (T_last)
 };
 
+// RDF (Output RDF 1): one solidification of a Surface run - its record's point and step, the
+// solidification time and the cooling rate (Grid::Solidify's add_RDF_tl / add_RDF_cr,
+// src/Grid.cpp:322,547) - and one melt event: a point still liquid when step `step` ended
+// (pushed at the start of the next step as t - dt, src/Run.cpp:604-609).
+struct RdfSol {
+  int32_t p, step;
+  double tsol, cr;
+};
+
 // A record of an FP32 run whose solidification is redone in FP64 (see k_solidify): the
 // record's index, and why (bit 0: the gradient or cooling-rate sum was ill-conditioned for
 // FP32 terms; bit 1: the solidification time was too sensitive to FP32 temperatures).
@@ -61,6 +70,7 @@ struct alignas(128) TrackCounters {
                                    // (both read with prof as its 19th and 20th words)
   alignas(128) int liq_n[3];     // liquid list lengths
   alignas(128) int rec_n[2];     // solidification records queued in each of the two record buffers
+  alignas(128) int tm_n[2];      // RDF melt events logged in each of the two event buffers
   // once step k is over: (next step's liquid-list length << 34) | (flags << 32) | (k + 1), flags
   // 1 finished run, 2 record high-water mark; low word 0xffffffff: aborted by a bounded wait
   alignas(128) unsigned long long fin;
@@ -93,6 +103,16 @@ struct TrackState {
   int redo_cap;            // (block b's at b * redo_cap), and per block its list's count and
   int redo_blocks;         // error bits (redo_aux[2 b], redo_aux[2 b + 1])
   int* redo_aux;
+  // RDF of Surface runs (null otherwise): per point the melt events opened minus the
+  // solidifications (the reference's tm count minus its tl count: an event opens only at
+  // 0), the launch's melt-event log (point, step) and its length, and the bulk
+  // solidification's per-record results at rdf_base + record index
+  int* rdf_open;
+  int2* tm_log;
+  int* tm_n;
+  int tm_cap;
+  RdfSol* rdf_sol;
+  long long rdf_base;
   // Stork: the launch's log of liquid lists (entries as in liq: point, column depth); list j
   // (j = 0: the liquid points of step k_begin - 1, then one per step run) spans
   // [rlog_off[j], rlog_off[j + 1]); null for the other forms
@@ -140,7 +160,7 @@ __device__ __forceinline__ NodeBufView slot_view(const NodeWindow& w, int slot) 
 enum { ERR_SEED_CAPACITY = 4 };
 
 // Error bits written by the solidification kernels (besides the node bits).
-enum { ERR_BARRIER = 16, ERR_RECORDS = 32, ERR_LISTS = 64, ERR_QUEUE = 128 };
+enum { ERR_BARRIER = 16, ERR_RECORDS = 32, ERR_LISTS = 64, ERR_QUEUE = 128, ERR_RDF = 256 };
 
 void th_launch_nodes_window(const DevProblem& P, const NodeWindow& w, int first_slot, int nslots, bool is_sol,
                             int* d_err, cudaStream_t s);

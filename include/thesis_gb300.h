@@ -157,6 +157,16 @@ th_status th_run_reset(th_ctx* ctx);
  * (33 values). */
 th_status th_run_stats(th_ctx* ctx, double* out, int32_t n);
 
+/* After th_solidify / th_simulate of a deck with Output RDF 1: the reduced data of the run
+ * so far as the reference's Grid holds it (Grid::get_RDF_tm / _tl / _cr,
+ * src/Grid.h:360-362): counts gets per point (3 * pnum values) its numbers of melting
+ * times, solidification times and cooling rates; vals gets, point by point in point order,
+ * its melting times, then solidification times, then cooling rates, each in time order (at
+ * most cap values); *nvals receives the number of values.  Melting times are kept by
+ * Surface tracking only (src/Run.cpp:604-609), as in the reference.  Either array may be
+ * null. */
+th_status th_rdf(th_ctx* ctx, int32_t* counts, double* vals, int64_t cap, int64_t* nvals);
+
 /* After th_solidify / th_simulate of a Stork deck (Tracking Stork): the doubly reduced data
  * of the run so far, the rows in step order and within a step in ascending cell index
  * (the reference's single-thread order).  Per row: idx the cell's (i, j, k) (3 values),
@@ -169,7 +179,8 @@ th_status th_rrdf(th_ctx* ctx, uint32_t* idx, double* ts, double* Ts, int64_t ca
 
 /* Whole run as the reference CLI does it: the mode loop, then the CSV files under
  * <deck dir>/Data (same names, columns and number format; a Stork deck writes
- * <name>.RRDF.csv in place of <name>.Solidification.Final.csv). */
+ * <name>.RRDF.csv in place of <name>.Solidification.Final.csv; Output RDF 1 adds
+ * <name>.RDF.Final.csv). */
 th_status th_simulate(th_ctx* ctx);
 
 /* Point x node pairs evaluated by this context so far (temperature and gradient sums). */

@@ -163,3 +163,57 @@ def compare_solidification(o, ref: dict, gpu: dict, *, T_tol: float, rel: float,
                 fail("G/V/dTdt against the oracle's run, same schedule, not explained by t_sol", solid[k],
                      dtSol=[float(ts_g[solid[i]] - ts_r[solid[i]]) for i in k[:max_listed]])
     return rep
+
+
+def compare_rdf(o, ref, gpu, *, rel: float, T_err: float, dt: float, threads: int = 0, max_listed: int = 8) -> dict:
+    """The reduced data of a run (Output RDF 1): ref = the oracle's (counts, vals, dT), gpu =
+    the library's (counts, vals).  Per point the same numbers of melting times, solidification
+    times and cooling rates; melting times (step times) equal; each solidification time
+    within the secant bound above; each cooling rate within ``rel`` (+ 1, its truncation) of
+    the oracle's at the GPU's own solidification time, and of the oracle's own except where
+    named by "schedule" or "t_sol" as for the fields."""
+    rep = {"violations": [], "counts": {}}
+    bad = rep["violations"]
+    cr_, vr, dT = ref
+    cg, vg = gpu
+    d = np.flatnonzero(np.any(cr_ != cg, axis=1))
+    if d.size:
+        bad.append({"check": "RDF counts", "n": int(d.size), "points": [int(i) for i in d[:max_listed]]})
+        return rep
+    n = cr_.sum(axis=1)
+    start = np.concatenate(([0], np.cumsum(n)[:-1]))
+    pts = np.flatnonzero(n)
+    tm_i = np.concatenate([start[p] + np.arange(cr_[p, 0]) for p in pts]) if pts.size else np.zeros(0, int)
+    tl_i = np.concatenate([start[p] + cr_[p, 0] + np.arange(cr_[p, 1]) for p in pts]) if pts.size else np.zeros(0, int)
+    cr_i = (np.concatenate([start[p] + cr_[p, 0] + cr_[p, 1] + np.arange(cr_[p, 2]) for p in pts]) if pts.size
+            else np.zeros(0, int))
+    sp = np.repeat(np.arange(cr_.shape[0]), cr_[:, 1])          # the point of each solidification
+    rep["counts"].update(melts=int(tm_i.size), solidifications=int(tl_i.size))
+    d = np.flatnonzero(vg[tm_i] != vr[tm_i])
+    if d.size:
+        bad.append({"check": "melting times", "n": int(d.size)})
+    tl_r, tl_g, c_r, c_g = vr[tl_i], vg[tl_i], vr[cr_i], vg[cr_i]
+    bound = dt * 2.0 * T_err / np.maximum(np.abs(dT), 1e-300) + 4 * np.spacing(np.abs(tl_r))
+    over = np.abs(tl_g - tl_r) > bound
+    if over.any():
+        bad.append({"check": "solidification times", "n": int(over.sum()), "points": [int(i) for i in sp[over][:max_listed]]})
+    want = o.solid_fields_many(sp, tl_g, threads=threads)["dTdt"] if sp.size else np.zeros(0)
+    off = _off("dTdt", c_g, want, rel, want)
+    if off.any():
+        bad.append({"check": "cooling rate at the GPU's time", "n": int(off.sum()),
+                    "points": [int(i) for i in sp[off][:max_listed]]})
+    off = _off("dTdt", c_g, c_r, rel, c_r)
+    rep["counts"]["off_by_schedule"] = rep["counts"]["off_by_tsol"] = 0
+    j = np.flatnonzero(off)
+    if j.size:
+        same = o.schedule(tl_r[j], True, threads=threads) == o.schedule(tl_g[j], True, threads=threads)
+        rep["counts"]["off_by_schedule"] = int((~same).sum())
+        k = j[same]
+        if k.size:
+            own = o.solid_fields_many(sp[k], tl_r[k], threads=threads)["dTdt"]
+            moved = _off("dTdt", want[k], own, rel, own)
+            rep["counts"]["off_by_tsol"] = int(moved.sum())
+            if (~moved).any():
+                bad.append({"check": "cooling rate against the oracle's, not explained", "n": int((~moved).sum()),
+                            "points": [int(i) for i in sp[k[~moved]][:max_listed]]})
+    return rep

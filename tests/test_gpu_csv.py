@@ -86,3 +86,60 @@ def test_simulate_writes_the_reference_files(built_library, thesis, oracle, tmp_
                 unit = 10.0 ** (np.floor(np.log10(max(abs(va), abs(vb)))) - 5)
                 assert abs(vb - v) <= _tol(col, v, prec) + 0.5 * unit, (fname, col, r, a[c], b[c], v)
                 assert abs(va - v) <= 1e-12 * abs(v) + 0.5 * unit, (fname, col, r, a[c], b[c], v)
+
+
+def _rdf_rows(counts, vals, flag):
+    """The reduced data's file rows (tm, tl, cr) from per-point counts and values, as
+    Grid::Output_RDF walks them: output points in order, per melting time."""
+    rows, at = [], 0
+    for p in np.flatnonzero(counts.sum(axis=1)):
+        a, b, c = counts[p]
+        at = int(at)
+        if flag[p]:
+            for e in range(a):
+                rows.append((vals[at + e], vals[at + a + e], vals[at + a + b + e]))
+        at += a + b + c
+    return rows
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_simulate_writes_the_reference_rdf_file(built_library, thesis, oracle, tmp_path, prec):
+    """Output RDF 1 on the small Surface deck: th_simulate adds Data/<name>.RDF.Final.csv
+    (Grid::Output_RDF, src/Grid.cpp:176-201, named by bin/Main.cpp:117) beside the
+    Solidification.Final file; the reference's file is in tests/golden/run_small_surface_rdf.npz.
+    Same header, rows, coordinates and melting times (text equal); where a solidification
+    time's or cooling rate's text differs, each file prints its own run's value (the GPU's
+    from th_rdf, the reference's = the oracle's) to half a printed unit - the two values are
+    compared, event by event, by test_gpu_solidify.py::test_rdf_matches_oracle."""
+    deck = make_golden.run_deck("small_surface_rdf")
+    path = deck.write(str(tmp_path / deck.name))
+    with thesis.Simulation(path, prec) as sim:
+        sim.simulate()
+        gcounts, gvals = sim.rdf()
+        gflag = sim.field("output_flag") > 0
+    data = os.path.join(os.path.dirname(path), "Data")
+    assert sorted(os.listdir(data)) == [f"{deck.name}.RDF.Final.csv", f"{deck.name}.Solidification.Final.csv"]
+    g = np.load(os.path.join(HERE, "golden", "run_small_surface_rdf.npz"))
+    ref_lines = bytes(g["rdf_file"]).decode().splitlines()
+    with open(os.path.join(data, f"{deck.name}.RDF.Final.csv")) as f:
+        got_lines = f.read().splitlines()
+    assert got_lines[0] == ref_lines[0]
+    assert len(got_lines) == len(ref_lines)
+    o = oracle(path)
+    o.solidify()
+    ocounts, ovals, _ = o.rdf()
+    ref_rows = _rdf_rows(ocounts, ovals, o.field("output_flag") > 0)
+    gpu_rows = _rdf_rows(gcounts, gvals, gflag)
+    assert len(ref_rows) == len(gpu_rows) == len(ref_lines) - 1
+    for r, (ra, rb) in enumerate(zip(ref_lines[1:], got_lines[1:])):
+        if ra == rb:
+            continue
+        a, b = ra.split(","), rb.split(",")
+        assert a[:4] == b[:4], (r, ra, rb)
+        for c in (4, 5):
+            if a[c] == b[c]:
+                continue
+            va, vb = float(a[c]), float(b[c])
+            unit = 10.0 ** (np.floor(np.log10(max(abs(va), abs(vb)))) - 5)
+            assert abs(vb - gpu_rows[r][c - 3]) <= 0.5 * unit * (1 + 1e-12), (r, c, b[c], gpu_rows[r][c - 3])
+            assert abs(va - ref_rows[r][c - 3]) <= 0.5 * unit * (1 + 1e-12), (r, c, a[c], ref_rows[r][c - 3])

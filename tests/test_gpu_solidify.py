@@ -32,10 +32,12 @@ def _fields(deck):
                                                "depth") if deck.outputs.get(f)]
 
 
-def _gpu_run(thesis, path, prec, fields, max_steps=0):
+def _gpu_run(thesis, path, prec, fields, max_steps=0, rdf=False):
     with thesis.Simulation(path, prec) as sim:
         steps = sim.solidify(max_steps=max_steps)
         out = {f: sim.field(f) for f in fields}
+        if rdf:
+            out["rdf"] = sim.rdf()
     out["steps"] = steps
     return out
 
@@ -52,7 +54,10 @@ def runs(built_library, thesis, oracle, tmp_path_factory):
         steps = o.solidify(threads=8)
         ref = {f: o.field(f) for f in _fields(deck)}
         ref["steps"] = steps
-        gpu = {prec: _gpu_run(thesis, path, prec, _fields(deck)) for prec in ("fp64", "fp32")}
+        rdf = bool(deck.outputs.get("RDF"))
+        if rdf:
+            ref["rdf"] = o.rdf()
+        gpu = {prec: _gpu_run(thesis, path, prec, _fields(deck), rdf=rdf) for prec in ("fp64", "fp32")}
         out[tag] = (deck, o, ref, gpu)
     return out
 
@@ -64,6 +69,25 @@ def test_run_matches_oracle(runs, tag, prec):
     rep = parity.compare_solidification(o, ref, gpu[prec], dt=deck.timestep, **TOL[prec])
     assert rep["counts"]["molten"] > 1000
     assert rep["violations"] == [], rep
+
+
+@pytest.mark.parametrize("tag", [t for t in CASES if t.endswith("_rdf")])
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_rdf_matches_oracle(runs, tag, prec):
+    """The reduced data (Output RDF 1): per point the same melting / solidification / cooling
+    rate counts, melting times equal, and the solidification times and cooling rates of every
+    melt event (not only the last) by the rules of the fields (tests/parity.py)."""
+    deck, o, ref, gpu = runs[tag]
+    tol = TOL[prec]
+    rep = parity.compare_rdf(o, ref["rdf"], gpu[prec]["rdf"], rel=tol["rel"], T_err=tol["T_err"], dt=deck.timestep)
+    assert rep["violations"] == [], rep
+    assert rep["counts"]["solidifications"] > 1000
+    if deck.tracking == "Surface":                 # only Surface tracking records melting times
+        assert rep["counts"]["melts"] == rep["counts"]["solidifications"]
+    else:
+        assert rep["counts"]["melts"] == 0
+    g = np.load(os.path.join(HERE, "golden", f"run_{tag}.npz"))     # and the reference's own counts
+    assert np.array_equal(gpu[prec]["rdf"][0].ravel(), g["rdf_counts"])
 
 
 @pytest.mark.parametrize("tag", CASES)
