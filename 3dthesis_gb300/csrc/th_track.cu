@@ -389,6 +389,11 @@ __device__ __forceinline__ unsigned long long globaltimer() {
 // ------------------------------------------------------------------ step work queue
 enum { IT_RETEST = 0, IT_VISIT = 2, IT_COLUMN = 3 };
 
+// Tracking forms of the loop: Volume, Surface, Surface logging RDF melt events, and Stork
+// (Surface's search without solidification, which logs the liquid columns for the doubly
+// reduced data).  Each is its own instantiation, so a form carries none of the others' work.
+enum { TM_VOLUME = 0, TM_SURFACE = 1, TM_STORK = 2, TM_SURFACE_RDF = 3 };
+
 struct StepCtx {
   Staged st, stl;          // this step's and the previous step's node lists in shared memory
   BlockBuf* bb;            // this block's buffered records
@@ -586,6 +591,7 @@ __device__ __forceinline__ bool step_over(unsigned long long v, int n_init, unsi
 // and the record queue's high-water mark, from the step's final counts - and publishes it
 // with the next step's liquid-list length and the step's stamp in one word, so a waiting
 // warp learns all three from the load that ends its wait.
+template <int TM>
 __device__ void finish_step(const DevProblem& P, const TrackState& S, const StepCtx& X, int k, unsigned long long v,
                             int high_water) {
   TrackCounters* C = S.C;
@@ -597,20 +603,21 @@ __device__ void finish_step(const DevProblem& P, const TrackState& S, const Step
   const int items = X.n_init + (int)((v >> 24) & kField);
   if (items > C->max_items) C->max_items = items;
   const int n_next = __ldcg(X.lo_n), n_rec = __ldcg(S.rec_n);
-  const bool tm_full = S.tm_n != nullptr && __ldcg(S.tm_n) > S.tm_cap / 2;   // RDF melt events
+  const bool tm_full = TM == TM_SURFACE_RDF && __ldcg(S.tm_n) > S.tm_cap / 2;   // RDF melt events
   unsigned long long flags = 0;
   // Stork: the end of the step's list in the launch's log; a log that could not take another
   // whole list ends the launch like a full record buffer
-  const bool log_full = S.rlog != nullptr && X.log_out + n_next > S.rlog_cap - S.rlog_step_max;
-  if (S.rlog != nullptr) S.rlog_off[X.log_j + 1] = X.log_out + n_next;
+  const bool log_full = TM == TM_STORK && X.log_out + n_next > S.rlog_cap - S.rlog_step_max;
+  if (TM == TM_STORK) S.rlog_off[X.log_j + 1] = X.log_out + n_next;
   if (X.t > P.end_time && n_next == 0) { flags |= 1u; C->done = 1; }
   else if (n_rec > high_water || log_full || tm_full) { flags |= 2u; C->stop = 1; }
-  __threadfence();
+  // the release store orders this lane's counter resets before the step-end word
   st_release_u64(&C->fin, ((unsigned long long)n_next << 34) | (flags << 32) | X.stamp);
 }
 
+template <bool RDF>
 __device__ __forceinline__ void push_rec(const TrackState& S, const StepCtx& X, int p, double T, double Tl) {
-  if (S.rdf_open) S.rdf_open[p] -= 1;               // RDF: a solidification time follows
+  if (RDF) S.rdf_open[p] -= 1;                       // RDF: a solidification time follows
   const int b = atomicAdd(&X.bb->nrec, 1);
   if (b < kBlkRec) {
     SolRec& r = X.bb->rec[b];
@@ -627,7 +634,7 @@ __device__ __forceinline__ void push_rec(const TrackState& S, const StepCtx& X, 
 // lane that stores q's T, after any solidification of q in the same item (an item is the
 // only one to touch its point in a step, so the step's order is kept).
 __device__ __forceinline__ void rdf_melt(const TrackState& S, const StepCtx& X, int q) {
-  if (S.rdf_open == nullptr || S.rdf_open[q] != 0) return;
+  if (S.rdf_open[q] != 0) return;
   S.rdf_open[q] = 1;
   const int j = atomicAdd(S.tm_n, 1);
   if (j < S.tm_cap) S.tm_log[j] = make_int2(q, X.k); else atomicOr(S.err, ERR_RDF);
@@ -800,7 +807,7 @@ __global__ void __launch_bounds__(kGenThreads, 2) k_nodes_window(DevProblem P, N
 // at a time ahead of it - the caller's first pass already holds D + 1 (down) and D (up) -
 // and only the layers the walk reaches are committed.  T at a layer does not depend on the
 // walk.
-template <int PREC>
+template <int PREC, bool RDF>
 __device__ int depth_walk(const DevProblem& P, const TrackState& S, const StepCtx& X, int p, int D,
                           const EvalT& first_down, const EvalT& first_up, unsigned long long& pairs) {
   const int lane = threadIdx.x & 31;
@@ -838,7 +845,7 @@ __device__ int depth_walk(const DevProblem& P, const TrackState& S, const StepCt
     pairs += X.nn;
     if (lane == 0) set_T(S, top - d, T, X.k);
     if (!T.liquid) break;
-    if (lane == 0) rdf_melt(S, X, top - d);
+    if (RDF && lane == 0) rdf_melt(S, X, top - d);
     none_deeper = false;
   }
   EvalT Tl4[4];                                       // the up layers' T at t - dt (below D)
@@ -877,9 +884,9 @@ __device__ int depth_walk(const DevProblem& P, const TrackState& S, const StepCt
     if (!T.liquid) {
       double Tl = Told;                                   // T of the previous step
       if (d != D) { Tl = pick4(Tl4, ub - d).T; pairs += X.nnl; }
-      if (lane == 0) push_rec(S, X, q, T.T, Tl);
+      if (lane == 0) push_rec<RDF>(S, X, q, T.T, Tl);
     } else {
-      if (lane == 0) rdf_melt(S, X, q);
+      if (RDF && lane == 0) rdf_melt(S, X, q);
       break;
     }
   }
@@ -972,10 +979,6 @@ __device__ int stork_walk(const DevProblem& P, const TrackState& S, const StepCt
   return d;
 }
 
-// Tracking forms of the loop: Volume, Surface and Stork (Surface's search without
-// solidification, which logs the liquid columns for the doubly reduced data).
-enum { TM_VOLUME = 0, TM_SURFACE = 1, TM_STORK = 2 };
-
 // One work item; returns the number of child items it published (already counted).
 // A beam-trace candidate arrives with its claim still in flight (the lane-0 result of the
 // atomic, `got`): the point is evaluated meanwhile and the item stops before any effect if
@@ -988,6 +991,7 @@ __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx&
                         int Dk, bool seed, bool got, unsigned long long& pairs, Kept& kept) {
   constexpr bool SURF = TM != TM_VOLUME;
   constexpr bool STORK = TM == TM_STORK;
+  constexpr bool RDF = TM == TM_SURFACE_RDF;
   constexpr bool RETEST_EXPANDS = SURF && !STORK;     // Surface: test_pts = last_liq_pts
   const int lane = threadIdx.x & 31;
   int nchild = 0;
@@ -999,8 +1003,8 @@ __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx&
     if (lane == 0) set_T(S, p, T, X.k);
     double Tl = Told;
     if (aux) { Tl = eval_T<PREC>(P, S, X, X.nbl, X.nnl, p, X.stl).T; pairs += X.nnl; }
-    if (lane == 0) push_rec(S, X, p, T.T, Tl);
-    if (lane == 0 && T.liquid) rdf_melt(S, X, p);      // solidified while still liquid
+    if (lane == 0) push_rec<RDF>(S, X, p, T.T, Tl);
+    if (RDF && lane == 0 && T.liquid) rdf_melt(S, X, p);   // solidified while still liquid
     return 0;
   }
   // Surface re-tests expand whatever their temperature (src/Run.cpp:655): the claims are
@@ -1036,7 +1040,7 @@ __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx&
   if (T.liquid) {
     int slot = 0;
     if (lane == 0) slot = atomicAdd(X.lo_n, 1);
-    if (TM == TM_SURFACE && lane == 0) rdf_melt(S, X, p);
+    if (RDF && lane == 0) rdf_melt(S, X, p);
     // Volume expands the liquid points; Surface the liquid visits (re-tests did above)
     // Volume items keep one claimed neighbour to run next in the same warp; Surface items
     // publish all of them (a kept child would wait for the rest of a long re-test or depth
@@ -1045,13 +1049,13 @@ __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx&
     // the depth walk under a liquid surface point needs nothing else from this step
     int Dn = 0;
     if (STORK) Dn = stork_walk<PREC>(P, S, X, p, D, T3[1], T3[2], pairs);
-    else if (SURF) Dn = depth_walk<PREC>(P, S, X, p, D, T3[1], T3[2], pairs);
+    else if (SURF) Dn = depth_walk<PREC, RDF>(P, S, X, p, D, T3[1], T3[2], pairs);
     if (lane == 0) push_liquid(S, X, slot, p, Dn);
     if (STORK && lane == 0) log_liquid(S, X, slot, p, Dn);
   } else if (STORK) {
     if (type == IT_RETEST && lane == 0) S.depths[p / P.nz] = 0;
   } else if (type == IT_RETEST) {          // cooled below T_L since the last step
-    if (lane == 0) push_rec(S, X, p, T.T, Told);
+    if (lane == 0) push_rec<RDF>(S, X, p, T.T, Told);
     if (SURF) {
       const int col = p / P.nz;
       for (int d0 = 1; d0 <= D; d0 += 32) {
@@ -1253,7 +1257,7 @@ __global__ void __launch_bounds__(track_bound<TM != TM_VOLUME>(), 1) k_track(Dev
         if (arrival_pending) {              // this block's entry, checked once its result is back
           arrival_pending = false;
           if (step_over(arrival + kArrive, X.n_init + hold, gridDim.x))
-            finish_step(P, S, X, k, arrival + kArrive, high_water);
+            finish_step<TM>(P, S, X, k, arrival + kArrive, high_water);
         }
         unsigned ticket = 0;
         if (lane == 0) ticket = atomicAdd(&X.qc->head, 1u);
@@ -1275,7 +1279,7 @@ __global__ void __launch_bounds__(track_bound<TM != TM_VOLUME>(), 1) k_track(Dev
           ready = __shfl_sync(0xffffffffu, ready, 0);
           finished = __shfl_sync(0xffffffffu, finished, 0);
           if (ready || finished) break;
-          backoff = backoff < 256 ? backoff * 2 : 256;
+          backoff = backoff < 64 ? backoff * 2 : 64;
           if (++idle > spin_limit) {
             if (lane == 0) {
               if (atomicOr(S.err, ERR_BARRIER) == 0) {        // first waiter to give up records its view
@@ -1335,7 +1339,7 @@ __global__ void __launch_bounds__(track_bound<TM != TM_VOLUME>(), 1) k_track(Dev
       }
       if (lane == 0) {                                           // completed, after the item's writes
         const unsigned long long st = atom_add_release(&X.qc->state, 1ull);
-        if (step_over(st + 1ull, X.n_init + hold, gridDim.x)) finish_step(P, S, X, k, st + 1ull, high_water);
+        if (step_over(st + 1ull, X.n_init + hold, gridDim.x)) finish_step<TM>(P, S, X, k, st + 1ull, high_water);
       }
       ++n_items;
       c_items += clock64() - c1;
@@ -2103,13 +2107,18 @@ static cudaError_t launch_track_t(const DevProblem& P, const TrackState& S, cons
 
 cudaError_t th_launch_track(const DevProblem& P, const TrackState& S, const NodeWindow& w, int k_begin, int k_end,
                             int precision, int rec_high_water, cudaStream_t s) {
-  const int tm = P.tracking == TH_TRACK_STORK ? TM_STORK : P.tracking == TH_TRACK_SURFACE ? TM_SURFACE : TM_VOLUME;
+  const int tm = P.tracking == TH_TRACK_STORK                           ? TM_STORK
+                 : P.tracking == TH_TRACK_SURFACE && S.rdf_open != nullptr ? TM_SURFACE_RDF
+                 : P.tracking == TH_TRACK_SURFACE                         ? TM_SURFACE
+                                                                          : TM_VOLUME;
   if (precision == 0) {
     if (tm == TM_STORK) return launch_track_t<0, TM_STORK>(P, S, w, k_begin, k_end, rec_high_water, s);
+    if (tm == TM_SURFACE_RDF) return launch_track_t<0, TM_SURFACE_RDF>(P, S, w, k_begin, k_end, rec_high_water, s);
     if (tm == TM_SURFACE) return launch_track_t<0, TM_SURFACE>(P, S, w, k_begin, k_end, rec_high_water, s);
     return launch_track_t<0, TM_VOLUME>(P, S, w, k_begin, k_end, rec_high_water, s);
   }
   if (tm == TM_STORK) return launch_track_t<1, TM_STORK>(P, S, w, k_begin, k_end, rec_high_water, s);
+  if (tm == TM_SURFACE_RDF) return launch_track_t<1, TM_SURFACE_RDF>(P, S, w, k_begin, k_end, rec_high_water, s);
   if (tm == TM_SURFACE) return launch_track_t<1, TM_SURFACE>(P, S, w, k_begin, k_end, rec_high_water, s);
   return launch_track_t<1, TM_VOLUME>(P, S, w, k_begin, k_end, rec_high_water, s);
 }
