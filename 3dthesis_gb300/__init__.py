@@ -45,7 +45,7 @@ EXPORTED = ("th_ctx_create_from_deck", "th_ctx_destroy", "th_last_error", "th_ge
             "th_batch_snapshot_device", "th_batch_set_tile_shape", "th_batch_autotune", "th_batch_pairs",
             "th_adj_create", "th_adj_destroy", "th_adj_last_error", "th_adj_num_params", "th_adj_params",
             "th_adj_host_nodes", "th_adj_forward", "th_adj_backward", "th_calc_T_times_device",
-            "th_device_rates", "th_rrdf", "th_rdf")
+            "th_device_rates", "th_rrdf", "th_rdf", "th_deck_info")
 
 
 class ThesisError(RuntimeError):
@@ -126,6 +126,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.th_device_rates.argtypes = [vp]
     L.th_rrdf.argtypes = [vp, vp, vp, vp, c_i64, ctypes.POINTER(c_i64)]
     L.th_rdf.argtypes = [vp, vp, vp, c_i64, ctypes.POINTER(c_i64)]
+    L.th_deck_info.argtypes = [ctypes.c_char_p, ctypes.POINTER(Info)]
     _lib = L
     return L
 
@@ -140,6 +141,44 @@ def device_rates() -> Dict[str, float]:
         raise ThesisError(st, L.th_last_error(None).decode())
     return {"sm_count": int(out[0]), "sm_max_mhz": float(out[1]), "ex2_per_sm_clk": float(out[2]),
             "fma_per_sm_clk": float(out[3])}
+
+
+def deck_info(param_input: str) -> Dict[str, float]:
+    """A deck's grid, mode and timing summary from host parsing alone (no context, no GPU):
+    th_deck_info."""
+    L = load_library()
+    info = Info()
+    st = L.th_deck_info(os.fspath(param_input).encode(), ctypes.byref(info))
+    if st != 0:
+        raise ThesisError(st, L.th_last_error(None).decode())
+    return {f: getattr(info, f) for f, _ in Info._fields_}
+
+
+def deck_weight(param_input: str) -> float:
+    """Work estimate of a deck for splitting decks across GPUs: points times snapshots
+    (Snapshots mode) or times timesteps (Solidification mode)."""
+    d = deck_info(param_input)
+    if d["mode"] == 0:
+        return float(d["pnum"]) * max(1, d["n_snapshots"])
+    return float(d["pnum"]) * max(1.0, d["end_time"] / d["dt"]) if d["dt"] > 0 else float(d["pnum"])
+
+
+def shard_decks(paths, rank: int, world: int, weights=None) -> list:
+    """The indices of the decks rank `rank` of `world` runs, in ascending order: decks are
+    dealt heaviest first to the least-loaded rank (ties to the lower rank, equal weights in
+    input order), so every rank computes the same partition from the same list and the
+    ranks exchange nothing.  Weights default to deck_weight."""
+    if not 0 <= rank < world:
+        raise ValueError(f"rank {rank} outside a world of {world}")
+    w = [deck_weight(p) for p in paths] if weights is None else [float(x) for x in weights]
+    load = [0.0] * world
+    mine = []
+    for i in sorted(range(len(w)), key=lambda i: (-w[i], i)):
+        r = min(range(world), key=lambda q: (load[q], q))
+        load[r] += w[i]
+        if r == rank:
+            mine.append(i)
+    return sorted(mine)
 
 
 def _ptr(a: Optional[np.ndarray]):

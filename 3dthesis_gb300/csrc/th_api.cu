@@ -190,9 +190,7 @@ void th_ctx_destroy(th_ctx* ctx) {
 
 const char* th_last_error(const th_ctx* ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
 
-th_status th_get_info(th_ctx* ctx, th_info* out) {
-  if (!ctx || !out) return th_fail(ctx, TH_ERR_INVALID, "null argument");
-  const HostProblem& hp = ctx->hp;
+static void fill_info(const HostProblem& hp, int precision, th_info* out) {
   std::memset(out, 0, sizeof(*out));
   out->nx = hp.nx; out->ny = hp.ny; out->nz = hp.nz; out->pnum = hp.pnum;
   out->n_beams = (int32_t)hp.beams.size();
@@ -200,7 +198,7 @@ th_status th_get_info(th_ctx* ctx, th_info* out) {
   out->mode = hp.mode; out->tracking = hp.tracking;
   out->dt = hp.dt; out->end_time = hp.end_time; out->T0 = hp.T0; out->TL = hp.TL;
   out->xmin = hp.xmin; out->xmax = hp.xmax; out->ymin = hp.ymin; out->ymax = hp.ymax; out->zmin = hp.zmin; out->zmax = hp.zmax;
-  out->precision = ctx->precision;
+  out->precision = precision;
   int f = 0;
   if (hp.o_T) f |= TH_OUT_T;
   if (hp.o_tSol) f |= TH_OUT_TSOL;
@@ -214,6 +212,26 @@ th_status th_get_info(th_ctx* ctx, th_info* out) {
   if (hp.o_depth) f |= TH_OUT_DEPTH;
   if (hp.o_numMelt) f |= TH_OUT_NUMMELT;
   out->out_flags = f;
+}
+
+th_status th_get_info(th_ctx* ctx, th_info* out) {
+  if (!ctx || !out) return th_fail(ctx, TH_ERR_INVALID, "null argument");
+  fill_info(ctx->hp, ctx->precision, out);
+  return TH_OK;
+}
+
+th_status th_deck_info(const char* param_input, th_info* out) {
+  if (!param_input || !out) {
+    g_create_error = "null argument";
+    return TH_ERR_INVALID;
+  }
+  HostProblem hp;
+  std::string err;
+  if (!th_load_deck(param_input, hp, err)) {
+    g_create_error = err;
+    return TH_ERR_INVALID;
+  }
+  fill_info(hp, -1, out);
   return TH_OK;
 }
 

@@ -78,6 +78,11 @@ th_status th_ctx_create_from_deck(const char* param_input, int32_t precision, th
 void th_ctx_destroy(th_ctx* ctx);
 const char* th_last_error(const th_ctx* ctx);
 th_status th_get_info(th_ctx* ctx, th_info* out);
+/* The same summary of a deck without a context or a GPU (host parsing only, as
+ * Init::ReadSimParams does, src/Init.cpp:33-908): what a launcher needs to split work
+ * across GPUs before any device is touched.  precision is reported as -1; errors go to
+ * th_last_error(NULL). */
+th_status th_deck_info(const char* param_input, th_info* out);
 double th_snapshot_time(th_ctx* ctx, int32_t idx);
 
 /* Quadrature nodes at time t (is_sol != 0: the refined solidification schedule).
