@@ -294,14 +294,14 @@ class Simulation:
 
     def run_stats(self) -> Dict[str, float]:
         """Device time (ms) and counters of the solidification loop so far."""
-        out = np.zeros(33)
-        self._check(self._lib.th_run_stats(self._ctx, _ptr(out), 33))
+        out = np.zeros(34)
+        self._check(self._lib.th_run_stats(self._ctx, _ptr(out), 34))
         keys = ("ms_nodes", "ms_track", "ms_solidify", "windows", "records", "max_items", "steps", "slot_cap",
                 "ms_device", "pairs_solidify", "pairs_total", "loop_ms_work", "loop_ms_barrier", "loop_items",
                 "loop_item_clocks", "loop_wait_clocks", "loop_depth_sum", "loop_steps", "loop_evals",
                 "loop_eval_clocks", "loop_ms_start0", "loop_ms_start1", "loop_ms_start2", "loop_ms_start3",
                 "loop_ms_end0", "loop_ms_end1", "loop_ms_end2", "loop_ms_end3", "loop_eval_nodes",
-                "records_redone_fp64", "guarded_decisions", "ms_rrdf", "rrdf_rows")
+                "records_redone_fp64", "guarded_decisions", "ms_rrdf", "rrdf_rows", "records_fixed_fp64")
         return dict(zip(keys, out.tolist()))
 
     def rdf(self):

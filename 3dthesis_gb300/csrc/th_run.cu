@@ -238,6 +238,9 @@ th_status init_run(th_ctx* ctx) {
   if (ctx->precision == TH_FP32_KAHAN || hp.compress) {
     ALLOC(S.redo, (size_t)kRecCap, 0);
     ALLOC(S.redo_n, 1, 0);
+    ALLOC(S.fix, (size_t)kRecCap, 0);
+    ALLOC(S.fix_n, 1, 0);
+    ALLOC(S.fix_T, (size_t)kRecCap, 0);
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -880,12 +883,12 @@ th_status th_run_stats(th_ctx* ctx, double* out, int32_t n) {
   unsigned long long pairs[2] = {0, 0};
   th_status st = th_cuda_check(ctx, cudaMemcpy(pairs, ctx->d_pairs, sizeof(pairs), cudaMemcpyDeviceToHost), "cudaMemcpy");
   if (st != TH_OK) return st;
-  unsigned long long prof[20] = {};     // the loop profile, then the FP64 redo and guard counts
+  unsigned long long prof[21] = {};     // the loop profile, then the FP64 redo, guard and fix counts
   if (r && r->S.C) {
     st = th_cuda_check(ctx, cudaMemcpy(prof, r->S.C->prof, sizeof(prof), cudaMemcpyDeviceToHost), "cudaMemcpy");
     if (st != TH_OK) return st;
   }
-  const double v[33] = {r ? r->ms_nodes : 0, r ? r->ms_track : 0, r ? r->ms_solid : 0, r ? (double)r->windows : 0,
+  const double v[34] = {r ? r->ms_nodes : 0, r ? r->ms_track : 0, r ? r->ms_solid : 0, r ? (double)r->windows : 0,
                         r ? (double)r->records : 0, r ? (double)r->max_items : 0, r ? (double)r->k : 0,
                         r ? (double)r->slot_cap : 0, r ? r->ms_device : 0, (double)pairs[1],
                         (double)pairs[0], prof[0] * 1e-6, prof[1] * 1e-6, (double)prof[2], (double)prof[3],
@@ -893,8 +896,8 @@ th_status th_run_stats(th_ctx* ctx, double* out, int32_t n) {
                         prof[10] * 1e-6, prof[11] * 1e-6, prof[12] * 1e-6, prof[13] * 1e-6,
                         prof[14] * 1e-6, prof[15] * 1e-6, prof[16] * 1e-6, prof[17] * 1e-6,
                         (double)prof[9], (double)prof[18], (double)prof[19],
-                        r ? r->ms_rrdf : 0, r ? (double)r->rows : 0};
-  for (int i = 0; i < n && i < 33; ++i) out[i] = v[i];
+                        r ? r->ms_rrdf : 0, r ? (double)r->rows : 0, (double)prof[20]};
+  for (int i = 0; i < n && i < 34; ++i) out[i] = v[i];
   return TH_OK;
 }
 

@@ -319,6 +319,117 @@ __device__ __forceinline__ void warp_T_n(const DevProblem& P, const TrackState& 
   }
 }
 
+// T at NP points anywhere on the grid (Volume tracking's batches: a chunk of re-tests, or the
+// neighbours one item claimed) from one node list, every lane returning the same values.
+// FP64: warp_T_n, whose FP64 form takes each point's own coordinates.  FP32: warp_T_n's
+// arithmetic with the x and y parts formed per point instead of once per column, so each
+// point's sum is bit for bit the one a pass over that point alone gives; the NP points'
+// independent sums are what keep a lane's pipes busy.
+template <int PREC, int NP>
+__device__ __forceinline__ void warp_T_gen(const DevProblem& P, const TrackState& S, const float2* ax,
+                                           const SlotRef& nb, int nn, const int (&pts)[NP], const Staged& st,
+                                           EvalT (&out)[NP]) {
+  if constexpr (PREC == 0) {
+    warp_T_n<0, NP>(P, S, ax, nb, nn, pts, st, out);
+  } else {
+    const int lane = threadIdx.x & 31;
+    const int n_sm = min(st.n_sm, nn);
+    unsigned long long Xh[NP], Xl[NP], Yh[NP], Yl[NP], Zh[NP], Zl[NP], s2[NP], c2[NP];
+    float x1[NP][2], y1[NP][2], z1[NP][2];
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+      const unsigned col = udiv((unsigned)pts[q], P.div_nz_m, P.div_nz_s);
+      const unsigned pi = udiv(col, P.div_ny_m, P.div_ny_s), pj = col - pi * (unsigned)P.ny;
+      const unsigned pk = min((unsigned)pts[q] - col * (unsigned)P.nz, (unsigned)P.nz - 1u);
+      const float2 X = ax[pi], Y = ax[P.nx + pj], Z = ax[P.nx + P.ny + pk];
+      x1[q][0] = X.x; x1[q][1] = X.y; y1[q][0] = Y.x; y1[q][1] = Y.y; z1[q][0] = Z.x; z1[q][1] = Z.y;
+      Xh[q] = pk2(X.x, X.x); Xl[q] = pk2(X.y, X.y);
+      Yh[q] = pk2(Y.x, Y.x); Yl[q] = pk2(Y.y, Y.y);
+      Zh[q] = pk2(Z.x, Z.x); Zl[q] = pk2(Z.y, Z.y);
+      s2[q] = c2[q] = 0ull;
+    }
+    const int cap4 = st.cap >> 2;
+    const ulonglong2* F = (const ulonglong2*)st.base;
+    const int ng = ((n_sm + kListPad - 1) & ~(kListPad - 1)) >> 2;
+    for (int g = lane; g < ng; g += 32) {
+      const ulonglong2 xh = F[g], yh = F[cap4 + g], zh = F[2 * cap4 + g], xl = F[3 * cap4 + g],
+                       yl = F[4 * cap4 + g], zl = F[5 * cap4 + g], kx = F[6 * cap4 + g], ky = F[7 * cap4 + g],
+                       kz = F[8 * cap4 + g], w = F[9 * cap4 + g];
+#pragma unroll
+      for (int q = 0; q < NP; ++q) {
+        const unsigned long long dxa = add2(sub2(Xh[q], xh.x), sub2(Xl[q], xl.x));
+        const unsigned long long dxb = add2(sub2(Xh[q], xh.y), sub2(Xl[q], xl.y));
+        const unsigned long long dya = add2(sub2(Yh[q], yh.x), sub2(Yl[q], yl.x));
+        const unsigned long long dyb = add2(sub2(Yh[q], yh.y), sub2(Yl[q], yl.y));
+        const unsigned long long ea = fma2(mul2(dya, dya), ky.x, mul2(mul2(dxa, dxa), kx.x));
+        const unsigned long long eb = fma2(mul2(dyb, dyb), ky.y, mul2(mul2(dxb, dxb), kx.y));
+        const unsigned long long dza = add2(sub2(Zh[q], zh.x), sub2(Zl[q], zl.x));
+        const unsigned long long dzb = add2(sub2(Zh[q], zh.y), sub2(Zl[q], zl.y));
+        const unsigned long long fa = fma2(mul2(dza, dza), kz.x, ea), fb = fma2(mul2(dzb, dzb), kz.y, eb);
+        float a0, a1, b0, b1;
+        upk2(fa, a0, a1);
+        upk2(fb, b0, b1);
+        const unsigned long long va = mul2(pk2(ex2_approx(a0), ex2_approx(a1)), w.x);
+        const unsigned long long vb = mul2(pk2(ex2_approx(b0), ex2_approx(b1)), w.y);
+        const unsigned long long y = sub2(add2(va, vb), c2[q]);
+        const unsigned long long t = add2(s2[q], y);
+        c2[q] = sub2(sub2(t, s2[q]), y);
+        s2[q] = t;
+      }
+    }
+    float hi[NP], lo[NP];
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+      float sl, sh, cl, ch;
+      upk2(s2[q], sl, sh);
+      upk2(c2[q], cl, ch);
+      hi[q] = sl;
+      lo[q] = -cl;
+      df_add_lazy(hi[q], lo[q], sh, -ch);
+    }
+    if (n_sm < nn) {                               // nodes past the staged copy, one per lane
+      float s1[NP], c1[NP];
+#pragma unroll
+      for (int q = 0; q < NP; ++q) s1[q] = c1[q] = 0.f;
+      for (int n = n_sm + lane; n < nn; n += 32) {
+        const float xh = nb.fv(NF_XH, n), yh = nb.fv(NF_YH, n), zh = nb.fv(NF_ZH, n), xl = nb.fv(NF_XL, n),
+                    yl = nb.fv(NF_YL, n), zl = nb.fv(NF_ZL, n), kx = nb.fv(NF_KX, n), ky = nb.fv(NF_KY, n),
+                    kz = nb.fv(NF_KZ, n), w = nb.fv(NF_W, n);
+#pragma unroll
+        for (int q = 0; q < NP; ++q) {
+          const float dx = (x1[q][0] - xh) + (x1[q][1] - xl), dy = (y1[q][0] - yh) + (y1[q][1] - yl);
+          const float exy = fmaf(dy * dy, ky, dx * dx * kx);
+          const float dz = (z1[q][0] - zh) + (z1[q][1] - zl);
+          const float v = ex2_approx(fmaf(dz * dz, kz, exy)) * w;
+          const float yy = v - c1[q];
+          const float tt = s1[q] + yy;
+          c1[q] = (tt - s1[q]) - yy;
+          s1[q] = tt;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < NP; ++q) df_add_lazy(hi[q], lo[q], s1[q], -c1[q]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+      for (int q = 0; q < NP; ++q) {
+        const float bh = __shfl_xor_sync(0xffffffffu, hi[q], o), bl = __shfl_xor_sync(0xffffffffu, lo[q], o);
+        df_add_lazy(hi[q], lo[q], bh, bl);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+      const float sh = hi[q];
+      hi[q] = sh + lo[q];
+      lo[q] = lo[q] - (hi[q] - sh);
+      const float d = ((hi[q] - P.tl_df[0]) + (lo[q] - P.tl_df[1])) - P.tl_df[2];
+      out[q].liquid = d >= 0.f;
+      out[q].T = pack_df(hi[q], lo[q]);
+    }
+  }
+}
+
 // a[i] of a four-entry register array without local-memory indexing.
 __device__ __forceinline__ EvalT pick4(const EvalT (&a)[4], int i) {
   return i == 0 ? a[0] : (i == 1 ? a[1] : (i == 2 ? a[2] : a[3]));
@@ -364,7 +475,8 @@ __device__ __forceinline__ void set_T(const TrackState& S, int p, const EvalT& e
   if (e.liquid) { S.outflag[p] = 1; S.last_liq[p] = step; }
 }
 
-// Bound on the polls of one wait for work (about 8 s at the longest back-off); past it the
+// Bound on the polls of one wait for work (seconds: each poll is an L2 round trip after its
+// back-off); past it the
 // waiter latches ERR_BARRIER and releases every warp of the launch.  The test knob
 // THESIS_GB300_SPIN_LIMIT lowers it.
 constexpr long long kSpinLimit = 1ll << 25;
@@ -387,7 +499,7 @@ __device__ __forceinline__ unsigned long long globaltimer() {
 }
 
 // ------------------------------------------------------------------ step work queue
-enum { IT_RETEST = 0, IT_VISIT = 2, IT_COLUMN = 3 };
+enum { IT_RETEST = 0, IT_VISIT = 2, IT_COLUMN = 3, IT_EXPAND = 4 };
 
 // Tracking forms of the loop: Volume, Surface, Surface logging RDF melt events, and Stork
 // (Surface's search without solidification, which logs the liquid columns for the doubly
@@ -1068,12 +1180,163 @@ __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx&
   return nchild;
 }
 
+// Volume items come in batches: the previous step's liquid points are re-tested kVolChunk at
+// a time, and an item evaluates the neighbours it claims itself, kVolBatch to a pass
+// (warp_T_gen), publishing only those found liquid, as IT_EXPAND items (a liquid point whose
+// neighbours are still to be claimed).  The sets of claims, evaluations and decisions are
+// the one-point-per-item loop's (src/Melt.cpp:185-269): a claim is the same atomic, and a
+// point's sum is bit for bit the same in a batch.
+constexpr int kVolChunk = 4;     // re-tests per initial item
+constexpr int kVolBatch = 4;     // points per evaluation pass
+constexpr int kVolCand = 18 * kVolChunk;   // most neighbours one item can claim
+static_assert(kVolChunk <= kVolBatch, "a chunk of re-tests is one pass");
+
+// One pass over the first n points of a batch (a pass of 1, 2 or 4 points; pts padded by
+// repeating a point).
+template <int PREC>
+__device__ __forceinline__ void vol_pass(const DevProblem& P, const TrackState& S, const StepCtx& X,
+                                         const int (&pts)[kVolBatch], int n, EvalT (&T)[kVolBatch]) {
+  static_assert(kVolBatch == 2 || kVolBatch == 4, "passes of 1, 2 or 4 points");
+  const long long c0 = clock64();
+  if (n == 1) {
+    const int p1[1] = {pts[0]};
+    EvalT t1[1];
+    warp_T_gen<PREC, 1>(P, S, X.ax, X.nb, X.nn, p1, X.st, t1);
+    T[0] = t1[0];
+  } else if (kVolBatch == 2 || n == 2) {
+    const int p2[2] = {pts[0], pts[1]};
+    EvalT t2[2];
+    warp_T_gen<PREC, 2>(P, S, X.ax, X.nb, X.nn, p2, X.st, t2);
+    T[0] = t2[0]; T[1] = t2[1];
+  } else {
+    if constexpr (kVolBatch == 4) warp_T_gen<PREC, 4>(P, S, X.ax, X.nb, X.nn, pts, X.st, T);
+  }
+  X.ev_c += clock64() - c0;
+  X.ev_n += 1;
+  X.ev_nodes += X.nn;
+}
+
+// Stores the T of the batch's first n points and returns which are liquid (bit q: pts[q]).
+template <int PREC>
+__device__ __forceinline__ unsigned vol_commit(const DevProblem& P, const TrackState& S, const StepCtx& X,
+                                               const int (&pts)[kVolBatch], int n, EvalT (&T)[kVolBatch],
+                                               unsigned long long& pairs) {
+  const int lane = threadIdx.x & 31;
+  unsigned liq = 0;
+#pragma unroll
+  for (int q = 0; q < kVolBatch; ++q) {
+    if (q >= n) break;
+    guard_T<PREC>(P, S, X, T[q], pts[q]);
+    pairs += X.nn;
+    if (lane == 0) set_T(S, pts[q], T[q], X.k);
+    if (T[q].liquid) liq |= 1u << q;
+  }
+  return liq;
+}
+
+// Claims the neighbours of the nE liquid points E (the same 3x3x{k-1, k} claims as
+// expand), evaluates the newly claimed ones in batches, adds the liquid ones to the next
+// step's list and publishes them as IT_EXPAND items (keeping one for this warp to run
+// next).  `cand` is the warp's slice of shared memory (kVolCand entries).
+template <int PREC>
+__device__ void vol_expand(const DevProblem& P, const TrackState& S, const StepCtx& X, const int (&E)[kVolChunk],
+                           int nE, int* cand, int& nchild, unsigned long long& pairs, Kept& kept) {
+  const int lane = threadIdx.x & 31;
+  Claims c[kVolChunk];
+#pragma unroll
+  for (int i = 0; i < kVolChunk; ++i)              // every claim in flight before any result is used
+    if (i < nE) c[i] = claim_neighbours<false>(P, S, X, E[i]);
+  int n = 0;
+#pragma unroll
+  for (int i = 0; i < kVolChunk; ++i) {
+    if (i >= nE) break;
+    const bool got = c[i].old < X.stamp;
+    const unsigned m = __ballot_sync(0xffffffffu, got);
+    if (got) cand[n + __popc(m & ((1u << lane) - 1u))] = c[i].q;
+    n += __popc(m);
+  }
+  __syncwarp();
+  for (int b = 0; b < n; b += kVolBatch) {
+    const int nb = min(kVolBatch, n - b);
+    int pts[kVolBatch];
+#pragma unroll
+    for (int q = 0; q < kVolBatch; ++q) pts[q] = cand[b + min(q, nb - 1)];
+    EvalT T[kVolBatch];
+    vol_pass<PREC>(P, S, X, pts, nb, T);
+    const unsigned liq = vol_commit<PREC>(P, S, X, pts, nb, T, pairs);
+    int slot = 0;
+    if (lane == 0 && liq) slot = atomicAdd(X.lo_n, __popc(liq));
+    // lane q < nb carries point q; the liquid ones join the list and the queue
+    int mine = pts[0];
+#pragma unroll
+    for (int q = 1; q < kVolBatch; ++q) if (lane == q) mine = pts[q];
+    const bool is_liq = lane < nb && ((liq >> lane) & 1u);
+    slot = __shfl_sync(0xffffffffu, slot, 0) + __popc(liq & ((1u << lane) - 1u));
+    if (is_liq) push_liquid(S, X, slot, mine, 0);
+    emit(S, X, is_liq, IT_EXPAND, mine, 0, nchild, &kept);
+    __syncwarp();
+  }
+}
+
+// One Volume item (see kVolChunk): a chunk of `units` re-tests starting at list entry p
+// (IT_RETEST), a beam-trace candidate (IT_VISIT), or a liquid point to expand (IT_EXPAND).
+template <int PREC>
+__device__ int run_item_vol(const DevProblem& P, const TrackState& S, const StepCtx& X, int type, int p, int units,
+                            bool seed, bool got, int* cand, unsigned long long& pairs, Kept& kept) {
+  const int lane = threadIdx.x & 31;
+  int nchild = 0;
+  int E[kVolChunk];
+  int nE = 0;
+  if (type == IT_RETEST) {
+    int pts[kVolBatch];
+    double Told[kVolBatch];
+#pragma unroll
+    for (int q = 0; q < kVolBatch; ++q) {
+      pts[q] = __ldcg(X.L + p + min(q, units - 1)).x;
+      Told[q] = ldcg_d(S.T + pts[q]);
+    }
+    EvalT T[kVolBatch];
+    vol_pass<PREC>(P, S, X, pts, units, T);
+    const unsigned liq = vol_commit<PREC>(P, S, X, pts, units, T, pairs);
+    int slot = 0;
+    if (lane == 0 && liq) slot = atomicAdd(X.lo_n, __popc(liq));
+#pragma unroll
+    for (int q = 0; q < kVolBatch; ++q) {
+      if (q >= units) break;
+      if ((liq >> q) & 1u) {
+        if (lane == 0) push_liquid(S, X, slot + __popc(liq & ((1u << q) - 1u)), pts[q], 0);
+        E[nE++] = pts[q];
+      } else if (lane == 0) {
+        push_rec<false>(S, X, pts[q], T[q].T, Told[q]);    // cooled below T_L since the last step
+      }
+    }
+  } else if (type == IT_VISIT) {
+    int pts[kVolBatch];
+#pragma unroll
+    for (int q = 0; q < kVolBatch; ++q) pts[q] = p;
+    EvalT T[kVolBatch];
+    vol_pass<PREC>(P, S, X, pts, 1, T);              // the claim's result arrives meanwhile
+    if (seed && !__shfl_sync(0xffffffffu, got, 0)) return 0;   // another item took the point
+    const unsigned liq = vol_commit<PREC>(P, S, X, pts, 1, T, pairs);
+    if (liq) {
+      int slot = 0;
+      if (lane == 0) slot = atomicAdd(X.lo_n, 1);
+      if (lane == 0) push_liquid(S, X, slot, p, 0);
+      E[nE++] = p;
+    }
+  } else {
+    E[nE++] = p;
+  }
+  if (nE) vol_expand<PREC>(P, S, X, E, nE, cand, nchild, pairs, kept);
+  return nchild;
+}
+
 // ------------------------------------------------------------------ the tracking loop
 // Warps per block, one block per SM: Surface steps are short chains of ~500 items (latency-
 // bound; more waiting warps only add polls), Volume steps have ~1e5 items (throughput-
 // bound: eight warps share one staged copy of the lists).
 template <bool SURF>
-constexpr int track_threads() { return SURF ? 128 : 256; }
+__host__ __device__ constexpr int track_threads() { return SURF ? 128 : 256; }
 // The thread bound the kernel is compiled for: the Volume kernel is held to the registers of
 // 328 threads (no spills) so that a 128-thread bulk-solidification block of the other
 // stream still fits beside its 256-thread block; at its unconstrained 230 registers the
@@ -1114,6 +1377,10 @@ __global__ void __launch_bounds__(track_bound<TM != TM_VOLUME>(), 1) k_track(Dev
                                                                         int k_begin, int k_end, int high_water,
                                                                         int stage_cap, long long spin_limit, int hold) {
   constexpr bool SURF = TM != TM_VOLUME;
+  constexpr bool VOL = TM == TM_VOLUME;
+  // Volume: each warp's neighbours claimed by one item, before they are evaluated
+  __shared__ int s_cand[VOL ? track_threads<false>() / 32 : 1][VOL ? kVolCand : 1];
+  const int tid_w = VOL ? (int)(threadIdx.x >> 5) : 0;
   extern __shared__ __align__(16) unsigned char stage_mem[];
   __shared__ BlockBuf bbuf;
   const int lane = threadIdx.x & 31;
@@ -1227,25 +1494,34 @@ __global__ void __launch_bounds__(track_bound<TM != TM_VOLUME>(), 1) k_track(Dev
     // it and every item has completed; whoever's update of the step word makes that true
     // resets the counters the next steps use and publishes the step-end word, which the
     // waiting warps see.  No grid barrier separates steps.
+    // Volume deals the re-tests kVolChunk to an item; an item completes as many initial
+    // entries as it took (one, or its chunk's re-tests)
+    const int n_rt = VOL ? (X.nL + kVolChunk - 1) / kVolChunk : X.nL;
+    const int n_units = n_rt + n_seed;
     int next_init = tid >> 5;
     long long idle = 0;
     unsigned long long fin_seen = 0xffffffffull;   // the step-end word this warp saw
     while (true) {
       const long long c0 = clock64();
-      int type, p = 0, aux = 0, Dk = 0;
+      int type, p = 0, aux = 0, Dk = 0, units = 1;
       bool is_seed = false, got = false;
-      if (next_init < X.n_init) {
+      if (next_init < n_units) {
         const int t = next_init;
         next_init += n_warps;
         X.depth = 0;
-        if (t < X.nL) {
+        if (t < n_rt) {
           type = IT_RETEST;
-          const int2 e = (t == (tid >> 5)) ? first_entry : __ldcg(X.L + t);
-          p = e.x;
-          Dk = e.y;
+          if (VOL) {                        // entries [p, p + units) of the list
+            p = t * kVolChunk;
+            units = min(kVolChunk, X.nL - p);
+          } else {
+            const int2 e = (t == (tid >> 5)) ? first_entry : __ldcg(X.L + t);
+            p = e.x;
+            Dk = e.y;
+          }
         } else {                            // a trace candidate: visited if this claim takes it
           type = IT_VISIT;
-          p = __ldg(seed + (t - X.nL));
+          p = __ldg(seed + (t - n_rt));
           is_seed = true;
           if (lane == 0) got = claim(S, p, X.stamp);
         }
@@ -1319,7 +1595,8 @@ __global__ void __launch_bounds__(track_bound<TM != TM_VOLUME>(), 1) k_track(Dev
       unsigned long long g_item = globaltimer();
       Kept kept{0, 0, false};
       while (true) {
-        run_item<PREC, TM>(P, S, X, type, p, aux, Dk, is_seed, got, pairs, kept);
+        if constexpr (VOL) run_item_vol<PREC>(P, S, X, type, p, units, is_seed, got, s_cand[tid_w], pairs, kept);
+        else run_item<PREC, TM>(P, S, X, type, p, aux, Dk, is_seed, got, pairs, kept);
         if (lane == 0) {
           const int l = min(X.depth, 3);
           atomicMax(&X.qc->lvl_start[l], (unsigned)(g_item - g0));
@@ -1327,7 +1604,7 @@ __global__ void __launch_bounds__(track_bound<TM != TM_VOLUME>(), 1) k_track(Dev
         }
         if (!kept.valid) break;
         // the kept child runs next; the item completes once its chain of kept children ends
-        type = IT_VISIT; p = kept.p; aux = kept.aux; Dk = 0; is_seed = false; got = false;
+        type = VOL ? IT_EXPAND : IT_VISIT; p = kept.p; aux = kept.aux; Dk = 0; is_seed = false; got = false;
         kept.valid = false;
         ++X.depth;
         if (X.depth > max_depth) {
@@ -1338,8 +1615,8 @@ __global__ void __launch_bounds__(track_bound<TM != TM_VOLUME>(), 1) k_track(Dev
         g_item = globaltimer();
       }
       if (lane == 0) {                                           // completed, after the item's writes
-        const unsigned long long st = atom_add_release(&X.qc->state, 1ull);
-        if (step_over(st + 1ull, X.n_init + hold, gridDim.x)) finish_step<TM>(P, S, X, k, st + 1ull, high_water);
+        const unsigned long long st = atom_add_release(&X.qc->state, (unsigned long long)units);
+        if (step_over(st + units, X.n_init + hold, gridDim.x)) finish_step<TM>(P, S, X, k, st + units, high_water);
       }
       ++n_items;
       c_items += clock64() - c1;
@@ -1356,7 +1633,7 @@ __global__ void __launch_bounds__(track_bound<TM != TM_VOLUME>(), 1) k_track(Dev
     const unsigned verdict = (unsigned)(fin_seen >> 32) & 3u;
     nL_next = (int)(fin_seen >> 34);
     log_pos += nL_next;
-    if (!aborted && (tid >> 5) < S.list_cap) first_next = __ldcg(X.Lo + (tid >> 5));
+    if (!VOL && !aborted && (tid >> 5) < S.list_cap) first_next = __ldcg(X.Lo + (tid >> 5));
     cp_async_wait_all();
     if (threadIdx.x == 0) s_flush[k & 1] = bbuf.nrec >= kBlkRec / 2;
     if (__syncthreads_or(aborted)) break;
@@ -1802,10 +2079,15 @@ constexpr double kSensMax = 4e-9;
 
 // Solidification time by the reference's secant step, then gradient, Laplacian and source
 // sums at that time with the refined schedule, and the derived fields (src/Grid.cpp:316-548).
-template <int PREC>
+// FIX: the second FP32 pass, over the records queued for FP64 temperatures only (k_fix_T has
+// summed T and T_last in FP64): the secant then starts exactly as the FP64 form's does, and
+// the record goes on to the full FP64 redo only if its sums cancel or the stop test needs the
+// secant's FP32 iterations.
+template <int PREC, bool FIX>
 __global__ void __launch_bounds__(128, 4) k_solidify(DevProblem P, TrackState S, const SolRec* rec, int nrec) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nrec) return;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (FIX ? min(__ldcg(S.fix_n), S.rec_cap) : nrec)) return;
+  const int i = FIX ? S.fix[e].i : e;
   const SolRec r = rec[i];
   // a later record of this point sets its fields; RDF keeps every record's time and rate
   const bool latest = S.sol_step[r.p] == r.step;
@@ -1814,12 +2096,13 @@ __global__ void __launch_bounds__(128, 4) k_solidify(DevProblem P, TrackState S,
   point_xyz(P, r.p, x, y, z);
   unsigned long long pairs = 0;
   int err = 0;
-  const double T2 = t_decode(S, P, r.T), T1 = t_decode(S, P, r.Tl);
+  const double T2 = FIX ? S.fix_T[e].x : t_decode(S, P, r.T), T1 = FIX ? S.fix_T[e].y : t_decode(S, P, r.Tl);
   double tsol = secant_first(P, T2, T1, r.t);
   PointSums ps;
   if (PREC == 0) point_sums<true>(P, x, y, z, tsol, true, ps, pairs, err);
   else point_sums_f32<true>(P, x, y, z, tsol, true, ps, pairs, err);
-  if (!stop_test_decided(P, P.T0 + ps.T)) {          // the secant as the reference runs it
+  const bool decided = stop_test_decided(P, P.T0 + ps.T);
+  if (!decided) {                                    // the secant as the reference runs it
     const double ts = secant_tsol<PREC>(P, x, y, z, T2, T1, r.t, pairs, err);
     if (ts != tsol) {
       tsol = ts;
@@ -1833,8 +2116,15 @@ __global__ void __launch_bounds__(128, 4) k_solidify(DevProblem P, TrackState S,
     const double mag = P.a * ps.lap_mag + ps.dtt, dT = fabs(T2 - T1);
     int why = 0;
     if (!(ps.g_mag <= kCondMax * G) || !(mag <= kCondMax * rate)) why |= 1;
-    if (!(dT >= kSecantMinK) || !(mag * P.dt * kTempErr * (P.TL - P.T0) <= kSensMax * rate * dT)) why |= 2;
-    if (why) {                                      // at most one entry per record: no overflow
+    if (FIX) {
+      if (!decided) why |= 2;                        // iterated on FP32 temperatures
+    } else if (!(dT >= kSecantMinK) || !(mag * P.dt * kTempErr * (P.TL - P.T0) <= kSensMax * rate * dT)) {
+      why |= 2;
+    }
+    if (!FIX && why == 2) {                          // FP64 temperatures are enough: k_fix_T, then FIX
+      const int j = atomicAdd(S.fix_n, 1);
+      if (j < S.rec_cap) S.fix[j] = RedoRec{i, why};
+    } else if (why) {                                // at most one entry per record: no overflow
       const int j = atomicAdd(S.redo_n, 1);
       if (j < S.rec_cap) S.redo[j] = RedoRec{i, why};
     }
@@ -1945,6 +2235,44 @@ __device__ void block_sums_at(const DevProblem& P, const TrackState& S, double t
   __syncthreads();
   o = bc;
   __syncthreads();
+}
+
+// FP64 temperatures of the records the FP32 pass queued for them (S.fix), one thread block
+// per record: T and T_last summed in FP64 over the node window's lists of the record's step
+// and the step before it - the sums the FP64 redo starts from - for k_solidify's FIX pass.
+// A queue that one round of redo blocks takes whole goes to the FP64 redo instead (its
+// latency is one record's; the second FP32 pass would add its own on the same stream).
+__global__ void __launch_bounds__(kGenThreads, 2) k_fix_T(DevProblem P, TrackState S, NodeWindow W, const SolRec* rec) {
+  __shared__ double red[kGenThreads / 32][6];
+  __shared__ int s_base;
+  const int n = min(__ldcg(S.fix_n), S.rec_cap);
+  if (n <= (int)gridDim.x) {
+    if (blockIdx.x == 0 && n > 0) {
+      if (threadIdx.x == 0) s_base = atomicAdd(S.redo_n, n);
+      __syncthreads();
+      for (int i = threadIdx.x; i < n; i += blockDim.x)
+        if (s_base + i < S.rec_cap) S.redo[s_base + i] = S.fix[i];
+      __syncthreads();
+      if (threadIdx.x == 0) *S.fix_n = 0;
+    }
+    return;
+  }
+  unsigned long long pairs = 0;
+  for (int e = blockIdx.x; e < n; e += gridDim.x) {
+    const SolRec r = rec[S.fix[e].i];
+    double x, y, z;
+    point_xyz(P, r.p, x, y, z);
+    const int slot = r.step - W.base + 1;
+    PointSums ps;
+    block_sums<false>(slot_view(W, slot), min(W.count[slot], W.slot_cap), x, y, z, ps, red, pairs);
+    const double T2 = P.T0 + ps.T;
+    block_sums<false>(slot_view(W, slot - 1), min(W.count[slot - 1], W.slot_cap), x, y, z, ps, red, pairs);
+    if (threadIdx.x == 0) {
+      S.fix_T[e] = make_double2(T2, P.T0 + ps.T);
+      atomicAdd(&S.C->fix_total, 1ull);
+    }
+  }
+  if (threadIdx.x == 0 && pairs) { atomicAdd(S.pairs, pairs); atomicAdd(S.pairs + 1, pairs); }
 }
 
 // The FP64 redo of the records an FP32 pass queued, one thread block per record: T and
@@ -2141,14 +2469,18 @@ void th_launch_solidify(const DevProblem& P, const TrackState& S, const NodeWind
     return;
   }
   if (precision == 0) {
-    k_solidify<0><<<(nrec + 127) / 128, 128, 0, s>>>(P, S, rec, nrec);
+    k_solidify<0, false><<<(nrec + 127) / 128, 128, 0, s>>>(P, S, rec, nrec);
     return;
   }
-  k_solidify<1><<<(nrec + 127) / 128, 128, 0, s>>>(P, S, rec, nrec);
-  // one to five percent of the records are redone, a block each: a persistent pass over the
-  // queue, then the queue is emptied
+  k_solidify<1, false><<<(nrec + 127) / 128, 128, 0, s>>>(P, S, rec, nrec);
+  // records whose secant is too sensitive to FP32 temperatures get FP64 ones (a block each)
+  // and a second FP32 pass; those whose sums cancel get the full FP64 redo (a block each): a
+  // persistent pass over each queue, then the queues are emptied
+  k_fix_T<<<S.redo_blocks, kGenThreads, 0, s>>>(P, S, w, rec);
+  k_solidify<1, true><<<(nrec + 127) / 128, 128, 0, s>>>(P, S, rec, nrec);
   k_solidify_redo<<<S.redo_blocks, kGenThreads, 0, s>>>(P, S, w, rec, 0);
   cudaMemsetAsync(S.redo_n, 0, sizeof(int), s);
+  cudaMemsetAsync(S.fix_n, 0, sizeof(int), s);
 }
 
 void th_launch_final_field(const DevProblem& P, const TrackState& S, int field, double* out, cudaStream_t s) {

@@ -67,7 +67,8 @@ struct alignas(128) TrackCounters {
   unsigned long long prof[18];
   unsigned long long redo_total;   // FP32 runs: records whose solidification was redone in FP64
   unsigned long long guard_total;  // FP32 runs: liquid decisions taken on an FP64 sum
-                                   // (both read with prof as its 19th and 20th words)
+  unsigned long long fix_total;    // FP32 runs: records re-solidified from FP64 temperatures
+                                   // (the three read with prof as its 19th to 21st words)
   alignas(128) int liq_n[3];     // liquid list lengths
   alignas(128) int rec_n[2];     // solidification records queued in each of the two record buffers
   alignas(128) int tm_n[2];      // RDF melt events logged in each of the two event buffers
@@ -99,6 +100,9 @@ struct TrackState {
   int rec_cap;
   RedoRec* redo;           // FP32 runs: records queued for the FP64 redo of their solidification
   int* redo_n;             // (capacity rec_cap; emptied after each redo pass)
+  RedoRec* fix;            // FP32 runs: records whose secant only needs FP64 temperatures, their
+  int* fix_n;              // count, and those temperatures (T, T_last) (capacity rec_cap)
+  double2* fix_T;
   NodeBufView redo_nb;     // FP32 runs: a scratch node list of redo_cap nodes per redo block
   int redo_cap;            // (block b's at b * redo_cap), and per block its list's count and
   int redo_blocks;         // error bits (redo_aux[2 b], redo_aux[2 b + 1])

@@ -275,7 +275,8 @@ def run_solidification(args, th, torch, dev, path, deck, world):
                 "note": "the same deck and run in the plain FP64 form (TH_FP64), one run after a 300-step warm-up"}
     detail = {"steps": int(st["steps"]), "pairs_per_step": pairs, "ms_node_windows": st["ms_nodes"],
               "ms_tracking": st["ms_track"], "ms_solidify": st["ms_solidify"], "records": int(st["records"]),
-              "records_redone_fp64": int(st["records_redone_fp64"]), "guarded_decisions": int(st["guarded_decisions"]),
+              "records_redone_fp64": int(st["records_redone_fp64"]),
+              "records_fixed_fp64": int(st["records_fixed_fp64"]), "guarded_decisions": int(st["guarded_decisions"]),
               "fp64_form": fp64,
               "max_items_per_step": int(st["max_items"]), "wall_s_per_step": statistics.median(wall),
               "device_s_per_step": statistics.median(dev_s)}

@@ -158,8 +158,8 @@ th_status th_run_reset(th_ctx* ctx);
  * item start and the latest item end after the step began, in ms summed over steps, the
  * nodes of the evaluation passes summed over passes, the records of an FP32 run whose
  * solidification was redone in FP64, the liquid decisions of an FP32 run taken on an
- * FP64 sum, and for Stork tracking the ms building the doubly reduced data and its rows
- * (33 values). */
+ * FP64 sum, for Stork tracking the ms building the doubly reduced data and its rows, and
+ * the records of an FP32 run re-solidified from FP64 temperatures (34 values). */
 th_status th_run_stats(th_ctx* ctx, double* out, int32_t n);
 
 /* After th_solidify / th_simulate of a deck with Output RDF 1: the reduced data of the run
