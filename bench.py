@@ -250,9 +250,10 @@ def run_solidification(args, th, torch, dev, path, deck, world):
     roof = {"bound": "latency", "kernel": f"k_track (persistent {loop} loop)",
             "achieved": achieved / 1e9, "peak": peak_pairs / 1e9, "unit": "Gpairs/s", "frac": achieved / peak_pairs,
             "peak_basis": basis, "device_rates": device_rates(th),
-            "note": (("each timestep runs ~96,000 work items (one evaluation pass of ~1,465 nodes each) over "
-                      "eight warps per SM; bound by the items' L2 round trips (claims, queue slots) and passes, "
-                      "not by FP32/MUFU issue or HBM") if loop == "Volume" else
+            "note": (("each timestep runs ~20,000 work items (re-tests four to an item, claimed neighbours "
+                      "evaluated by their claimer up to four to a pass: ~26,000 passes of ~1,465 nodes) over "
+                      "eight warps per SM; bound by the passes' latency at two warps per scheduler and the items' "
+                      "L2 round trips, not by FP32/MUFU issue or HBM") if loop == "Volume" else
                      ("each timestep runs ~580 work items (~690 evaluation passes of ~400 nodes) as a chain of "
                       "dependent L2 round trips (claims, queue slots, step word); the loop is bound by per-step "
                       "latency, not by FP32/MUFU issue or HBM")),
