@@ -176,7 +176,7 @@ RUNS = {"small_surface": ("small_surface", "Surface"), "small_volume": ("small_s
 CSV_DECKS = ("csv_snapshot", "small_multibeam")
 # Stork runs (Tracking Stork, src/Run.cpp:711-1079): the doubly reduced data; the first deck's
 # fixture also holds the reference's RRDF file
-RRDF_DECKS = ("small_stork", "surface_stork")
+RRDF_DECKS = ("small_stork", "surface_stork", "stork_bigpool")
 
 
 def rrdf_deck(name):
@@ -184,6 +184,14 @@ def rrdf_deck(name):
     if name == "surface_stork":
         d = decks.small_surface("Stork")
         d.name = "surface_stork"
+        return d
+    if name == "stork_bigpool":                # a 150 um beam on a 5 um grid: ~2,400 cell columns a step
+        d = decks.small_surface("Stork")
+        d.name = "stork_bigpool"
+        d.beams = [decks.BeamSpec(width_x=150e-6, width_y=150e-6, power=400.0)]
+        d.paths = [decks.serpentine_path(1, 0.2, 0.08, 0.8)]
+        d.axes = (decks.AxisSpec(-0.1e-3, -0.1e-3 + 89 * 5e-6, num=90),
+                  decks.AxisSpec(-34.5 * 5e-6, 34.5 * 5e-6, num=70), decks.AxisSpec(-11 * 5e-6, 0.0, num=12))
         return d
     return decks.small_stork()
 
