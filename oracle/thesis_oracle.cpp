@@ -1174,16 +1174,46 @@ int64_t run_stork(Problem& P, int threads, int64_t max_steps, double budget_s) {
       depths[dn] = depth;
       for (int d = 0; d <= depth; ++d) is_liq[pid(P, i, j, nz - 1 - d)] = 1;
     }
+    // the cells in index order, split over threads in contiguous chunks whose relevant
+    // cells are joined in chunk order (the single-thread order)
     std::vector<long> relevant;
     if (!last_liq.empty() || !liq.empty()) {
-      for (long c = 0; c < cpnum; ++c) {
-        const int ci = (int)((c / cy) / cz), cj = (int)((c / cz) % cy), ck = (int)(c % cz);
-        int n = 0;
-        for (int di = 0; di < 2; ++di) for (int dj = 0; dj < 2; ++dj) for (int dk = 0; dk < 2; ++dk)
-          n += is_liq[pid(P, ci + di, cj + dj, ck + dk)];
-        c_cur[c] = (uint8_t)n;
-        if (c_cur[c] != c_prev[c] || c_prev[c] % 8 || c_cur[c] % 8) relevant.push_back(c);
+      const int nt = std::max(1, threads);
+      std::vector<std::vector<long>> part(nt);
+      #pragma omp parallel num_threads(nt)
+      {
+        const int th = omp_get_thread_num(), nth = omp_get_num_threads();
+        const long c0 = cpnum * th / nth, c1 = cpnum * (th + 1) / nth;
+        for (long c = c0; c < c1; ++c) {
+          const int ci = (int)((c / cy) / cz), cj = (int)((c / cz) % cy), ck = (int)(c % cz);
+          int n = 0;
+          for (int di = 0; di < 2; ++di) for (int dj = 0; dj < 2; ++dj) for (int dk = 0; dk < 2; ++dk)
+            n += is_liq[pid(P, ci + di, cj + dj, ck + dk)];
+          c_cur[c] = (uint8_t)n;
+          if (c_cur[c] != c_prev[c] || c_prev[c] % 8 || c_cur[c] % 8) part[th].push_back(c);
+        }
       }
+      for (const auto& v : part) relevant.insert(relevant.end(), v.begin(), v.end());
+    }
+    // vertex temperatures: each point's at both times once (the values do not depend on who
+    // computes them), then the rows
+    {
+      std::vector<long> need;
+      for (long c : relevant) {
+        const int ci = (int)((c / cy) / cz), cj = (int)((c / cz) % cy), ck = (int)(c % cz);
+        for (int di = 0; di < 2; ++di) for (int dj = 0; dj < 2; ++dj) for (int dk = 0; dk < 2; ++dk) {
+          const long p = pid(P, ci + di, cj + dj, ck + dk);
+          if (calc_prev[p] == 0 || calc_cur[p] == 0) need.push_back(p);
+        }
+      }
+      std::sort(need.begin(), need.end());
+      need.erase(std::unique(need.begin(), need.end()), need.end());
+      par_for((long)need.size(), threads, [&](long i) {
+        const long p = need[i];
+        if (calc_prev[p] == 0) T_prev[p] = sum_T(P, Nlast, p);
+        if (calc_cur[p] == 0) T_cur[p] = sum_T(P, N, p);
+      });
+      for (long p : need) { calc_prev[p] = 1; calc_cur[p] = 1; }
     }
     for (long c : relevant) {
       const int ci = (int)((c / cy) / cz), cj = (int)((c / cz) % cy), ck = (int)(c % cz);
@@ -1193,8 +1223,6 @@ int64_t run_stork(Problem& P, int threads, int64_t max_steps, double budget_s) {
       int n = 0;
       for (int di = 0; di < 2; ++di) for (int dj = 0; dj < 2; ++dj) for (int dk = 0; dk < 2; ++dk) {
         const long p = pid(P, ci + di, cj + dj, ck + dk);
-        if (calc_prev[p] == 0) { calc_prev[p] = 1; T_prev[p] = sum_T(P, Nlast, p); }
-        if (calc_cur[p] == 0) { calc_cur[p] = 1; T_cur[p] = sum_T(P, N, p); }
         Ts[n] = T_prev[p];
         Ts[n + 8] = T_cur[p];
         ++n;
@@ -1207,7 +1235,6 @@ int64_t run_stork(Problem& P, int threads, int64_t max_steps, double budget_s) {
     if (max_steps > 0 && itert >= max_steps) return itert;
     if (budget_s > 0 && omp_get_wtime() - t_start > budget_s) return itert;
   }
-  (void)threads;
   return itert + 1;
 }
 

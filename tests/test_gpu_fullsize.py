@@ -4,6 +4,8 @@ cores in the same process.
 * the headline Surface deck (500 x 500 x 100, 25 M points, 31,769 timesteps) in FP64 and
   FP32: every point compared as in test_gpu_solidify (tests/parity.py);
 * the four-beam Volume deck (400 x 400 x 80): its first 2,000 timesteps;
+* the headline deck with Stork tracking: the doubly reduced data of its first 300
+  timesteps (about 230,000 rows);
 * eight decks of the 256-deck snapshot sweep, evaluated as part of the whole batch;
 * the calibration deck (300 x 300 x 60, 4,096 probes x 3 times): the adjoint gradient
   against central differences of the oracle for P, efficiency, the widths, alpha and the ten
@@ -46,6 +48,31 @@ def volume(built_library, decks, oracle, tmp_path_factory):
     ref = {f: o.field(f) for f in FIELDS}
     ref["steps"] = steps
     return deck, path, o, ref
+
+
+@pytest.fixture(scope="module")
+def stork(built_library, decks, oracle, tmp_path_factory):
+    deck = decks.surface_serpentine()
+    deck.tracking, deck.name = "Stork", "surface_serpentine_stork"
+    path = deck.write(str(tmp_path_factory.mktemp("stork") / "stork"))
+    o = oracle(path)
+    steps = o.solidify(threads=THREADS, max_steps=300)
+    return path, steps, o.rrdf()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_stork_prefix_full_size(stork, thesis, prec):
+    """The same rows in the same order (cell indices and step times exactly), the 16 vertex
+    temperatures within the temperature tolerance (1e-7 K / 0.01 K)."""
+    path, steps, (ri, rt, rT) = stork
+    with thesis.Simulation(path, prec) as sim:
+        assert sim.solidify(max_steps=300) == steps
+        gi, gt, gT = sim.rrdf()
+    assert ri.shape[0] > 100000
+    assert gi.shape == ri.shape
+    assert np.array_equal(gi, ri) and np.array_equal(gt, rt)
+    err = float(np.max(np.abs(gT - rT)))
+    assert err <= TOL[prec]["T_tol"], err
 
 
 def _gpu(thesis, path, prec, max_steps=0):
