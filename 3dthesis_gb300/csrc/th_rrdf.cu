@@ -374,6 +374,8 @@ __global__ void __launch_bounds__(kRThreads) k_rrdf_fill(DevProblem P, NodeWindo
     __syncthreads();
     const int k = B.k0 + j;
     const int slot = k - W.base + 1;
+    if (threadIdx.x == 0 && B.pairs)                  // the point x node pairs of both times
+      atomicAdd(B.pairs, (unsigned long long)r.nv * (W.count[slot] + (k > 0 ? W.count[slot - 1] : 0)));
     eval_vertices<PREC>(P, W, slot, vpt, r.nv, Tc, (float4*)s_sort);
     if (k > 0) {
       eval_vertices<PREC>(P, W, slot - 1, vpt, r.nv, Tp, (float4*)s_sort);

@@ -483,6 +483,7 @@ th_status rrdf_buffer(th_ctx* ctx, RunState* r, int b, cudaStream_t s) {
   RrdfBatch B{};
   B.log = r->rlog[b]; B.off = r->rlog_off[b]; B.k0 = r->rr_k0[b]; B.nsteps = n; B.nmax = nmax;
   B.counts = r->d_counts; B.row_base = r->d_row_base; B.scratch = r->d_rscratch; B.err = r->d_rerr;
+  B.pairs = ctx->d_pairs;
   cudaEventRecord(r->ev_rr[0], s);
   th_launch_rrdf(ctx->dp, r->win[b].W, B, false, ctx->precision, blocks, s);
   if ((st = th_cuda_check(ctx, cudaGetLastError(), "rrdf count")) != TH_OK) return st;
