@@ -47,7 +47,8 @@ struct alignas(128) QueueCounters {
   unsigned depth;                // longest parent -> child chain of the step's items
   unsigned lvl_start[4];         // latest start / end (ns after the step began) of the items of
   unsigned lvl_end[4];           // chain depth 0, 1, 2, >= 3 (profile)
-  unsigned pad0[22];
+  unsigned init_head;             // Volume: initial items taken (dealt by this counter, not by warp)
+  unsigned pad0[21];
   unsigned long long state;      // (dynamic items published << 32) | items completed; the
                                  // published count also hands out the items' queue slots
   unsigned long long pad1[15];
@@ -201,6 +202,7 @@ struct RrdfBatch {
   double* ts;
   double* Ts;
   int* err;                  // bit 0: a step had more vertex values than vals_cap
+  unsigned long long* pairs; // the context's point x node pair count
 };
 size_t th_rrdf_scratch_ints(int nmax);
 void th_launch_rrdf(const DevProblem& P, const NodeWindow& w, const RrdfBatch& b, bool fill, int precision, int blocks,
