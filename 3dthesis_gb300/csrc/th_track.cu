@@ -708,7 +708,7 @@ __device__ void finish_step(const DevProblem& P, const TrackState& S, const Step
                             int high_water) {
   TrackCounters* C = S.C;
   QueueCounters& q = C->q[(k + 1) % 3];
-  q.head = 0; q.depth = 0; q.state = 0ull;
+  q.head = 0; q.depth = 0; q.state = 0ull; q.init_head = 0;
   for (int l = 0; l < 4; ++l) { q.lvl_start[l] = 0; q.lvl_end[l] = 0; }
   C->liq_n[(k + 2) % 3] = 0;
   C->step = k + 1;
@@ -1495,19 +1495,31 @@ __global__ void __launch_bounds__(track_bound<TM != TM_VOLUME>(), 1) k_track(Dev
     // resets the counters the next steps use and publishes the step-end word, which the
     // waiting warps see.  No grid barrier separates steps.
     // Volume deals the re-tests kVolChunk to an item; an item completes as many initial
-    // entries as it took (one, or its chunk's re-tests)
+    // entries as it took (one, or its chunk's re-tests).  Volume warps take the initial items
+    // from a counter (a warp runs about ten a step, of uneven cost); Surface and Stork deal
+    // them by warp, so that they all start at once without a round trip.
     const int n_rt = VOL ? (X.nL + kVolChunk - 1) / kVolChunk : X.nL;
     const int n_units = n_rt + n_seed;
-    int next_init = tid >> 5;
+    int next_init = VOL ? 0 : tid >> 5;
     long long idle = 0;
     unsigned long long fin_seen = 0xffffffffull;   // the step-end word this warp saw
     while (true) {
       const long long c0 = clock64();
       int type, p = 0, aux = 0, Dk = 0, units = 1;
       bool is_seed = false, got = false;
+      int t = -1;
       if (next_init < n_units) {
-        const int t = next_init;
-        next_init += n_warps;
+        if (VOL) {
+          unsigned u = 0;
+          if (lane == 0) u = atomicAdd(&X.qc->init_head, 1u);
+          u = __shfl_sync(0xffffffffu, u, 0);
+          if ((int)u < n_units) t = (int)u; else next_init = n_units;   // none left this step
+        } else {
+          t = next_init;
+          next_init += n_warps;
+        }
+      }
+      if (t >= 0) {
         X.depth = 0;
         if (t < n_rt) {
           type = IT_RETEST;
