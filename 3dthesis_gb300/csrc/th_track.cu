@@ -335,14 +335,18 @@ __device__ __forceinline__ void warp_T_gen(const DevProblem& P, const TrackState
     const int lane = threadIdx.x & 31;
     const int n_sm = min(st.n_sm, nn);
     unsigned long long Xh[NP], Xl[NP], Yh[NP], Yl[NP], Zh[NP], Zl[NP], s2[NP], c2[NP];
-    float x1[NP][2], y1[NP][2], z1[NP][2];
-#pragma unroll
-    for (int q = 0; q < NP; ++q) {
+    // a point's axis-table entries (coordinates as (hi, lo) floats); looked up again for the
+    // rare nodes past the staged copy rather than kept live through the pass
+    auto axes = [&](int q, float2& X, float2& Y, float2& Z) {
       const unsigned col = udiv((unsigned)pts[q], P.div_nz_m, P.div_nz_s);
       const unsigned pi = udiv(col, P.div_ny_m, P.div_ny_s), pj = col - pi * (unsigned)P.ny;
       const unsigned pk = min((unsigned)pts[q] - col * (unsigned)P.nz, (unsigned)P.nz - 1u);
-      const float2 X = ax[pi], Y = ax[P.nx + pj], Z = ax[P.nx + P.ny + pk];
-      x1[q][0] = X.x; x1[q][1] = X.y; y1[q][0] = Y.x; y1[q][1] = Y.y; z1[q][0] = Z.x; z1[q][1] = Z.y;
+      X = ax[pi]; Y = ax[P.nx + pj]; Z = ax[P.nx + P.ny + pk];
+    };
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+      float2 X, Y, Z;
+      axes(q, X, Y, Z);
       Xh[q] = pk2(X.x, X.x); Xl[q] = pk2(X.y, X.y);
       Yh[q] = pk2(Y.x, Y.x); Yl[q] = pk2(Y.y, Y.y);
       Zh[q] = pk2(Z.x, Z.x); Zl[q] = pk2(Z.y, Z.y);
@@ -388,9 +392,14 @@ __device__ __forceinline__ void warp_T_gen(const DevProblem& P, const TrackState
       df_add_lazy(hi[q], lo[q], sh, -ch);
     }
     if (n_sm < nn) {                               // nodes past the staged copy, one per lane
-      float s1[NP], c1[NP];
+      float s1[NP], c1[NP], x1[NP][2], y1[NP][2], z1[NP][2];
 #pragma unroll
-      for (int q = 0; q < NP; ++q) s1[q] = c1[q] = 0.f;
+      for (int q = 0; q < NP; ++q) {
+        s1[q] = c1[q] = 0.f;
+        float2 X, Y, Z;
+        axes(q, X, Y, Z);
+        x1[q][0] = X.x; x1[q][1] = X.y; y1[q][0] = Y.x; y1[q][1] = Y.y; z1[q][0] = Z.x; z1[q][1] = Z.y;
+      }
       for (int n = n_sm + lane; n < nn; n += 32) {
         const float xh = nb.fv(NF_XH, n), yh = nb.fv(NF_YH, n), zh = nb.fv(NF_ZH, n), xl = nb.fv(NF_XL, n),
                     yl = nb.fv(NF_YL, n), zl = nb.fv(NF_ZL, n), kx = nb.fv(NF_KX, n), ky = nb.fv(NF_KY, n),
