@@ -1195,17 +1195,17 @@ __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx&
 // neighbours are still to be claimed).  The sets of claims, evaluations and decisions are
 // the one-point-per-item loop's (src/Melt.cpp:185-269): a claim is the same atomic, and a
 // point's sum is bit for bit the same in a batch.
-constexpr int kVolChunk = 4;     // re-tests per initial item
-constexpr int kVolBatch = 4;     // points per evaluation pass
+constexpr int kVolChunk = 3;     // re-tests per initial item
+constexpr int kVolBatch = 3;     // points per evaluation pass (3 ran 2 % faster than 4)
 constexpr int kVolCand = 18 * kVolChunk;   // most neighbours one item can claim
 static_assert(kVolChunk <= kVolBatch, "a chunk of re-tests is one pass");
 
-// One pass over the first n points of a batch (a pass of 1, 2 or 4 points; pts padded by
-// repeating a point).
+// One pass over the first n points of a batch (a pass of 1, 2 or kVolBatch points; pts
+// padded by repeating a point).
 template <int PREC>
 __device__ __forceinline__ void vol_pass(const DevProblem& P, const TrackState& S, const StepCtx& X,
                                          const int (&pts)[kVolBatch], int n, EvalT (&T)[kVolBatch]) {
-  static_assert(kVolBatch == 2 || kVolBatch == 4, "passes of 1, 2 or 4 points");
+  static_assert(kVolBatch >= 2 && kVolBatch <= 4, "passes of 1, 2 or kVolBatch points");
   const long long c0 = clock64();
   if (n == 1) {
     const int p1[1] = {pts[0]};
@@ -1218,7 +1218,7 @@ __device__ __forceinline__ void vol_pass(const DevProblem& P, const TrackState& 
     warp_T_gen<PREC, 2>(P, S, X.ax, X.nb, X.nn, p2, X.st, t2);
     T[0] = t2[0]; T[1] = t2[1];
   } else {
-    if constexpr (kVolBatch == 4) warp_T_gen<PREC, 4>(P, S, X.ax, X.nb, X.nn, pts, X.st, T);
+    if constexpr (kVolBatch > 2) warp_T_gen<PREC, kVolBatch>(P, S, X.ax, X.nb, X.nn, pts, X.st, T);
   }
   X.ev_c += clock64() - c0;
   X.ev_n += 1;

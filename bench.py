@@ -250,8 +250,8 @@ def run_solidification(args, th, torch, dev, path, deck, world):
     roof = {"bound": "latency", "kernel": f"k_track (persistent {loop} loop)",
             "achieved": achieved / 1e9, "peak": peak_pairs / 1e9, "unit": "Gpairs/s", "frac": achieved / peak_pairs,
             "peak_basis": basis, "device_rates": device_rates(th),
-            "note": (("each timestep runs ~20,000 work items (re-tests four to an item, claimed neighbours "
-                      "evaluated by their claimer up to four to a pass: ~26,000 passes of ~1,465 nodes) over "
+            "note": (("each timestep runs ~26,600 work items (re-tests three to an item, claimed neighbours "
+                      "evaluated by their claimer up to three to a pass: ~34,400 passes of ~1,465 nodes) over "
                       "eight warps per SM; bound by the passes' latency at two warps per scheduler and the items' "
                       "L2 round trips, not by FP32/MUFU issue or HBM") if loop == "Volume" else
                      ("each timestep runs ~580 work items (~690 evaluation passes of ~400 nodes) as a chain of "
