@@ -205,11 +205,16 @@ th_status init_run(th_ctx* ctx) {
     ALLOC(r->d_rerr, 1, 0);
   }
   if (hp.tracking != TH_TRACK_NONE) {
-    S.list_cap = (int)n;
+    // the step word's fields bound a step's items (2^24 - 1 for Volume, 2^18 - 1 for the
+    // Surface forms) and the Surface forms' liquid points (2^18 - 1: their lists hold
+    // surface points only)
+    const bool vol = hp.tracking == TH_TRACK_VOLUME;
+    const size_t field = vol ? ((size_t)1 << 24) - 1 : ((size_t)1 << 18) - 1;
+    S.list_cap = (int)(vol ? n : std::min<size_t>(n, field));
     for (int i = 0; i < 3; ++i) ALLOC(S.liq[i], n, 0);
     // work items of one step: every claimed point and column layer at most once, which
     // in practice stays far below 2 * pnum
-    S.queue_cap = (int)std::min<size_t>(2 * n + 4096, ((size_t)1 << 24) - 1);   // fits the step word's fields
+    S.queue_cap = (int)std::min<size_t>(2 * n + 4096, field);
     // test knob of the failure path: a smaller work queue overflows (ERR_QUEUE)
     if (const char* env = std::getenv("THESIS_GB300_QUEUE_CAP")) {
       const int v = std::atoi(env);

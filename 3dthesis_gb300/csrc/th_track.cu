@@ -456,11 +456,12 @@ __device__ __forceinline__ double t_decode(const TrackState& S, const DevProblem
 __device__ __forceinline__ int ldcg_i(const int* p) { return __ldcg(p); }
 __device__ __forceinline__ double ldcg_d(const double* p) { return __ldcg(p); }
 
-__device__ __forceinline__ void push_record(const TrackState& S, int p, int step, double t, double T, double Tl) {
+__device__ __forceinline__ int push_record(const TrackState& S, int p, int step, double t, double T, double Tl) {
   const int i = atomicAdd(S.rec_n, 1);
   if (i < S.rec_cap) { SolRec r; r.p = p; r.step = step; r.t = t; r.T = T; r.Tl = Tl; S.rec[i] = r; }
   else atomicOr(S.err, ERR_RECORDS);
   atomicAdd(&S.num_melt[p], 1);
+  return i;
 }
 
 // A block's solidification records, gathered in shared memory and appended to the launch's
@@ -473,9 +474,27 @@ struct BlockBuf {
   SolRec rec[kBlkRec];
 };
 
-// The step word of QueueCounters::state: items completed (bits 0-23), items published
-// (24-47), blocks that have entered the step (48-63).
-constexpr unsigned long long kField = 0xffffffull, kArrive = 1ull << 48;
+// The step word of QueueCounters::state.  Volume: items completed (bits 0-23), items
+// published (24-47), blocks that have entered the step (48-63).  Surface forms: completed
+// (0-17), published (18-35), the step's liquid points (36-53), blocks entered (54-62) and a
+// request to end the launch after the step (63), so that a waiting warp learns from this
+// one word that the step is over, how long the next step's list is and the launch's verdict.
+constexpr int kSurfLiq = 36;
+constexpr unsigned long long kSurfStop = 1ull << 63;
+template <bool SURF>
+struct StepWord {
+  static constexpr int kPub = SURF ? 18 : 24, kArr = SURF ? 54 : 48;
+  static constexpr unsigned long long kField = SURF ? 0x3ffffull : 0xffffffull;
+  static constexpr unsigned long long kArrMask = SURF ? 0x1ffull : 0xffffull;
+  static constexpr unsigned long long kArrive = 1ull << kArr;
+  __host__ __device__ static unsigned completed(unsigned long long v) { return (unsigned)(v & kField); }
+  __host__ __device__ static unsigned published(unsigned long long v) { return (unsigned)((v >> kPub) & kField); }
+  __host__ __device__ static unsigned entered(unsigned long long v) { return (unsigned)((v >> kArr) & kArrMask); }
+  __host__ __device__ static unsigned liquid(unsigned long long v) { return (unsigned)((v >> kSurfLiq) & kField); }
+  __host__ __device__ static bool over(unsigned long long v, int n_init, unsigned blocks) {
+    return entered(v) == blocks && completed(v) == (unsigned long long)n_init + published(v);
+  }
+};
 
 // Grid::Calc_T with set = true (src/Grid.cpp:300-311): the liquid markers (G = V = DBL_MIN,
 // eqFrac = -1) are applied when fields are read, from last_liq.
@@ -533,6 +552,8 @@ struct StepCtx {
   const float2* ax;        // grid axis table (hi, lo) (shared memory when it fits)
   int log_out;             // Stork: where this step's liquid list starts in the launch's log
   int log_j;               // and which of the launch's lists it is
+  int hw;                  // the record buffer's high-water mark
+  mutable int liq;         // Surface forms: the item joined the next step's list (counted at completion)
 };
 
 __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
@@ -560,6 +581,9 @@ __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long
 }
 __device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v) {
   asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void red_or(unsigned long long* p, unsigned long long v) {
+  asm volatile("red.relaxed.gpu.global.or.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
 template <int PREC>
@@ -618,8 +642,10 @@ struct Kept { int p, aux; bool valid; };
 // can be taken, so "completed == initial + published" can only hold once the step has no
 // work left.  Both 64-bit words of a slot carry the step's stamp, so a reader that sees
 // the stamp in both has the whole item without any further ordering.
+template <bool SURF>
 __device__ __forceinline__ void emit(const TrackState& S, const StepCtx& X, bool has, int type, int p, int aux,
                                      int& nchild, Kept* keep = nullptr) {
+  using W = StepWord<SURF>;
   const int lane = threadIdx.x & 31;
   unsigned m = __ballot_sync(0xffffffffu, has);
   if (!m) return;
@@ -633,7 +659,7 @@ __device__ __forceinline__ void emit(const TrackState& S, const StepCtx& X, bool
     if (!m) return;
   }
   unsigned base = 0;
-  if (lane == 0) base = (unsigned)((atomicAdd(&X.qc->state, (unsigned long long)__popc(m) << 24) >> 24) & kField);
+  if (lane == 0) base = W::published(atomicAdd(&X.qc->state, (unsigned long long)__popc(m) << W::kPub));
   base = __shfl_sync(0xffffffffu, base, 0);
   if (has) {
     const unsigned j = base + __popc(m & ((1u << lane) - 1u));
@@ -674,15 +700,16 @@ __device__ __forceinline__ Claims claim_neighbours(const DevProblem& P, const Tr
   return c;
 }
 
+template <bool SURF>
 __device__ __forceinline__ void emit_claimed(const TrackState& S, const StepCtx& X, const Claims& c, int& nchild,
                                              Kept* keep) {
-  emit(S, X, c.old < X.stamp, IT_VISIT, c.q, c.dq, nchild, keep);
+  emit<SURF>(S, X, c.old < X.stamp, IT_VISIT, c.q, c.dq, nchild, keep);
 }
 
 template <bool SURF>
 __device__ __forceinline__ void expand(const DevProblem& P, const TrackState& S, const StepCtx& X, int p, int& nchild,
                                        Kept* keep) {
-  emit_claimed(S, X, claim_neighbours<SURF>(P, S, X, p), nchild, keep);
+  emit_claimed<SURF>(S, X, claim_neighbours<SURF>(P, S, X, p), nchild, keep);
 }
 
 // A liquid point joins the next step's list with its column's depth (the next re-test
@@ -691,6 +718,7 @@ __device__ __forceinline__ void expand(const DevProblem& P, const TrackState& S,
 __device__ __forceinline__ void push_liquid(const TrackState& S, const StepCtx& X, int i, int p, int depth) {
   atomicMax(S.stamp + p, X.stamp + 1u);   // already claimed for the next step's re-test
   if (i < S.list_cap) X.Lo[i] = make_int2(p, depth); else atomicOr(S.err, ERR_LISTS);
+  X.liq = 1;
 }
 
 // Stork: the liquid point also joins the launch's log of liquid lists (the doubly reduced
@@ -700,52 +728,77 @@ __device__ __forceinline__ void log_liquid(const TrackState& S, const StepCtx& X
   if (j < S.rlog_cap) S.rlog[j] = make_int2(p, depth); else atomicOr(S.err, ERR_LISTS);
 }
 
-__device__ __forceinline__ bool step_over(unsigned long long v, int n_init, unsigned blocks) {
-  return (v >> 48) == blocks && (v & kField) == (unsigned long long)n_init + ((v >> 24) & kField);
-}
-
-// Run by the one lane whose update ended step k: clears the counters of steps k + 1 (its
-// queue) and k + 2 (the liquid list it will fill), records the step, then publishes the
-// step's end.  Every block has entered step k and no item of it is left, so nothing reads
-// those counters any more and nothing of step k + 1 has started.
-// It also takes the step's verdict for every warp - the finish test (src/Util.cpp:239-243)
-// and the record queue's high-water mark, from the step's final counts - and publishes it
-// with the next step's liquid-list length and the step's stamp in one word, so a waiting
-// warp learns all three from the load that ends its wait.
-template <int TM>
-__device__ void finish_step(const DevProblem& P, const TrackState& S, const StepCtx& X, int k, unsigned long long v,
-                            int high_water) {
-  TrackCounters* C = S.C;
+// The counters of a step are cleared while no warp can touch them: those of step k + 1
+// (queue and step word, in the third of the rotating sets: last used by step k - 2) and the
+// slot counter of the list step k + 1 fills (last used by step k - 2).  Volume: by the lane
+// whose update ended step k (every block has entered step k, so none still reads step
+// k - 2's counters).  Surface forms: by every block as it enters step k, before its entry
+// is counted (all blocks have left step k - 2, and step k + 1 starts only once every block
+// has entered step k).
+__device__ __forceinline__ void clear_counters(TrackCounters* C, int k) {
   QueueCounters& q = C->q[(k + 1) % 3];
   q.head = 0; q.depth = 0; q.state = 0ull; q.init_head = 0;
   for (int l = 0; l < 4; ++l) { q.lvl_start[l] = 0; q.lvl_end[l] = 0; }
   C->liq_n[(k + 2) % 3] = 0;
+}
+
+// Volume: run by the one lane whose update ended step k: clears the counters, records the
+// step, then publishes the step's end.  It also takes the step's verdict for every warp -
+// the finish test (src/Util.cpp:239-243) and the record queue's high-water mark, from the
+// step's final counts - and publishes it with the next step's liquid-list length and the
+// step's stamp in one word, so a waiting warp learns all three from the load that ends its
+// wait.
+__device__ void finish_step(const DevProblem& P, const TrackState& S, const StepCtx& X, int k, unsigned long long v,
+                            int high_water) {
+  TrackCounters* C = S.C;
+  clear_counters(C, k);
   C->step = k + 1;
-  const int items = X.n_init + (int)((v >> 24) & kField);
+  const int items = X.n_init + (int)StepWord<false>::published(v);
   if (items > C->max_items) C->max_items = items;
   const int n_next = __ldcg(X.lo_n), n_rec = __ldcg(S.rec_n);
-  const bool tm_full = TM == TM_SURFACE_RDF && __ldcg(S.tm_n) > S.tm_cap / 2;   // RDF melt events
   unsigned long long flags = 0;
-  // Stork: the end of the step's list in the launch's log; a log that could not take another
-  // whole list ends the launch like a full record buffer
-  const bool log_full = TM == TM_STORK && X.log_out + n_next > S.rlog_cap - S.rlog_step_max;
-  if (TM == TM_STORK) S.rlog_off[X.log_j + 1] = X.log_out + n_next;
   if (X.t > P.end_time && n_next == 0) { flags |= 1u; C->done = 1; }
-  else if (n_rec > high_water || log_full || tm_full) { flags |= 2u; C->stop = 1; }
+  else if (n_rec > high_water) { flags |= 2u; C->stop = 1; }
   // the release store orders this lane's counter resets before the step-end word
   st_release_u64(&C->fin, ((unsigned long long)n_next << 34) | (flags << 32) | X.stamp);
 }
 
-template <bool RDF>
+// Surface forms: run by the one lane whose update ended the step, v the step word after it.
+// The word holds everything the step-end word needs - the next step's list length and a
+// stop requested during the step (record buffer or melt-event log past its high-water
+// mark) - so the lane publishes the end at once, with the verdict: the finish test
+// (src/Util.cpp:239-243), else the stop request or, for Stork, a launch log that could not
+// take another whole list.  The counters were cleared as the blocks entered the step, and
+// the host's record of the step follows the publication.
+template <int TM>
+__device__ void surface_finish(const DevProblem& P, const TrackState& S, const StepCtx& X, unsigned long long v) {
+  using W = StepWord<true>;
+  TrackCounters* C = S.C;
+  const unsigned n_next = min(W::liquid(v), (unsigned)S.list_cap);   // more latched ERR_LISTS
+  const bool log_full = TM == TM_STORK && (long long)X.log_out + n_next > (long long)S.rlog_cap - S.rlog_step_max;
+  unsigned long long flags = 0;
+  if (X.t > P.end_time && n_next == 0) flags = 1;
+  else if ((v & kSurfStop) || log_full) flags = 2;
+  st_release_u64(&C->fin, ((unsigned long long)n_next << 34) | (flags << 32) | X.stamp);
+  C->step = X.k + 1;
+  atomicMax(&C->max_items, X.n_init + (int)W::published(v));
+  if (flags == 1) C->done = 1;
+  else if (flags == 2) C->stop = 1;
+  if (TM == TM_STORK) S.rlog_off[X.log_j + 1] = X.log_out + n_next;   // the list's end in the launch's log
+}
+
+// A record past the buffer's high-water mark asks the Surface forms' step to end the launch.
+template <int TM>
 __device__ __forceinline__ void push_rec(const TrackState& S, const StepCtx& X, int p, double T, double Tl) {
-  if (RDF) S.rdf_open[p] -= 1;                       // RDF: a solidification time follows
+  if (TM == TM_SURFACE_RDF) S.rdf_open[p] -= 1;       // RDF: a solidification time follows
   const int b = atomicAdd(&X.bb->nrec, 1);
   if (b < kBlkRec) {
     SolRec& r = X.bb->rec[b];
     r.p = p; r.step = X.k; r.t = X.t; r.T = T; r.Tl = Tl;
     atomicAdd(&S.num_melt[p], 1);
   } else {
-    push_record(S, p, X.k, X.t, T, Tl);
+    const int i = push_record(S, p, X.k, X.t, T, Tl);
+    if (TM != TM_VOLUME && i >= X.hw) red_or(&X.qc->state, kSurfStop);
   }
 }
 
@@ -759,11 +812,13 @@ __device__ __forceinline__ void rdf_melt(const TrackState& S, const StepCtx& X, 
   S.rdf_open[q] = 1;
   const int j = atomicAdd(S.tm_n, 1);
   if (j < S.tm_cap) S.tm_log[j] = make_int2(q, X.k); else atomicOr(S.err, ERR_RDF);
+  if (j >= S.tm_cap / 2) red_or(&X.qc->state, kSurfStop);   // the log's high-water mark
 }
 
 // Appends the block's buffered records to the launch's record buffer (all threads of the
-// block; ends with the buffer empty).
-__device__ void flush_block(const TrackState& S, BlockBuf* bbp, int* rec_n) {
+// block; ends with the buffer empty).  Returns the launch buffer's length after the append
+// as this block's atomic saw it (0 if the block had none; the same in every thread).
+__device__ int flush_block(const TrackState& S, BlockBuf* bbp, int* rec_n) {
   BlockBuf& bb = *bbp;
   __syncthreads();
   const int nr = min(bb.nrec, kBlkRec);
@@ -774,8 +829,10 @@ __device__ void flush_block(const TrackState& S, BlockBuf* bbp, int* rec_n) {
     if (j < S.rec_cap) S.rec[j] = bb.rec[i]; else atomicOr(S.err, ERR_RECORDS);
   }
   __syncthreads();
+  const int total = nr ? bb.base_rec + nr : 0;
   if (threadIdx.x == 0) bb.nrec = 0;
   __syncthreads();
+  return total;
 }
 
 // First segment whose end time is >= t, clamped to the last (src/Melt.cpp:58-60), found by
@@ -1005,7 +1062,7 @@ __device__ int depth_walk(const DevProblem& P, const TrackState& S, const StepCt
     if (!T.liquid) {
       double Tl = Told;                                   // T of the previous step
       if (d != D) { Tl = pick4(Tl4, ub - d).T; pairs += X.nnl; }
-      if (lane == 0) push_rec<RDF>(S, X, q, T.T, Tl);
+      if (lane == 0) push_rec<RDF ? TM_SURFACE_RDF : TM_SURFACE>(S, X, q, T.T, Tl);
     } else {
       if (RDF && lane == 0) rdf_melt(S, X, q);
       break;
@@ -1124,7 +1181,7 @@ __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx&
     if (lane == 0) set_T(S, p, T, X.k);
     double Tl = Told;
     if (aux) { Tl = eval_T<PREC>(P, S, X, X.nbl, X.nnl, p, X.stl).T; pairs += X.nnl; }
-    if (lane == 0) push_rec<RDF>(S, X, p, T.T, Tl);
+    if (lane == 0) push_rec<TM>(S, X, p, T.T, Tl);
     if (RDF && lane == 0 && T.liquid) rdf_melt(S, X, p);   // solidified while still liquid
     return 0;
   }
@@ -1152,7 +1209,7 @@ __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx&
     if (SURF) D = type == IT_RETEST ? Dk : (seed ? ldcg_i(S.depths + p / P.nz) : aux);
     T3[0] = eval_T<PREC>(P, S, X, X.nb, X.nn, p, X.st);
   }
-  if (RETEST_EXPANDS && type == IT_RETEST) emit_claimed(S, X, rc, nchild, nullptr);
+  if (RETEST_EXPANDS && type == IT_RETEST) emit_claimed<SURF>(S, X, rc, nchild, nullptr);
   if (seed && !__shfl_sync(0xffffffffu, got, 0)) return 0;
   EvalT T = T3[0];
   guard_T<PREC>(P, S, X, T, p);
@@ -1176,12 +1233,12 @@ __device__ int run_item(const DevProblem& P, const TrackState& S, const StepCtx&
   } else if (STORK) {
     if (type == IT_RETEST && lane == 0) S.depths[p / P.nz] = 0;
   } else if (type == IT_RETEST) {          // cooled below T_L since the last step
-    if (lane == 0) push_rec<RDF>(S, X, p, T.T, Told);
+    if (lane == 0) push_rec<TM>(S, X, p, T.T, Told);
     if (SURF) {
       const int col = p / P.nz;
       for (int d0 = 1; d0 <= D; d0 += 32) {
         const int d = d0 + lane;
-        emit(S, X, d <= D, IT_COLUMN, col * P.nz + (P.nz - 1 - d), d != D, nchild);
+        emit<SURF>(S, X, d <= D, IT_COLUMN, col * P.nz + (P.nz - 1 - d), d != D, nchild);
       }
       if (lane == 0) S.depths[col] = 0;
     }
@@ -1282,7 +1339,7 @@ __device__ void vol_expand(const DevProblem& P, const TrackState& S, const StepC
     const bool is_liq = lane < nb && ((liq >> lane) & 1u);
     slot = __shfl_sync(0xffffffffu, slot, 0) + __popc(liq & ((1u << lane) - 1u));
     if (is_liq) push_liquid(S, X, slot, mine, 0);
-    emit(S, X, is_liq, IT_EXPAND, mine, 0, nchild, &kept);
+    emit<false>(S, X, is_liq, IT_EXPAND, mine, 0, nchild, &kept);
     __syncwarp();
   }
 }
@@ -1316,7 +1373,7 @@ __device__ int run_item_vol(const DevProblem& P, const TrackState& S, const Step
         if (lane == 0) push_liquid(S, X, slot + __popc(liq & ((1u << q) - 1u)), pts[q], 0);
         E[nE++] = pts[q];
       } else if (lane == 0) {
-        push_rec<false>(S, X, pts[q], T[q].T, Told[q]);    // cooled below T_L since the last step
+        push_rec<TM_VOLUME>(S, X, pts[q], T[q].T, Told[q]);    // cooled below T_L since the last step
       }
     }
   } else if (type == IT_VISIT) {
@@ -1447,6 +1504,9 @@ __global__ void __launch_bounds__(track_bound<TM != TM_VOLUME>(), 1) k_track(Dev
     const int slot = k_begin - W.base + 1;
     t_next = W.t[slot]; cnt_next = W.count[slot]; cntl_next = W.count[slot - 1]; nseed_next = W.nseed[slot];
   }
+  // Surface forms: this block's last flush took the record buffer past its high-water mark
+  // (the block's next step entry asks for the launch to end after that step)
+  bool stop_vote = false;
   int k = k_begin;
   for (; k < k_end; ++k) {
     StepCtx X;
@@ -1493,16 +1553,29 @@ __global__ void __launch_bounds__(track_bound<TM != TM_VOLUME>(), 1) k_track(Dev
     X.ax = ax;
     X.log_out = log_pos;
     X.log_j = k - k_begin + 1;
+    X.hw = high_water;
+    X.liq = 0;
     unsigned long long arrival = 0;         // this block enters the step (thread 0)
     bool arrival_pending = threadIdx.x == 0;
-    if (arrival_pending) arrival = atomicAdd(&X.qc->state, kArrive);
+    if (VOL && arrival_pending) arrival = atomicAdd(&X.qc->state, StepWord<false>::kArrive);
+    if (SURF && arrival_pending) {
+      clear_counters(C, k);
+      if (stop_vote) red_or(&X.qc->state, kSurfStop);
+      arrival = atom_add_release(&X.qc->state, StepWord<true>::kArrive);   // ordered after the clears and the vote
+    }
+    stop_vote = false;
     // The work loop.  The step's initial items - re-tests of the previous liquid points,
     // then the beam trace's candidates - are dealt to the warps in order (warp w takes
     // w, w + warps, ...), so they all start at once; items published during the step are
     // taken with tickets from the queue.  The step is over when every block has entered
     // it and every item has completed; whoever's update of the step word makes that true
-    // resets the counters the next steps use and publishes the step-end word, which the
-    // waiting warps see.  No grid barrier separates steps.
+    // publishes the step-end word, which the waiting warps see (Volume: after resetting
+    // the counters the next steps use and reading the next list's length and the record
+    // count; Surface forms: at once, the step word holding the list's length and any stop
+    // request, the counters cleared by the blocks as they entered the step).  No grid
+    // barrier separates steps.  (Surface forms whose waiting warps read the end from the
+    // step word itself, with no step-end word, took 6 % longer: ~600 warps polling the
+    // line that the step's atomics update.)
     // Volume deals the re-tests kVolChunk to an item; an item completes as many initial
     // entries as it took (one, or its chunk's re-tests).  Volume warps take the initial items
     // from a counter (a warp runs about ten a step, of uneven cost); Surface and Stork deal
@@ -1553,8 +1626,12 @@ __global__ void __launch_bounds__(track_bound<TM != TM_VOLUME>(), 1) k_track(Dev
         }
         if (arrival_pending) {              // this block's entry, checked once its result is back
           arrival_pending = false;
-          if (step_over(arrival + kArrive, X.n_init + hold, gridDim.x))
-            finish_step<TM>(P, S, X, k, arrival + kArrive, high_water);
+          const unsigned long long v = arrival + StepWord<SURF>::kArrive;
+          if constexpr (SURF) {
+            if (StepWord<true>::over(v, X.n_init + hold, gridDim.x)) surface_finish<TM>(P, S, X, v);
+          } else {
+            if (StepWord<false>::over(v, X.n_init + hold, gridDim.x)) finish_step(P, S, X, k, v, high_water);
+          }
         }
         unsigned ticket = 0;
         if (lane == 0) ticket = atomicAdd(&X.qc->head, 1u);
@@ -1565,26 +1642,30 @@ __global__ void __launch_bounds__(track_bound<TM != TM_VOLUME>(), 1) k_track(Dev
         unsigned backoff = 8;
         ulonglong2 it = make_ulonglong2(0ull, 0ull);
         while (true) {
+          // one round trip for both: lane 0 reads the ticket's slot, lane 1 the step-end word
+          // (read one after the other they took two: Surface 1 %, Volume 2.7 % slower)
           if (lane == 0) {
             if (j < (unsigned)S.queue_cap) it = ld_relaxed_v2(S.queue + j);
             ready = (unsigned)(it.x >> 32) == X.stamp && (unsigned)(it.y >> 32) == X.stamp;
-            if (!ready) {
-              fin = ld_acquire_u64(&C->fin);
-              finished = (unsigned)fin >= X.stamp;
-            }
+          } else if (lane == 1) {
+            fin = ld_acquire_u64(&C->fin);
+            finished = (unsigned)fin >= X.stamp;
           }
           ready = __shfl_sync(0xffffffffu, ready, 0);
-          finished = __shfl_sync(0xffffffffu, finished, 0);
+          finished = !ready && __shfl_sync(0xffffffffu, finished, 1);
+          fin = ((unsigned long long)__shfl_sync(0xffffffffu, (unsigned)(fin >> 32), 1) << 32) |
+                __shfl_sync(0xffffffffu, (unsigned)fin, 1);
           if (ready || finished) break;
           backoff = backoff < 64 ? backoff * 2 : 64;
           if (++idle > spin_limit) {
             if (lane == 0) {
               if (atomicOr(S.err, ERR_BARRIER) == 0) {        // first waiter to give up records its view
+                using SW = StepWord<SURF>;
                 const unsigned long long st = ld_relaxed_u64(&X.qc->state);
                 int* g = S.C->diag;
                 g[0] = 1; g[1] = k; g[2] = (int)j; g[3] = X.n_init;
-                g[4] = (int)*(volatile unsigned*)&X.qc->head; g[5] = (int)(st >> 48);
-                g[6] = (int)((st >> 24) & kField); g[7] = (int)(st & kField);
+                g[4] = (int)*(volatile unsigned*)&X.qc->head; g[5] = (int)SW::entered(st);
+                g[6] = (int)SW::published(st); g[7] = (int)SW::completed(st);
               }
               st_release_u64(&C->fin, 0xffffffffull);       // let every warp leave
             }
@@ -1615,6 +1696,7 @@ __global__ void __launch_bounds__(track_bound<TM != TM_VOLUME>(), 1) k_track(Dev
       }
       unsigned long long g_item = globaltimer();
       Kept kept{0, 0, false};
+      X.liq = 0;
       while (true) {
         if constexpr (VOL) run_item_vol<PREC>(P, S, X, type, p, units, is_seed, got, s_cand[tid_w], pairs, kept);
         else run_item<PREC, TM>(P, S, X, type, p, aux, Dk, is_seed, got, pairs, kept);
@@ -1636,8 +1718,15 @@ __global__ void __launch_bounds__(track_bound<TM != TM_VOLUME>(), 1) k_track(Dev
         g_item = globaltimer();
       }
       if (lane == 0) {                                           // completed, after the item's writes
-        const unsigned long long st = atom_add_release(&X.qc->state, (unsigned long long)units);
-        if (step_over(st + units, X.n_init + hold, gridDim.x)) finish_step<TM>(P, S, X, k, st + units, high_water);
+        if constexpr (SURF) {
+          const unsigned long long add = (unsigned long long)units | ((unsigned long long)X.liq << kSurfLiq);
+          const unsigned long long v = atom_add_release(&X.qc->state, add) + add;
+          if (StepWord<true>::over(v, X.n_init + hold, gridDim.x)) surface_finish<TM>(P, S, X, v);
+        } else {
+          const unsigned long long st = atom_add_release(&X.qc->state, (unsigned long long)units);
+          if (StepWord<false>::over(st + units, X.n_init + hold, gridDim.x))
+            finish_step(P, S, X, k, st + units, high_water);
+        }
       }
       ++n_items;
       c_items += clock64() - c1;
@@ -1664,7 +1753,10 @@ __global__ void __launch_bounds__(track_bound<TM != TM_VOLUME>(), 1) k_track(Dev
       prof_pend = true;
     }
     if (verdict) { ++k; break; }
-    if (s_flush[k & 1]) flush_block(S, &bbuf, S.rec_n);
+    if (s_flush[k & 1]) {
+      const int n_rec = flush_block(S, &bbuf, S.rec_n);
+      stop_vote = SURF && n_rec > high_water;
+    }
   }
   cp_async_wait_all();
   if (tid == 0 && prof_pend) add_step_prof(s_qprof[(k - 1) & 1], s_acc);
@@ -2445,7 +2537,7 @@ static cudaError_t launch_track_t(const DevProblem& P, const TrackState& S, cons
   constexpr bool SURF = TM != TM_VOLUME;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_track<PREC, TM>, track_threads<SURF>(), smem);
   const int blocks = sms * (occ < 1 ? occ : 1);
-  if (blocks <= 0) return cudaErrorInvalidConfiguration;
+  if (blocks <= 0 || (unsigned)blocks > StepWord<SURF>::kArrMask) return cudaErrorInvalidConfiguration;
   DevProblem Pc = P;
   TrackState Sc = S;
   NodeWindow Wc = w;

@@ -49,7 +49,9 @@ struct alignas(128) QueueCounters {
   unsigned lvl_end[4];           // chain depth 0, 1, 2, >= 3 (profile)
   unsigned init_head;             // Volume: initial items taken (dealt by this counter, not by warp)
   unsigned pad0[21];
-  unsigned long long state;      // (dynamic items published << 32) | items completed; the
+  unsigned long long state;      // the step word: items completed and published, blocks
+                                 // entered (Surface forms: also liquid points and a stop
+                                 // request; the layouts are StepWord's in th_track.cu); the
                                  // published count also hands out the items' queue slots
   unsigned long long pad1[15];
 };
@@ -74,7 +76,8 @@ struct alignas(128) TrackCounters {
   alignas(128) int rec_n[2];     // solidification records queued in each of the two record buffers
   alignas(128) int tm_n[2];      // RDF melt events logged in each of the two event buffers
   // once step k is over: (next step's liquid-list length << 34) | (flags << 32) | (k + 1), flags
-  // 1 finished run, 2 record high-water mark; low word 0xffffffff: aborted by a bounded wait
+  // 1 finished run, 2 launch ends (a record buffer or log at its high-water mark); low word
+  // 0xffffffff: aborted by a bounded wait
   alignas(128) unsigned long long fin;
   QueueCounters q[3];
 };
