@@ -590,6 +590,13 @@ th_status advance_tracking(th_ctx* ctx, int64_t stop_at) {
   bool pending_sol[2] = {false, false};
   int n0 = (int)std::min<int64_t>(kWindowTrack, stop_at - r->k);
   if (n0 <= 0 || r->done) return TH_OK;
+  // a launch ends after the step that takes its record buffer past half full; test knob:
+  // THESIS_GB300_REC_HIGH_WATER lowers that mark (launches then end early, full-size buffers)
+  int high_water = r->S.rec_cap / 2;
+  if (const char* env = std::getenv("THESIS_GB300_REC_HIGH_WATER")) {
+    const int v = std::atoi(env);
+    if (v > 0) high_water = std::min(high_water, v);
+  }
   th_status st = enqueue_window(ctx, r, b, r->k, n0, as);
   if (st != TH_OK) return st;
   while (true) {
@@ -605,7 +612,7 @@ th_status advance_tracking(th_ctx* ctx, int64_t stop_at) {
     S.rlog_off = r->rlog_off[b];
     if (r->tm_log[b]) { S.tm_log = r->tm_log[b]; S.tm_n = &r->S.C->tm_n[b]; }
     cudaEventRecord(r->ev_trk[b][0], ts);
-    st = th_cuda_check(ctx, th_launch_track(ctx->dp, S, w.W, w.base, w.base + w.n, ctx->precision, r->S.rec_cap / 2, ts),
+    st = th_cuda_check(ctx, th_launch_track(ctx->dp, S, w.W, w.base, w.base + w.n, ctx->precision, high_water, ts),
                        "cooperative launch");
     if (st != TH_OK) return st;
     cudaEventRecord(r->ev_trk[b][1], ts);

@@ -3,7 +3,8 @@ without faulting the GPU: a lost work item (its step can never end, so the track
 bounded waits run out), record and work-queue overflows, and a failed device allocation in
 context creation.  Each returns its status code through the C ABI, and a new context on the
 same GPU then runs normally.  The knobs are environment variables read on the host
-(THESIS_GB300_SPIN_LIMIT, _HOLD_ITEMS, _REC_CAP, _QUEUE_CAP, _FAIL_ALLOC)."""
+(THESIS_GB300_SPIN_LIMIT, _HOLD_ITEMS, _REC_CAP, _QUEUE_CAP, _FAIL_ALLOC; _REC_HIGH_WATER,
+which ends launches early without a failure, is tested in test_gpu_fullsize)."""
 import os
 import sys
 

@@ -103,6 +103,36 @@ def test_volume_multibeam_first_2000_steps(volume, thesis, prec):
     assert rep["violations"] == [], rep
 
 
+def _stats_run(thesis, path, prec, max_steps):
+    with thesis.Simulation(path, prec) as sim:
+        steps = sim.solidify(max_steps=max_steps)
+        out = {f: sim.field(f) for f in FIELDS}
+        st = sim.run_stats()
+    return steps, out, st
+
+
+@pytest.mark.parametrize("which,max_steps", [("surface", 0), ("volume", 2000)])
+def test_record_high_water_mark_ends_launches_early(surface, volume, thesis, monkeypatch, which, max_steps):
+    """A record high-water mark of 100 records (THESIS_GB300_REC_HIGH_WATER; the buffers
+    keep their size) ends tracking launches early, at the first blocks' record flushes -
+    Surface: a block whose flush passes the mark asks the next step to end the launch,
+    through the step word; Volume: the step's finisher reads the record count - and the host
+    starts the next launch from the step reached.  The run does the same work either way: in
+    FP64 (whose records are solidified alike in any buffer; FP32 runs pick a record's FP64
+    path by the size of its buffer's queues) every field is the same bits as the run's with
+    the normal mark."""
+    path = (surface if which == "surface" else volume)[1]
+    steps, ref, st0 = _stats_run(thesis, path, "fp64", max_steps)
+    monkeypatch.setenv("THESIS_GB300_REC_HIGH_WATER", "100")
+    got_steps, got, st = _stats_run(thesis, path, "fp64", max_steps)
+    monkeypatch.delenv("THESIS_GB300_REC_HIGH_WATER")
+    assert got_steps == steps
+    assert st["records"] == st0["records"] > 100_000
+    assert st["windows"] > st0["windows"] + 3, (st["windows"], st0["windows"])   # launches that ended early
+    for f in FIELDS:
+        assert np.array_equal(got[f], ref[f], equal_nan=True), f
+
+
 @pytest.fixture(scope="module")
 def sweep(built_library, decks, tmp_path_factory):
     base = tmp_path_factory.mktemp("sweep")
