@@ -1400,15 +1400,19 @@ __device__ int run_item_vol(const DevProblem& P, const TrackState& S, const Step
 // ------------------------------------------------------------------ the tracking loop
 // Warps per block, one block per SM: Surface steps are short chains of ~500 items (latency-
 // bound; more waiting warps only add polls), Volume steps have ~1e5 items (throughput-
-// bound: eight warps share one staged copy of the lists).
+// bound: twelve warps share one staged copy of the lists).
 template <bool SURF>
-__host__ __device__ constexpr int track_threads() { return SURF ? 128 : 256; }
-// The thread bound the kernel is compiled for: the Volume kernel is held to the registers of
-// 328 threads (no spills) so that a 128-thread bulk-solidification block of the other
-// stream still fits beside its 256-thread block; at its unconstrained 230 registers the
-// solidification of a window waited for the tracking launch and ran after it.
+__host__ __device__ constexpr int track_threads() { return SURF ? 128 : 384; }
+// The thread bound the kernel is compiled for.  Volume: 512 threads hold it to 128 registers
+// (a few hundred bytes of spills), so that each of the SM's four register partitions
+// (16,384 registers) takes three tracking warps and one warp of a 128-thread, 128-register
+// bulk-solidification block of the other stream.  Eight warps at 168 registers ran the run
+// 9 % slower (4.74 against 4.33 s), nine at 168 left a partition no room for the
+// solidification warp (its windows waited for the tracking launches: 5.24 s), ten at 128
+// took 4.82 s, sixteen at 96 4.57 s; at its unconstrained 230 registers the solidification
+// of a window waited for the tracking launch and ran after it.
 template <bool SURF>
-constexpr int track_bound() { return SURF ? 128 : 328; }
+constexpr int track_bound() { return SURF ? 128 : 512; }
 // The first 48 bytes of a step's QueueCounters (head, depth, lvl_start, lvl_end) into
 // shared memory, bypassing L1 (the counters are updated by atomics in L2).
 __device__ __forceinline__ void copy_step_prof(const QueueCounters* q, unsigned* dst) {

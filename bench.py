@@ -252,7 +252,7 @@ def run_solidification(args, th, torch, dev, path, deck, world):
             "peak_basis": basis, "device_rates": device_rates(th),
             "note": (("each timestep runs ~26,600 work items (re-tests three to an item, claimed neighbours "
                       "evaluated by their claimer up to three to a pass: ~34,400 passes of ~1,465 nodes) over "
-                      "eight warps per SM; bound by the passes' latency at two warps per scheduler and the items' "
+                      "twelve warps per SM; bound by the passes' latency at three warps per scheduler and the items' "
                       "L2 round trips, not by FP32/MUFU issue or HBM") if loop == "Volume" else
                      ("each timestep runs ~580 work items (~690 evaluation passes of ~400 nodes) as a chain of "
                       "dependent L2 round trips (claims, queue slots, step word); the loop is bound by per-step "
