@@ -63,7 +63,7 @@ FP32_OPS_KAHAN = 9.5
 OPS_PER_PAIR = 16           # algorithmic work of a pair: 15 floating-point operations + 1 exp
 # DRAM bytes (read + write) of one launch of the dominant kernel, from one ncu capture of
 # that kernel on that deck (dram__bytes_read.sum + dram__bytes_write.sum)
-NCU_TRAFFIC = {"snapshot_raster": 21248, "surface_serpentine": 5916819, "volume_multibeam": 22929684}
+NCU_TRAFFIC = {"snapshot_raster": 21248, "surface_serpentine": 5916819, "volume_multibeam": 38883143}
 
 DECK_TEXT = {
     "surface_serpentine": "Solidification/Surface; 50 tracks x 5 mm serpentine, hatch 80 um, 0.8 m/s, P=200 W, "
