@@ -1559,15 +1559,12 @@ __global__ void __launch_bounds__(track_bound<TM != TM_VOLUME>(), 1) k_track(Dev
     X.log_j = k - k_begin + 1;
     X.hw = high_water;
     X.liq = 0;
-    unsigned long long arrival = 0;         // this block enters the step (thread 0)
+    // this block enters the step (thread 0; Surface forms: once its warp has run out of
+    // initial items - the entry waits for the clears before it, and the step cannot end
+    // before those items anyway)
+    unsigned long long arrival = 0;
     bool arrival_pending = threadIdx.x == 0;
     if (VOL && arrival_pending) arrival = atomicAdd(&X.qc->state, StepWord<false>::kArrive);
-    if (SURF && arrival_pending) {
-      clear_counters(C, k);
-      if (stop_vote) red_or(&X.qc->state, kSurfStop);
-      arrival = atom_add_release(&X.qc->state, StepWord<true>::kArrive);   // ordered after the clears and the vote
-    }
-    stop_vote = false;
     // The work loop.  The step's initial items - re-tests of the previous liquid points,
     // then the beam trace's candidates - are dealt to the warps in order (warp w takes
     // w, w + warps, ...), so they all start at once; items published during the step are
@@ -1630,6 +1627,12 @@ __global__ void __launch_bounds__(track_bound<TM != TM_VOLUME>(), 1) k_track(Dev
         }
         if (arrival_pending) {              // this block's entry, checked once its result is back
           arrival_pending = false;
+          if constexpr (SURF) {
+            clear_counters(C, k);
+            if (stop_vote) red_or(&X.qc->state, kSurfStop);
+            stop_vote = false;
+            arrival = atom_add_release(&X.qc->state, StepWord<true>::kArrive);   // after the clears and the vote
+          }
           const unsigned long long v = arrival + StepWord<SURF>::kArrive;
           if constexpr (SURF) {
             if (StepWord<true>::over(v, X.n_init + hold, gridDim.x)) surface_finish<TM>(P, S, X, v);
