@@ -734,7 +734,8 @@ __device__ __forceinline__ void log_liquid(const TrackState& S, const StepCtx& X
 // whose update ended step k (every block has entered step k, so none still reads step
 // k - 2's counters).  Surface forms: by every block as it enters step k, before its entry
 // is counted (all blocks have left step k - 2, and step k + 1 starts only once every block
-// has entered step k).
+// has entered step k); the entry is made when the block's first warp has run out of the
+// step's initial items.
 __device__ __forceinline__ void clear_counters(TrackCounters* C, int k) {
   QueueCounters& q = C->q[(k + 1) % 3];
   q.head = 0; q.depth = 0; q.state = 0ull; q.init_head = 0;
