@@ -60,6 +60,30 @@ bool th_write_rrdf_csv(const HostProblem& hp, const std::string& tag, const uint
   return ok;
 }
 
+// Stork's doubly reduced data as a binary file (Grid::Output_RRDF_bin, src/Grid.cpp:241-273):
+// the row count (uint32), the grid's extents (3 x uint32), its origin, x resolution and the
+// liquidus (5 x double), then the rows' cell indices (3 x uint32 each), step times (2 x
+// double each) and vertex temperatures (16 x double each), in the machine's byte order.
+bool th_write_rrdf_bin(const HostProblem& hp, const std::string& tag, const uint32_t* idx, const double* ts,
+                       const double* Ts, int64_t rows, std::string& err) {
+  if (rows < 0 || rows > (int64_t)UINT32_MAX) { err = "too many rows for the binary file's uint32 count"; return false; }
+  const std::string dir = th_data_dir(hp);
+  mkdir(dir.c_str(), 0777);
+  const std::string path = dir + "/" + hp.name + "." + tag + ".bin";
+  FILE* f = std::fopen(path.c_str(), "wb");
+  if (!f) { err = "cannot write " + path; return false; }
+  const uint32_t head[4] = {(uint32_t)rows, (uint32_t)hp.nx, (uint32_t)hp.ny, (uint32_t)hp.nz};
+  const double geo[5] = {hp.xmin, hp.ymin, hp.zmin, hp.xres, hp.TL};
+  const size_t n = (size_t)rows;
+  bool ok = std::fwrite(head, sizeof(uint32_t), 4, f) == 4 && std::fwrite(geo, sizeof(double), 5, f) == 5;
+  ok = ok && (n == 0 || (std::fwrite(idx, sizeof(uint32_t), 3 * n, f) == 3 * n &&
+                         std::fwrite(ts, sizeof(double), 2 * n, f) == 2 * n &&
+                         std::fwrite(Ts, sizeof(double), 16 * n, f) == 16 * n));
+  ok = (std::fclose(f) == 0) && ok;
+  if (!ok) err = "error writing " + path;
+  return ok;
+}
+
 // The reference's reduced data (Grid::Output_RDF, src/Grid.cpp:176-201): the header, then per
 // row the point's coordinates, melting time, solidification time and cooling rate.
 bool th_write_rdf_csv(const HostProblem& hp, const std::string& tag, const int64_t* pts, const double* tm,

@@ -13,6 +13,9 @@ bool th_write_csv(const HostProblem& hp, const std::string& tag, const std::vect
 // temperatures each).
 bool th_write_rrdf_csv(const HostProblem& hp, const std::string& tag, const uint32_t* idx, const double* ts,
                        const double* Ts, int64_t rows, std::string& err);
+// Writes <deck dir>/Data/<name>.<tag>.bin: the same rows in the reference's binary layout.
+bool th_write_rrdf_bin(const HostProblem& hp, const std::string& tag, const uint32_t* idx, const double* ts,
+                       const double* Ts, int64_t rows, std::string& err);
 // Writes <deck dir>/Data/<name>.<tag>.csv with the reduced data's rows (point, melting time,
 // solidification time, cooling rate).
 bool th_write_rdf_csv(const HostProblem& hp, const std::string& tag, const int64_t* pts, const double* tm,

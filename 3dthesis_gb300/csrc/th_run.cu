@@ -959,6 +959,21 @@ th_status th_rrdf(th_ctx* ctx, uint32_t* idx, double* ts, double* Ts, int64_t ca
   return TH_OK;
 }
 
+th_status th_output_rrdf(th_ctx* ctx, const char* name, int32_t binary) {
+  if (!ctx || !name) return th_fail(ctx, TH_ERR_INVALID, "null argument");
+  int64_t n = 0;
+  th_status st = th_rrdf(ctx, nullptr, nullptr, nullptr, 0, &n);
+  if (st != TH_OK) return st;
+  std::vector<uint32_t> idx(3 * (size_t)n);
+  std::vector<double> ts(2 * (size_t)n), Ts(16 * (size_t)n);
+  int64_t got = 0;
+  if ((st = th_rrdf(ctx, idx.data(), ts.data(), Ts.data(), n, &got)) != TH_OK) return st;
+  std::string err;
+  const bool ok = binary ? th_write_rrdf_bin(ctx->hp, name, idx.data(), ts.data(), Ts.data(), n, err)
+                         : th_write_rrdf_csv(ctx->hp, name, idx.data(), ts.data(), Ts.data(), n, err);
+  return ok ? TH_OK : th_fail(ctx, TH_ERR_IO, err);
+}
+
 th_status th_rdf(th_ctx* ctx, int32_t* counts, double* vals, int64_t cap, int64_t* nvals) {
   if (!ctx) return th_fail(ctx, TH_ERR_INVALID, "null context");
   if (!ctx->hp.o_rdf) return th_fail(ctx, TH_ERR_INVALID, "the deck does not ask for RDF output");
@@ -1021,13 +1036,7 @@ th_status th_simulate(th_ctx* ctx) {
     // intermediate files (bin/Main.cpp:104-111, src/Run.cpp:711-1079)
     while (!ctx->run->done)
       if ((st = advance(ctx, (int64_t)INT_MAX - 1)) != TH_OK) return st;
-    const int64_t n = ctx->run->rows;
-    std::vector<uint32_t> idx(3 * (size_t)n);
-    std::vector<double> ts(2 * (size_t)n), Ts(16 * (size_t)n);
-    int64_t got = 0;
-    if ((st = th_rrdf(ctx, idx.data(), ts.data(), Ts.data(), n, &got)) != TH_OK) return st;
-    std::string err;
-    if (!th_write_rrdf_csv(hp, "RRDF", idx.data(), ts.data(), Ts.data(), n, err)) return th_fail(ctx, TH_ERR_IO, err);
+    if ((st = th_output_rrdf(ctx, "RRDF", 0)) != TH_OK) return st;
     return hp.o_rdf ? write_rdf_csv(ctx, "RDF.Final") : TH_OK;
   }
   // intermediate outputs every OutputFrequency steps (src/Run.cpp:446-458, 553-565, 689-701)

@@ -182,6 +182,14 @@ th_status th_rdf(th_ctx* ctx, int32_t* counts, double* vals, int64_t cap, int64_
  * (src/Grid.h:368-370), filled by Run::Stork (src/Run.cpp:711-1079). */
 th_status th_rrdf(th_ctx* ctx, uint32_t* idx, double* ts, double* Ts, int64_t cap, int64_t* rows);
 
+/* The same rows as a file: <deck dir>/Data/<deck name>.<name>.csv (binary 0, the columns of
+ * th_simulate's RRDF file) or .bin (binary 1: the row count as uint32, the grid's point
+ * counts as 3 x uint32, its x, y, z minima, x resolution and the liquidus as 5 x double,
+ * then every row's 3 indices as uint32, 2 times and 16 temperatures as double, block by
+ * block, in the machine's byte order).  Replaces Grid::Output_RRDF_csv / Output_RRDF_bin
+ * (src/Grid.cpp:203-273).  TH_ERR_IO if the file cannot be written. */
+th_status th_output_rrdf(th_ctx* ctx, const char* name, int32_t binary);
+
 /* Whole run as the reference CLI does it: the mode loop, then the CSV files under
  * <deck dir>/Data (same names, columns and number format; a Stork deck writes
  * <name>.RRDF.csv in place of <name>.Solidification.Final.csv; Output RDF 1 adds

@@ -107,6 +107,12 @@ void ref_output_rrdf(void* h, const char* name) {
   r->grid->Output_RRDF_csv(r->sim, name);
 }
 
+// The same rows as the reference's binary file (Grid::Output_RRDF_bin, src/Grid.cpp:241-273).
+void ref_output_rrdf_bin(void* h, const char* name) {
+  RefRun* r = (RefRun*)h;
+  r->grid->Output_RRDF_bin(r->sim, name);
+}
+
 // The reduced data a run with Output RDF 1 leaves in the grid (Grid::get_RDF_tm / _tl /
 // _cr, src/Grid.h:360-362): per point the three counts, then all values in point order
 // (per point its tm, then tl, then cr values).  Returns the number of values; copies at most

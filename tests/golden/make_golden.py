@@ -96,6 +96,9 @@ if "rrdf" in job:
     for i, nm in enumerate(names):
         with open(os.path.join("Data", nm), "rb") as f:
             out[f"file{i}"] = np.frombuffer(f.read(), dtype=np.uint8)
+    L.ref_output_rrdf_bin(h, b"RRDF")                # the binary form, kept apart from the CSV
+    with open(os.path.join("Data", [nm for nm in os.listdir("Data") if nm.endswith(".bin")][0]), "rb") as f:
+        out["bin_file"] = np.frombuffer(f.read(), dtype=np.uint8)
 if "fields" in job:
     L.ref_simulate(h)
     if "rdf" in job:
@@ -211,7 +214,7 @@ def rrdf_fixture(deck, scratch, with_file):
            "steps": np.int64(np.unique(r["ts"][:, 1]).size)}
     if with_file:
         out["names"] = r["names"]
-        out.update({k: v for k, v in r.items() if k.startswith("file")})
+        out.update({k: v for k, v in r.items() if k.startswith("file") or k == "bin_file"})
     np.savez_compressed(os.path.join(HERE, f"rrdf_{deck.name}.npz"), **out)
     return out
 

@@ -217,3 +217,21 @@ def compare_rdf(o, ref, gpu, *, rel: float, T_err: float, dt: float, threads: in
                 bad.append({"check": "cooling rate against the oracle's, not explained", "n": int((~moved).sum()),
                             "points": [int(i) for i in sp[k[~moved]][:max_listed]]})
     return rep
+
+
+def read_rrdf_bin(buf: bytes) -> dict:
+    """Stork's doubly reduced data in the reference's binary layout (Grid::Output_RRDF_bin,
+    src/Grid.cpp:241-273), little-endian: the row count and the grid's three point counts
+    (uint32), its x, y, z minima, x resolution and liquidus (double), then the rows' indices
+    (3 x uint32), times (2 x double) and vertex temperatures (16 x double), block by block.
+    Raises if the buffer is not exactly that long."""
+    head = np.frombuffer(buf[:16], dtype="<u4")
+    n = int(head[0])
+    sizes = (16, 40, 12 * n, 16 * n, 128 * n)
+    if len(buf) != sum(sizes):
+        raise ValueError(f"{len(buf)} bytes for {n} rows, expected {sum(sizes)}")
+    o = np.cumsum((0,) + sizes)
+    return {"rows": n, "extent": head[1:4].copy(), "geometry": np.frombuffer(buf[o[1]:o[2]], dtype="<f8").copy(),
+            "idx": np.frombuffer(buf[o[2]:o[3]], dtype="<u4").reshape(n, 3),
+            "ts": np.frombuffer(buf[o[3]:o[4]], dtype="<f8").reshape(n, 2),
+            "Ts": np.frombuffer(buf[o[4]:o[5]], dtype="<f8").reshape(n, 16)}

@@ -14,6 +14,7 @@ import pytest
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(HERE, "golden"))
 import make_golden  # noqa: E402
+import parity  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 T_TOL = {"fp64": 1e-7, "fp32": 0.01}
@@ -105,3 +106,33 @@ def test_simulate_writes_the_reference_rrdf_file(built_library, thesis, stork_ru
             unit = 10.0 ** (np.floor(np.log10(max(abs(va), abs(vb)))) - 5)
             assert abs(vb - v) <= T_TOL[prec] + 0.5 * unit, (r, c, ra[c], rb[c], v)
             assert abs(va - v) <= 0.5 * unit * (1 + 1e-9), (r, c, ra[c], rb[c], v)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_output_rrdf_binary_matches_the_reference_file(built_library, thesis, tmp_path, prec):
+    """th_output_rrdf with binary 1 writes Data/<name>.<tag>.bin in the layout of
+    Grid::Output_RRDF_bin (src/Grid.cpp:241-273): its header (row count, point counts,
+    minima, x resolution, liquidus) is the reference's byte for byte, the indices and times
+    are the reference's, the temperatures within the precision's tolerance; with binary 0 it
+    writes the CSV that th_simulate writes, under the given tag."""
+    deck = make_golden.rrdf_deck("small_stork")
+    path = deck.write(str(tmp_path / "small_stork"))
+    g = np.load(os.path.join(HERE, "golden", "rrdf_small_stork.npz"))
+    ref_buf = g["bin_file"].tobytes()
+    with thesis.Simulation(path, prec) as sim:
+        sim.solidify()
+        sim.output_rrdf("RRDF", binary=True)
+        sim.output_rrdf("Copy", binary=False)
+    data = os.path.join(os.path.dirname(path), "Data")
+    assert sorted(os.listdir(data)) == [f"{deck.name}.Copy.csv", f"{deck.name}.RRDF.bin"]
+    with open(os.path.join(data, f"{deck.name}.RRDF.bin"), "rb") as f:
+        buf = f.read()
+    assert buf[:56] == ref_buf[:56]
+    got, ref = parity.read_rrdf_bin(buf), parity.read_rrdf_bin(ref_buf)
+    assert np.array_equal(got["idx"], ref["idx"]) and np.array_equal(got["ts"], ref["ts"])
+    err = float(np.max(np.abs(got["Ts"] - ref["Ts"])))
+    assert err <= T_TOL[prec], err
+    with open(os.path.join(data, f"{deck.name}.Copy.csv")) as f:
+        lines = f.read().splitlines()
+    assert lines[0] == bytes(g["file0"]).decode().splitlines()[0]
+    assert len(lines) == 1 + ref["rows"]

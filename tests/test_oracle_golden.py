@@ -8,6 +8,7 @@ import pytest
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(HERE, "golden"))
 import make_golden  # noqa: E402
+import parity  # noqa: E402
 
 GOLDEN = os.path.join(HERE, "golden")
 
@@ -92,3 +93,18 @@ def test_oracle_stork_rows_match_reference(name, oracle, tmp_path):
     assert make_golden.rrdf_digest(idx, ts, Ts) == str(g["digest"])
     if name == "small_stork":                      # the pool reaches the bottom cell layer
         assert idx[:, 2].min() == 0
+
+
+def test_reference_rrdf_binary_layout():
+    """The reference's binary RRDF file of small_stork (Grid::Output_RRDF_bin,
+    src/Grid.cpp:241-273) read with the layout the GPU test checks the library's file
+    against: the header holds the row count, the deck's point counts, its minima, x
+    resolution and liquidus, and the rows are the reference's own."""
+    g = _load("rrdf_small_stork.npz")
+    b = parity.read_rrdf_bin(g["bin_file"].tobytes())
+    deck = make_golden.rrdf_deck("small_stork")
+    assert b["rows"] == int(g["rows"])
+    assert b["extent"].tolist() == [ax.num for ax in deck.axes]
+    assert np.array_equal(b["geometry"][:3], [ax.vmin for ax in deck.axes])
+    assert b["geometry"][4] == deck.material.TL
+    assert make_golden.rrdf_digest(b["idx"], b["ts"], b["Ts"]) == str(g["digest"])
