@@ -45,7 +45,7 @@ EXPORTED = ("th_ctx_create_from_deck", "th_ctx_destroy", "th_last_error", "th_ge
             "th_batch_snapshot_device", "th_batch_set_tile_shape", "th_batch_autotune", "th_batch_pairs",
             "th_adj_create", "th_adj_destroy", "th_adj_last_error", "th_adj_num_params", "th_adj_params",
             "th_adj_host_nodes", "th_adj_forward", "th_adj_backward", "th_calc_T_times_device",
-            "th_device_rates", "th_rrdf", "th_rdf", "th_deck_info", "th_output_rrdf")
+            "th_device_rates", "th_rrdf", "th_rdf", "th_deck_info", "th_output_rrdf", "th_T_hist")
 
 
 class ThesisError(RuntimeError):
@@ -127,6 +127,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.th_rrdf.argtypes = [vp, vp, vp, vp, c_i64, ctypes.POINTER(c_i64)]
     L.th_rdf.argtypes = [vp, vp, vp, c_i64, ctypes.POINTER(c_i64)]
     L.th_output_rrdf.argtypes = [vp, ctypes.c_char_p, c_int]
+    L.th_T_hist.argtypes = [vp, vp, vp, c_i64, ctypes.POINTER(c_i64)]
     L.th_deck_info.argtypes = [ctypes.c_char_p, ctypes.POINTER(Info)]
     _lib = L
     return L
@@ -327,6 +328,16 @@ class Simulation:
         ts, Ts = np.zeros((n.value, 2)), np.zeros((n.value, 16))
         self._check(self._lib.th_rrdf(self._ctx, _ptr(idx), _ptr(ts), _ptr(Ts), n.value, ctypes.byref(n)))
         return idx, ts, Ts
+
+    def T_hist(self):
+        """With Output T_hist 1 (Tracking None), after simulate() or solidify(): the
+        evaluation times (n,) and every point's temperature at each, (n, pnum)
+        (Grid::get_t_hist / get_T_hist, src/Grid.h:357-358)."""
+        n = ctypes.c_int64()
+        self._check(self._lib.th_T_hist(self._ctx, None, None, 0, ctypes.byref(n)))
+        t, T = np.zeros(n.value), np.zeros((n.value, self.pnum))
+        self._check(self._lib.th_T_hist(self._ctx, _ptr(t), _ptr(T), n.value, ctypes.byref(n)))
+        return t, T
 
     def output_rrdf(self, name: str = "RRDF", binary: bool = False):
         """After solidify() on a Stork deck: writes the doubly reduced data to

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/thesis_gb300.h"
 #include "th_kernels.h"
@@ -34,6 +35,11 @@ struct th_ctx {
   double* d_export = nullptr;  size_t export_bytes = 0;
 
   RunState* run = nullptr;
+
+  // the temperature history (Output T_hist 1, Tracking None): the evaluation times and, time
+  // by time, every point's temperature, collected by th_simulate (snapshots) or the
+  // solidification loop
+  std::vector<double> hist_t, hist_T;
 
   // several node lists at once (th_calc_T_times_device): slot-major buffers of nb.cap nodes
   void* multi_mem = nullptr;   int multi_slots = 0;   int multi_cap = 0;

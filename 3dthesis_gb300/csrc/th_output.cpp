@@ -60,6 +60,35 @@ bool th_write_rrdf_csv(const HostProblem& hp, const std::string& tag, const uint
   return ok;
 }
 
+// The temperature history without tracking (Grid::Output_T_hist, src/Grid.cpp:101-136): the
+// file is <name><tag>.csv (no dot between them, as the reference names it); the header is
+// x,y,z and one column per evaluation time, each row a point's coordinates (ostream's default
+// 6 significant digits) and its temperatures, times and temperatures as std::to_string prints a
+// double (6 decimals).  T holds nt rows of pnum values.
+bool th_write_T_hist_csv(const HostProblem& hp, const std::string& tag, const double* t, const double* T, int64_t nt,
+                         std::string& err) {
+  const std::string dir = th_data_dir(hp);
+  mkdir(dir.c_str(), 0777);
+  const std::string path = dir + "/" + hp.name + tag + ".csv";
+  FILE* f = std::fopen(path.c_str(), "w");
+  if (!f) { err = "cannot write " + path; return false; }
+  std::vector<char> buf(1 << 20);
+  std::setvbuf(f, buf.data(), _IOFBF, buf.size());
+  std::fputs("x,y,z", f);
+  for (int64_t i = 0; i < nt; ++i) std::fprintf(f, ",%f", t[i]);
+  std::fputc('\n', f);
+  for (int64_t p = 0; p < hp.pnum; ++p) {
+    double x, y, z;
+    th_point_coord(hp, p, x, y, z);
+    std::fprintf(f, "%g,%g,%g", x, y, z);
+    for (int64_t i = 0; i < nt; ++i) std::fprintf(f, ",%f", T[i * hp.pnum + p]);
+    std::fputc('\n', f);
+  }
+  const bool ok = std::fclose(f) == 0;
+  if (!ok) err = "error writing " + path;
+  return ok;
+}
+
 // Stork's doubly reduced data as a binary file (Grid::Output_RRDF_bin, src/Grid.cpp:241-273):
 // the row count (uint32), the grid's extents (3 x uint32), its origin, x resolution and the
 // liquidus (5 x double), then the rows' cell indices (3 x uint32 each), step times (2 x

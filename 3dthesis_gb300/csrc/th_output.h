@@ -13,6 +13,10 @@ bool th_write_csv(const HostProblem& hp, const std::string& tag, const std::vect
 // temperatures each).
 bool th_write_rrdf_csv(const HostProblem& hp, const std::string& tag, const uint32_t* idx, const double* ts,
                        const double* Ts, int64_t rows, std::string& err);
+// Writes <deck dir>/Data/<name><tag>.csv: the temperature history of a run without tracking
+// (nt times; T time by time, pnum values each).
+bool th_write_T_hist_csv(const HostProblem& hp, const std::string& tag, const double* t, const double* T, int64_t nt,
+                         std::string& err);
 // Writes <deck dir>/Data/<name>.<tag>.bin: the same rows in the reference's binary layout.
 bool th_write_rrdf_bin(const HostProblem& hp, const std::string& tag, const uint32_t* idx, const double* ts,
                        const double* Ts, int64_t rows, std::string& err);

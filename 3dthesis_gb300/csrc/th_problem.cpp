@@ -318,7 +318,11 @@ bool th_load_deck(const std::string& param_input, HostProblem& hp, std::string& 
       if (!f_out.empty()) o.read(join_dir(hp.dir, f_out), {"Grid", "Temperature", "Solidification", "Solidification+"});
       hp.o_x = o.flag("Grid", "x", true); hp.o_y = o.flag("Grid", "y", true); hp.o_z = o.flag("Grid", "z", true);
       hp.o_T = o.flag("Temperature", "T", true);
-      if (o.flag("Temperature", "T_hist", false)) { err = "T_hist output is not supported"; return false; }
+      // the temperature history (Grid::Output_T_hist, src/Grid.cpp:101-174): without tracking
+      // every point is evaluated at the same times and the history is one table; tracked runs'
+      // per-point histories are not kept
+      hp.o_T_hist = o.flag("Temperature", "T_hist", false);
+      if (hp.o_T_hist && hp.tracking != TH_TRACK_NONE) { err = "T_hist output needs Tracking None"; return false; }
       hp.o_tSol = o.flag("Solidification", "tSol", false); hp.o_G = o.flag("Solidification", "G", false);
       hp.o_Gx = o.flag("Solidification", "Gx", false); hp.o_Gy = o.flag("Solidification", "Gy", false);
       hp.o_Gz = o.flag("Solidification", "Gz", false); hp.o_V = o.flag("Solidification", "V", false);

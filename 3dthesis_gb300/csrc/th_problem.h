@@ -91,6 +91,7 @@ struct HostProblem {
   // outputs
   bool o_x, o_y, o_z, o_T, o_tSol, o_G, o_Gx, o_Gy, o_Gz, o_V, o_dTdt, o_eqFrac, o_depth, o_numMelt;
   bool o_rdf;                     // the reduced data format (per point melting / solidification events)
+  bool o_T_hist;                  // every point's temperature at every evaluation (Tracking None)
   bool do_sol;
   // settings
   double sol_tol;

@@ -676,6 +676,23 @@ th_status advance_tracking(th_ctx* ctx, int64_t stop_at) {
 }
 
 // NoTracking: one whole-grid kernel per step, windows built and drained in sequence.
+th_status fetch_field(th_ctx* ctx, int id, double* out);
+
+// After step k of a run without tracking: if the step ran, its time and every point's T join
+// the temperature history.
+th_status record_T_hist(th_ctx* ctx, RunState* r, int k) {
+  int step = 0;
+  th_status st = th_cuda_check(ctx, cudaMemcpyAsync(&step, &r->S.C->step, sizeof(int), cudaMemcpyDeviceToHost,
+                                                    ctx->stream), "cudaMemcpyAsync");
+  if (st != TH_OK || (st = th_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "T_hist")) != TH_OK) return st;
+  if (step != k + 1) return TH_OK;
+  const size_t n = (size_t)ctx->hp.pnum, at = ctx->hist_T.size();
+  ctx->hist_T.resize(at + n);
+  if ((st = fetch_field(ctx, F_T, ctx->hist_T.data() + at)) != TH_OK) return st;
+  ctx->hist_t.push_back(time_of(r, ctx->hp.dt, k));
+  return TH_OK;
+}
+
 th_status advance_notrack(th_ctx* ctx, int64_t stop_at) {
   RunState* r = ctx->run;
   while (!r->done && r->k < stop_at) {
@@ -685,7 +702,12 @@ th_status advance_notrack(th_ctx* ctx, int64_t stop_at) {
     if ((st = finish_window(ctx, r, 0)) != TH_OK) return st;
     TrackState S = r->S;
     cudaEventRecord(r->ev_trk[0][0], ctx->stream);
-    for (int k = r->k; k < r->k + n; ++k) th_launch_notrack_step(ctx->dp, S, r->win[0].W, k, ctx->precision, ctx->stream);
+    for (int k = r->k; k < r->k + n; ++k) {
+      th_launch_notrack_step(ctx->dp, S, r->win[0].W, k, ctx->precision, ctx->stream);
+      // Output T_hist 1: every point's T joins the history at each step the loop ran
+      // (src/Grid.cpp:300-304; the loop runs no step after the finish test passed)
+      if (ctx->hp.o_T_hist && (st = record_T_hist(ctx, r, k)) != TH_OK) return st;
+    }
     if ((st = th_cuda_check(ctx, cudaGetLastError(), "notrack step")) != TH_OK) return st;
     cudaEventRecord(r->ev_trk[0][1], ctx->stream);
     TrackCounters h;
@@ -880,6 +902,8 @@ th_status th_run_reset(th_ctx* ctx) {
   }
   if (ctx->hp.tracking == TH_TRACK_NONE) k_fill_d<<<1024, 256, 0, ctx->stream>>>(r->S.T, (int64_t)ctx->hp.pnum, ctx->hp.T0);
   r->k = 0; r->done = false; r->max_items = 0;
+  ctx->hist_t.clear();
+  ctx->hist_T.clear();
   r->sol_timed[0] = r->sol_timed[1] = true;
   r->ms_nodes = r->ms_track = r->ms_solid = r->ms_device = 0;
   r->rows = 0; r->rr_n[0] = r->rr_n[1] = 0; r->rr_timed = true; r->ms_rrdf = 0;
@@ -1006,6 +1030,26 @@ th_status th_rdf(th_ctx* ctx, int32_t* counts, double* vals, int64_t cap, int64_
   return TH_OK;
 }
 
+// <name>T.hist.csv of a deck with Output T_hist 1 (bin/Main.cpp:113-115).
+static th_status write_T_hist(th_ctx* ctx) {
+  if (!ctx->hp.o_T_hist) return TH_OK;
+  std::string err;
+  if (!th_write_T_hist_csv(ctx->hp, "T.hist", ctx->hist_t.data(), ctx->hist_T.data(), (int64_t)ctx->hist_t.size(), err))
+    return th_fail(ctx, TH_ERR_IO, err);
+  return TH_OK;
+}
+
+th_status th_T_hist(th_ctx* ctx, double* times, double* T, int64_t cap, int64_t* ntimes) {
+  if (!ctx) return th_fail(ctx, TH_ERR_INVALID, "null context");
+  if (!ctx->hp.o_T_hist) return th_fail(ctx, TH_ERR_INVALID, "the deck does not ask for T_hist output");
+  const int64_t n = (int64_t)ctx->hist_t.size();
+  if (ntimes) *ntimes = n;
+  const int64_t m = std::min<int64_t>(std::max<int64_t>(cap, 0), n);
+  if (times) std::copy(ctx->hist_t.begin(), ctx->hist_t.begin() + m, times);
+  if (T) std::copy(ctx->hist_T.begin(), ctx->hist_T.begin() + m * ctx->hp.pnum, T);
+  return TH_OK;
+}
+
 th_status th_simulate(th_ctx* ctx) {
   if (!ctx) return th_fail(ctx, TH_ERR_INVALID, "null context");
   const HostProblem& hp = ctx->hp;
@@ -1019,14 +1063,20 @@ th_status th_simulate(th_ctx* ctx) {
     if (hp.o_y) { names.push_back("y"); cols.push_back(y.data()); }
     if (hp.o_z) { names.push_back("z"); cols.push_back(z.data()); }
     if (hp.o_T) { names.push_back("T"); cols.push_back(T.data()); }
+    ctx->hist_t.clear();
+    ctx->hist_T.clear();
     for (int i = 0; i < (int)hp.snaps.size(); ++i) {
       th_status st = th_snapshot(ctx, i, T.data());
       if (st != TH_OK) return st;
       std::string err;
       if (!th_write_csv(hp, "Snapshot." + th_zero_pad(i, 2), names, cols, nullptr, err))
         return th_fail(ctx, TH_ERR_IO, err);
+      if (hp.o_T_hist) {                      // each snapshot's T joins the history (src/Run.cpp:109)
+        ctx->hist_t.push_back(hp.snaps[i]);
+        ctx->hist_T.insert(ctx->hist_T.end(), T.begin(), T.end());
+      }
     }
-    return TH_OK;
+    return write_T_hist(ctx);
   }
   th_status st = th_cuda_check(ctx, cudaSetDevice(ctx->device), "cudaSetDevice");
   if (st != TH_OK) return st;
@@ -1060,7 +1110,8 @@ th_status th_simulate(th_ctx* ctx) {
       if ((st = write_solidification_csv(ctx, prefix + th_zero_pad((int)last, 7))) != TH_OK) return st;
   }
   if ((st = write_solidification_csv(ctx, "Solidification.Final")) != TH_OK) return st;
-  // the reduced data after the grid's fields (bin/Main.cpp:104-119)
+  // the temperature history, then the reduced data, after the grid's fields (bin/Main.cpp:104-119)
+  if ((st = write_T_hist(ctx)) != TH_OK) return st;
   return hp.o_rdf ? write_rdf_csv(ctx, "RDF.Final") : TH_OK;
 }
 

@@ -148,7 +148,7 @@ class Deck:
 
     def _output_text(self) -> str:
         grid = [("x", 1), ("y", 1), ("z", 1)]
-        temp = [("T", self.outputs.get("T", 1)), ("T_hist", 0)]
+        temp = [("T", self.outputs.get("T", 1)), ("T_hist", self.outputs.get("T_hist", 0))]
         sol_keys = ["tSol", "G", "Gx", "Gy", "Gz", "V", "dTdt", "eqFrac", "depth", "numMelt"]
         sol = [(k, self.outputs.get(k, 0)) for k in sol_keys] + [("RDF", self.outputs.get("RDF", 0)),
                                                                   ("MP_Stats", 0)]

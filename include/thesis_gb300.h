@@ -190,10 +190,20 @@ th_status th_rrdf(th_ctx* ctx, uint32_t* idx, double* ts, double* Ts, int64_t ca
  * (src/Grid.cpp:203-273).  TH_ERR_IO if the file cannot be written. */
 th_status th_output_rrdf(th_ctx* ctx, const char* name, int32_t binary);
 
+/* With Output T_hist 1 (Tracking None only: every point is evaluated at the same times):
+ * the temperature history th_simulate or th_solidify collected - times the evaluation times
+ * (Snapshots: the snapshot times; Solidification: every step the loop ran), T time by time
+ * every point's temperature (pnum values per time, in point order).  Copies min(cap,
+ * ntimes) times and their rows into each non-null array; *ntimes receives the count.
+ * Replaces Grid::get_t_hist / get_T_hist (src/Grid.h:357-358), filled by Grid::Calc_T with
+ * set (src/Grid.cpp:300-304); th_simulate writes them as <name>T.hist.csv
+ * (Grid::Output_T_hist, src/Grid.cpp:101-136). */
+th_status th_T_hist(th_ctx* ctx, double* times, double* T, int64_t cap, int64_t* ntimes);
+
 /* Whole run as the reference CLI does it: the mode loop, then the CSV files under
  * <deck dir>/Data (same names, columns and number format; a Stork deck writes
  * <name>.RRDF.csv in place of <name>.Solidification.Final.csv; Output RDF 1 adds
- * <name>.RDF.Final.csv). */
+ * <name>.RDF.Final.csv; Output T_hist 1 adds <name>T.hist.csv). */
 th_status th_simulate(th_ctx* ctx);
 
 /* Point x node pairs evaluated by this context so far (temperature and gradient sums). */

@@ -107,6 +107,12 @@ void ref_output_rrdf(void* h, const char* name) {
   r->grid->Output_RRDF_csv(r->sim, name);
 }
 
+// The temperature history file (Grid::Output_T_hist, src/Grid.cpp:101-174).
+void ref_output_T_hist(void* h, const char* name) {
+  RefRun* r = (RefRun*)h;
+  r->grid->Output_T_hist(r->sim, name);
+}
+
 // The same rows as the reference's binary file (Grid::Output_RRDF_bin, src/Grid.cpp:241-273).
 void ref_output_rrdf_bin(void* h, const char* name) {
   RefRun* r = (RefRun*)h;

@@ -99,6 +99,14 @@ if "rrdf" in job:
     L.ref_output_rrdf_bin(h, b"RRDF")                # the binary form, kept apart from the CSV
     with open(os.path.join("Data", [nm for nm in os.listdir("Data") if nm.endswith(".bin")][0]), "rb") as f:
         out["bin_file"] = np.frombuffer(f.read(), dtype=np.uint8)
+if "thist" in job:
+    import os
+    L.ref_simulate(h)
+    L.ref_output_T_hist(h, b"T.hist")
+    nm = [f for f in os.listdir("Data") if f.endswith("T.hist.csv")][0]
+    out["thist_name"] = np.asarray(nm)
+    with open(os.path.join("Data", nm), "rb") as f:
+        out["thist_file"] = np.frombuffer(f.read(), dtype=np.uint8)
 if "fields" in job:
     L.ref_simulate(h)
     if "rdf" in job:
@@ -230,6 +238,31 @@ def csv_deck(name):
     return getattr(decks, name)()
 
 
+THIST_DECKS = ("thist_snapshot", "thist_notrack")
+
+
+def thist_deck(name):
+    """The deck each thist_<name>.npz fixture (Output T_hist 1) was made from."""
+    if name == "thist_snapshot":                   # three snapshots of a 30x20x5 grid
+        d = csv_deck("csv_snapshot")
+        d.outputs = {"T": 1, "T_hist": 1}
+    else:                                          # every step of a 16x14x5 grid without tracking
+        d = decks.small_stork()
+        d.tracking = "None"
+        d.axes = (decks.AxisSpec(-0.05e-3, 0.1e-3, num=16), decks.AxisSpec(-0.1e-3, 0.03e-3, num=14),
+                  decks.AxisSpec(-0.04e-3, 0.0, num=5))
+        d.outputs = {"T": 1, "tSol": 1, "T_hist": 1}
+    d.name = name
+    return d
+
+
+def thist_fixture(deck, scratch):
+    r = run_ref(deck, {"thist": np.asarray(1)}, scratch)
+    out = {"file_name": r["thist_name"], "file_bytes": r["thist_file"]}
+    np.savez_compressed(os.path.join(HERE, f"{deck.name}.npz"), **out)
+    return out
+
+
 def csv_fixture(deck, scratch):
     r = run_ref(deck, {"csv": np.asarray(deck.mode)}, scratch)
     out = {k: v for k, v in r.items() if k == "names" or k.startswith("file")}
@@ -288,6 +321,12 @@ def main():
             for i, name in enumerate(RRDF_DECKS):
                 rrdf_fixture(rrdf_deck(name), scratch, i == 0)
         print("rrdf fixtures written to", HERE)
+        return
+    if sys.argv[1:] == ["thist"]:
+        with tempfile.TemporaryDirectory() as scratch:
+            for name in THIST_DECKS:
+                thist_fixture(thist_deck(name), scratch)
+        print("thist fixtures written to", HERE)
         return
     if sys.argv[1:] == ["csv"]:
         with tempfile.TemporaryDirectory() as scratch:

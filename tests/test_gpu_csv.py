@@ -143,3 +143,41 @@ def test_simulate_writes_the_reference_rdf_file(built_library, thesis, oracle, t
             unit = 10.0 ** (np.floor(np.log10(max(abs(va), abs(vb)))) - 5)
             assert abs(vb - gpu_rows[r][c - 3]) <= 0.5 * unit * (1 + 1e-12), (r, c, b[c], gpu_rows[r][c - 3])
             assert abs(va - ref_rows[r][c - 3]) <= 0.5 * unit * (1 + 1e-12), (r, c, a[c], ref_rows[r][c - 3])
+
+
+def _read_thist(text):
+    """A temperature-history file: header fields, coordinate texts (n, 3), T texts (n, nt)."""
+    lines = text.splitlines()
+    rows = [ln.split(",") for ln in lines[1:]]
+    return lines[0].split(","), [r[:3] for r in rows], np.array([[float(v) for v in r[3:]] for r in rows])
+
+
+@pytest.mark.parametrize("name", make_golden.THIST_DECKS)
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_simulate_writes_the_reference_T_hist(built_library, thesis, tmp_path, name, prec):
+    """Output T_hist 1 without tracking (Grid::Output_T_hist, src/Grid.cpp:101-136, named as
+    bin/Main.cpp:113-115 names it): th_simulate writes <name>T.hist.csv with the reference's
+    header (x,y,z and the evaluation times, printed alike: the snapshot times, or every step
+    the solidification loop ran) and rows (every point's coordinates as the reference prints
+    them); each temperature, printed with 6 decimals, is within the temperature tolerance
+    (1e-7 K / 0.01 K) and half a printed unit of the reference's.  th_T_hist returns the same
+    history."""
+    deck = make_golden.thist_deck(name)
+    path = deck.write(str(tmp_path / name))
+    g = np.load(os.path.join(HERE, "golden", f"{name}.npz"))
+    with thesis.Simulation(path, prec) as sim:
+        sim.simulate()
+        t, T = sim.T_hist()
+    fname = str(g["file_name"])
+    with open(os.path.join(os.path.dirname(path), "Data", fname)) as f:
+        got = f.read()
+    ref_head, ref_xyz, ref_T = _read_thist(bytes(g["file_bytes"]).decode())
+    head, xyz, T_txt = _read_thist(got)
+    assert head == ref_head
+    assert xyz == ref_xyz
+    tol = 1e-7 if prec == "fp64" else 0.01
+    err = np.abs(T_txt - ref_T)
+    assert float(err.max()) <= tol + 1e-6, (float(err.max()), np.unravel_index(np.argmax(err), err.shape))
+    assert ["%f" % v for v in t] == ref_head[3:]
+    assert T.shape == (len(t), len(ref_xyz))
+    assert float(np.max(np.abs(T.T - T_txt))) <= 5e-7 + 1e-9

@@ -95,6 +95,24 @@ def test_oracle_stork_rows_match_reference(name, oracle, tmp_path):
         assert idx[:, 2].min() == 0
 
 
+def test_oracle_snapshots_print_as_the_reference_T_hist(oracle, tmp_path):
+    """The reference's temperature-history file of a Snapshots deck (Output T_hist 1,
+    Grid::Output_T_hist, src/Grid.cpp:101-136): its header holds the snapshot times and
+    each row a point's temperature at every snapshot, all printed with 6 decimals; the
+    oracle's snapshots print to the same text."""
+    g = _load("thist_snapshot.npz")
+    lines = bytes(g["file_bytes"]).decode().splitlines()
+    deck = make_golden.thist_deck("thist_snapshot")
+    o = oracle(deck.write(str(tmp_path / deck.name)))
+    head = lines[0].split(",")
+    assert head[:3] == ["x", "y", "z"] and len(head) == 3 + o.n_snapshots
+    assert head[3:] == ["%f" % o.snapshot_time(i) for i in range(o.n_snapshots)]
+    T = [o.snapshot(i, threads=2) for i in range(o.n_snapshots)]
+    assert len(lines) == 1 + T[0].size
+    for p in range(0, T[0].size, 97):
+        assert lines[1 + p].split(",")[3:] == ["%f" % T[i][p] for i in range(len(T))], p
+
+
 def test_reference_rrdf_binary_layout():
     """The reference's binary RRDF file of small_stork (Grid::Output_RRDF_bin,
     src/Grid.cpp:241-273) read with the layout the GPU test checks the library's file
