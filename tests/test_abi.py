@@ -45,6 +45,7 @@ def test_missing_deck_is_an_error(thesis, built_library, tmp_path):
     (lambda d: setattr(d, "mode", "Bogus"), "exactly one"),
     (lambda d: setattr(d, "tracking", "Geometry"), "tracking"),
     (lambda d: setattr(d.beams[0], "width_x", 0.0), "widths"),
+    (lambda d: d.outputs.update(T_hist=1), "T_hist output needs Tracking None"),
 ])
 def test_bad_decks_are_rejected_before_any_launch(thesis, built_library, decks, tmp_path, edit, needle):
     d = decks.small_surface("Surface")
@@ -55,3 +56,16 @@ def test_bad_decks_are_rejected_before_any_launch(thesis, built_library, decks, 
             f.write("Bogus\n{\n}\n")
     st, msg, ctx = _create(thesis, path)
     assert st != 0 and needle.lower() in msg.lower() and not ctx.value
+
+
+def test_T_hist_decks_without_tracking_parse(thesis, built_library, tmp_path):
+    """Output T_hist 1 is taken without tracking (Snapshots and NoTracking solidification:
+    every point shares the evaluation times); the host-only parse accepts both decks."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import make_golden
+    import numpy as np
+    for name in make_golden.THIST_DECKS:
+        d = make_golden.thist_deck(name)
+        info = thesis.deck_info(d.write(str(tmp_path / name)))
+        assert info["pnum"] == np.prod([ax.num for ax in d.axes])
