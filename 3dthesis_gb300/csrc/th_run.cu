@@ -17,6 +17,7 @@
 #include <cstdlib>
 #include <cstdio>
 #include <cstring>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -687,7 +688,12 @@ th_status record_T_hist(th_ctx* ctx, RunState* r, int k) {
   if (st != TH_OK || (st = th_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "T_hist")) != TH_OK) return st;
   if (step != k + 1) return TH_OK;
   const size_t n = (size_t)ctx->hp.pnum, at = ctx->hist_T.size();
-  ctx->hist_T.resize(at + n);
+  try {                                   // every step adds pnum values on the host
+    ctx->hist_T.resize(at + n);
+    ctx->hist_t.reserve(ctx->hist_t.size() + 1);
+  } catch (const std::bad_alloc&) {
+    return th_fail(ctx, TH_ERR_CAPACITY, "the T_hist history does not fit in host memory");
+  }
   if ((st = fetch_field(ctx, F_T, ctx->hist_T.data() + at)) != TH_OK) return st;
   ctx->hist_t.push_back(time_of(r, ctx->hp.dt, k));
   return TH_OK;
@@ -1072,8 +1078,12 @@ th_status th_simulate(th_ctx* ctx) {
       if (!th_write_csv(hp, "Snapshot." + th_zero_pad(i, 2), names, cols, nullptr, err))
         return th_fail(ctx, TH_ERR_IO, err);
       if (hp.o_T_hist) {                      // each snapshot's T joins the history (src/Run.cpp:109)
-        ctx->hist_t.push_back(hp.snaps[i]);
-        ctx->hist_T.insert(ctx->hist_T.end(), T.begin(), T.end());
+        try {
+          ctx->hist_t.push_back(hp.snaps[i]);
+          ctx->hist_T.insert(ctx->hist_T.end(), T.begin(), T.end());
+        } catch (const std::bad_alloc&) {
+          return th_fail(ctx, TH_ERR_CAPACITY, "the T_hist history does not fit in host memory");
+        }
       }
     }
     return write_T_hist(ctx);
