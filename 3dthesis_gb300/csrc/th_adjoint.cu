@@ -446,6 +446,7 @@ th_status th_adj_create(const char* param_input, int32_t precision, const int64_
   std::string e;
   if (!th_load_deck(param_input, A->hp, e)) { delete A; return afail(nullptr, TH_ERR_INVALID, e); }
   if (A->hp.beams.size() != 1) { delete A; return afail(nullptr, TH_ERR_UNSUPPORTED, "the adjoint takes single-beam decks"); }
+  if (A->hp.custom) { delete A; return afail(nullptr, TH_ERR_UNSUPPORTED, "the adjoint takes grid decks (probes are grid points)"); }
   if (A->hp.compress) {
     delete A;
     return afail(nullptr, TH_ERR_UNSUPPORTED, "the adjoint takes decks without path compression");

@@ -144,6 +144,17 @@ th_status th_ctx_create_from_deck(const char* param_input, int32_t precision, th
                     "cudaMemcpy") != TH_OK)
     return fail(TH_ERR_CUDA);
   th_make_dev_problem(ctx->hp, ctx->d_segs, ctx->dp);
+  if (ctx->hp.custom) {                     // the custom points' coordinates, read by point_xyz
+    const size_t n = (size_t)ctx->hp.pnum;
+    if (th_cuda_check(ctx, create_malloc((void**)&ctx->d_custom, 3 * n * sizeof(double)), "cudaMalloc") != TH_OK)
+      return fail(TH_ERR_CUDA);
+    const std::vector<double>* c[3] = {&ctx->hp.px, &ctx->hp.py, &ctx->hp.pz};
+    for (int a = 0; a < 3; ++a)
+      if (th_cuda_check(ctx, cudaMemcpy(ctx->d_custom + a * n, c[a]->data(), n * sizeof(double), cudaMemcpyHostToDevice),
+                        "cudaMemcpy") != TH_OK)
+        return fail(TH_ERR_CUDA);
+    ctx->dp.cx = ctx->d_custom; ctx->dp.cy = ctx->d_custom + n; ctx->dp.cz = ctx->d_custom + 2 * n;
+  }
   if (ctx->dp.n_images > TH_MAX_IMAGES) {
     ctx->err = "more boundary images than TH_MAX_IMAGES";
     return fail(TH_ERR_CAPACITY);
@@ -172,6 +183,7 @@ void th_ctx_destroy(th_ctx* ctx) {
   th_release_run_state(ctx);
   cudaFree(ctx->node_mem);
   cudaFree(ctx->d_segs);
+  cudaFree(ctx->d_custom);
   cudaFree(ctx->d_small);
   cudaFree(ctx->d_pairs);
   cudaFree(ctx->d_T);

@@ -139,6 +139,11 @@ th_status th_batch_create(const char* const* param_inputs, int32_t n, int32_t pr
       delete b;
       return TH_ERR_INVALID;
     }
+    if (b->hp[d].custom) {                 // the batch kernels tile grids
+      g_batch_error = std::string("deck ") + std::to_string(d) + " has custom points (not a grid)";
+      delete b;
+      return TH_ERR_UNSUPPORTED;
+    }
   }
   b->n_snap = INT32_MAX;
   for (const HostProblem& h : b->hp) b->n_snap = std::min<int>(b->n_snap, (int)h.snaps.size());

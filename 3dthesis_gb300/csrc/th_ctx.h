@@ -22,6 +22,7 @@ struct th_ctx {
   std::string err;
 
   DevSeg* d_segs = nullptr;
+  double* d_custom = nullptr;             // custom points' x, y, z (pnum each), null for a grid
   void* node_mem = nullptr;
   NodeBufView nb{};
   int* d_small = nullptr;                 // [0] node count, [1] error bits, [2..] scratch

@@ -66,6 +66,10 @@ __device__ __forceinline__ void store_node(const NodeBufView& nb, int slot, cons
 }
 
 __device__ __forceinline__ void point_xyz(const DevProblem& P, int64_t p, double& x, double& y, double& z) {
+  if (P.cx) {                               // custom points (Grid::get_x with its x array, src/Grid.h:310-327)
+    x = P.cx[p]; y = P.cy[p]; z = P.cz[p];
+    return;
+  }
   const int64_t nyz = (int64_t)P.ny * P.nz;
   const int i = (int)(p / nyz), j = (int)((p / P.nz) % P.ny), k = (int)(p % P.nz);
   x = coord(P.gx, P.xmin, P.xmax, P.hx, i);

@@ -235,7 +235,7 @@ __global__ void __launch_bounds__(kThreads) k_list_fp32(DevProblem P, NodeBufVie
   const int64_t gi = (int64_t)blockIdx.x * kThreads + threadIdx.x;
   const bool live = gi < n;
   double x = 0, y = 0, z = 0;
-  if (live) point_xyz(P, pts[gi], x, y, z);
+  if (live) point_xyz(P, pts ? pts[gi] : gi, x, y, z);   // pts null: points 0 .. n - 1
   const float xh = __double2float_rn(x), yh = __double2float_rn(y), zh = __double2float_rn(z);
   const float xl = __double2float_rn(x - (double)xh), yl = __double2float_rn(y - (double)yh),
               zl = __double2float_rn(z - (double)zh);
@@ -275,7 +275,7 @@ __global__ void __launch_bounds__(kThreads) k_list_fp64(DevProblem P, NodeBufVie
   const int64_t gi = (int64_t)blockIdx.x * kThreads + threadIdx.x;
   const bool live = gi < n;
   double x = 0, y = 0, z = 0;
-  if (live) point_xyz(P, pts[gi], x, y, z);
+  if (live) point_xyz(P, pts ? pts[gi] : gi, x, y, z);   // pts null: points 0 .. n - 1
   double s = 0.0;
   for (int base = 0; base < nn; base += kChunk) {
     __syncthreads();
@@ -335,6 +335,8 @@ bool th_tile_shape_supported(TileShape sh) {
 
 void th_launch_grid_sum(const DevProblem& P, const NodeBufView& nb, const int* d_count, double* d_T, int precision,
                         TileShape sh, unsigned long long* pairs, cudaStream_t s) {
+  // custom points have no grid to tile: every point as a list
+  if (P.cx) { th_launch_list_sum(P, nb, d_count, nullptr, P.pnum, d_T, precision, pairs, s); return; }
   if (sh.kp == 4 && sh.kch == 1) launch_grid<4, 1>(P, nb, d_count, d_T, precision, pairs, s);
   else if (sh.kp == 4 && sh.kch == 4) launch_grid<4, 4>(P, nb, d_count, d_T, precision, pairs, s);
   else if (sh.kp == 2 && sh.kch == 2) launch_grid<2, 2>(P, nb, d_count, d_T, precision, pairs, s);

@@ -22,11 +22,12 @@ struct TileShape { int kp, kch; };
 void th_launch_nodes(const DevProblem& P, double t, bool is_sol, const NodeBufView& nb, int* d_count, int* d_err,
                      cudaStream_t s);
 
-// T at every grid point (p = i*ny*nz + j*nz + k) from the node list.
+// T at every grid point (p = i*ny*nz + j*nz + k) from the node list (custom points: every
+// point, by the list kernels).
 void th_launch_grid_sum(const DevProblem& P, const NodeBufView& nb, const int* d_count, double* d_T, int precision,
                         TileShape shape, unsigned long long* d_pairs, cudaStream_t s);
 
-// T at n listed points.
+// T at n listed points (d_pts null: points 0 .. n - 1).
 void th_launch_list_sum(const DevProblem& P, const NodeBufView& nb, const int* d_count, const int64_t* d_pts,
                         int64_t n, double* d_T, int precision, unsigned long long* d_pairs, cudaStream_t s);
 

@@ -136,6 +136,7 @@ bool th_write_rdf_csv(const HostProblem& hp, const std::string& tag, const int64
 }
 
 void th_point_coord(const HostProblem& hp, int64_t p, double& x, double& y, double& z) {
+  if (hp.custom) { x = hp.px[p]; y = hp.py[p]; z = hp.pz[p]; return; }
   const int gx = (uint16_t)hp.nx, gy = (uint16_t)hp.ny, gz = (uint16_t)hp.nz;
   const int64_t nyz = (int64_t)hp.ny * hp.nz;
   const int i = (int)(p / nyz), j = (int)((p / hp.nz) % hp.ny), k = (int)(p % hp.nz);
@@ -145,6 +146,7 @@ void th_point_coord(const HostProblem& hp, int64_t p, double& x, double& y, doub
 }
 
 void th_grid_coords(const HostProblem& hp, std::vector<double>& x, std::vector<double>& y, std::vector<double>& z) {
+  if (hp.custom) { x = hp.px; y = hp.py; z = hp.pz; return; }
   const int gx = (uint16_t)hp.nx, gy = (uint16_t)hp.ny, gz = (uint16_t)hp.nz;
   const double hx = gx > 1 ? (hp.xmax - hp.xmin) / (gx - 1) : 0.0;
   const double hy = gy > 1 ? (hp.ymax - hp.ymin) / (gy - 1) : 0.0;

@@ -278,7 +278,22 @@ bool th_load_deck(const std::string& param_input, HostProblem& hp, std::string& 
       hp.bcy0 = d.num("BoundaryConditions", "Y_min", DBL_MAX); hp.bcy1 = d.num("BoundaryConditions", "Y_max", DBL_MAX);
       hp.bcz0 = d.num("BoundaryConditions", "Z_min", DBL_MAX); hp.bc_refl = d.integer("BoundaryConditions", "Reflections", INT_MAX);
       hp.use_bcs = hp.bcx0 != DBL_MAX || hp.bcx1 != DBL_MAX || hp.bcy0 != DBL_MAX || hp.bcy1 != DBL_MAX || hp.bcz0 != DBL_MAX;
-      if (!d.str("Custom", "File").empty()) { err = "custom point files are not supported"; return false; }
+      // custom points (src/Init.cpp:686-703), read as Init::FileRead_Points does
+      // (src/Init.cpp:816-857): the first line is skipped; then, point by point, the rest of
+      // the current line is skipped and three numbers are read (mm), until a read fails
+      const std::string f_pts = d.str("Custom", "File");
+      hp.custom = !f_pts.empty();
+      hp.px.clear(); hp.py.clear(); hp.pz.clear();
+      if (hp.custom) {
+        std::ifstream in(join_dir(hp.dir, f_pts));
+        if (!in) { err = "cannot open the points file " + f_pts; return false; }
+        std::string line;
+        double x = 0, y = 0, z = 0;
+        while (std::getline(in, line) && (in >> x >> y >> z)) {
+          hp.px.push_back(x / 1000.0); hp.py.push_back(y / 1000.0); hp.pz.push_back(z / 1000.0);
+        }
+        if (hp.px.empty()) { err = "no points found in " + f_pts; return false; }
+      }
 
       double sx0 = DBL_MAX, sx1 = -DBL_MAX, sy0 = DBL_MAX, sy1 = -DBL_MAX, sz0 = DBL_MAX, sz1 = -DBL_MAX;
       double px = 0, py = 0, pz = 0, pq = 0;
@@ -303,13 +318,22 @@ bool th_load_deck(const std::string& param_input, HostProblem& hp, std::string& 
       if (hp.ymax == DBL_MAX) hp.ymax = sy1 + 500e-6;
       if (hp.zmin == -DBL_MAX) hp.zmin = sz0 - 250e-6;
       if (hp.zmax == DBL_MAX) hp.zmax = sz1;
-      axis(hp.nx, hp.xmin, hp.xmax, hp.xres, hp.nx == 1);
-      axis(hp.ny, hp.ymin, hp.ymax, hp.yres, hp.ny == 1);
-      axis(hp.nz, hp.zmin, hp.zmax, hp.zres, hp.ny == 1);
-      if (hp.nx < 1 || hp.ny < 1 || hp.nz < 1 || hp.nx > 65535 || hp.ny > 65535 || hp.nz > 65535) {
-        err = "grid axis counts must be within 1..65535"; return false;
+      if (hp.custom) {
+        // no grid (src/Init.cpp:866-869): the points are the list, laid out as pnum x 1 x 1;
+        // such a run goes without tracking (src/Run.cpp:61, 391)
+        if (hp.px.size() > (size_t)INT_MAX) { err = "too many custom points"; return false; }
+        hp.nx = (int)hp.px.size(); hp.ny = hp.nz = 1;
+        hp.pnum = (int64_t)hp.px.size();
+        hp.tracking = TH_TRACK_NONE;
+      } else {
+        axis(hp.nx, hp.xmin, hp.xmax, hp.xres, hp.nx == 1);
+        axis(hp.ny, hp.ymin, hp.ymax, hp.yres, hp.ny == 1);
+        axis(hp.nz, hp.zmin, hp.zmax, hp.zres, hp.ny == 1);
+        if (hp.nx < 1 || hp.ny < 1 || hp.nz < 1 || hp.nx > 65535 || hp.ny > 65535 || hp.nz > 65535) {
+          err = "grid axis counts must be within 1..65535"; return false;
+        }
+        hp.pnum = (int64_t)hp.nx * hp.ny * hp.nz;
       }
-      hp.pnum = (int64_t)hp.nx * hp.ny * hp.nz;
     }
     // outputs (src/Init.cpp:709-771)
     {
@@ -407,6 +431,7 @@ void th_make_dev_problem(const HostProblem& hp, const DevSeg* d_segs, DevProblem
     dp.tl_df[0] = f0; dp.tl_df[1] = f1; dp.tl_df[2] = f2;
   }
   dp.cetN0 = hp.cetN0; dp.cetn = hp.cetn; dp.ceta = hp.ceta;
+  dp.cx = dp.cy = dp.cz = nullptr;          // set by the context for custom points
   dp.nx = hp.nx; dp.ny = hp.ny; dp.nz = hp.nz;
   udiv_magic((uint32_t)std::max(1, hp.nz), dp.div_nz_m, dp.div_nz_s);
   udiv_magic((uint32_t)std::max(1, hp.ny), dp.div_ny_m, dp.div_ny_s);

@@ -63,6 +63,11 @@ struct DevProblem {
   double end_time;
   // Gauss-Legendre tables for orders 2/4/8/16 packed at offset order - 2
   double gl_loc[30], gl_w[30];
+  // custom points (Domain: Custom File): every point's coordinates, pnum each (device
+  // arrays); null for a grid
+  const double* cx;
+  const double* cy;
+  const double* cz;
 };
 
 struct HostBeam { double ax, ay, az, eff, q, nond, power; };
@@ -92,6 +97,8 @@ struct HostProblem {
   bool o_x, o_y, o_z, o_T, o_tSol, o_G, o_Gx, o_Gy, o_Gz, o_V, o_dTdt, o_eqFrac, o_depth, o_numMelt;
   bool o_rdf;                     // the reduced data format (per point melting / solidification events)
   bool o_T_hist;                  // every point's temperature at every evaluation (Tracking None)
+  bool custom = false;            // points from a points file (Domain: Custom File), not a grid
+  std::vector<double> px, py, pz; // their coordinates (m)
   bool do_sol;
   // settings
   double sol_tol;

@@ -73,6 +73,9 @@ class Deck:
     max_threads: int = 1
     bcs: Optional[Dict[str, float]] = None
     settings_extra: Dict[str, Dict[str, str]] = field(default_factory=dict)
+    # custom points in place of a grid (Domain: Custom File), mm, written to Points.txt under
+    # a header line (the reference skips the file's first line)
+    points: Optional[Sequence[Tuple[float, float, float]]] = None
 
     # ------------------------------------------------------------------ write
     def write(self, directory: str) -> str:
@@ -94,6 +97,8 @@ class Deck:
             "Output.txt": self._output_text(),
             "Settings.txt": self._settings_text(),
         }
+        if self.points is not None:
+            files["Points.txt"] = "x y z\n" + "".join(f"{_f(x)} {_f(y)} {_f(z)}\n" for x, y, z in self.points)
         for i, (b, p) in enumerate(zip(self.beams, self.paths)):
             bname = f"Beam.{i + 1}.txt" if multi else "Beam.txt"
             pname = f"Path.{i + 1}.txt" if multi else "Path.txt"
@@ -144,6 +149,8 @@ class Deck:
                 text += _block(name, items)
         if self.bcs:
             text += _block("BoundaryConditions", [(k, _f(v)) for k, v in self.bcs.items()])
+        if self.points is not None:
+            text += _block("Custom", [("File", "Points.txt")])
         return text
 
     def _output_text(self) -> str:

@@ -99,6 +99,18 @@ if "rrdf" in job:
     L.ref_output_rrdf_bin(h, b"RRDF")                # the binary form, kept apart from the CSV
     with open(os.path.join("Data", [nm for nm in os.listdir("Data") if nm.endswith(".bin")][0]), "rb") as f:
         out["bin_file"] = np.frombuffer(f.read(), dtype=np.uint8)
+if "custom" in job:
+    import os
+    L.ref_simulate(h)
+    if str(job["custom"]) == "Solidification":
+        L.ref_output(h, b"Solidification.Final")
+        for f in ("T", "tSol", "G", "V", "dTdt"):
+            a = np.zeros(int(info[3])); L.ref_field(h, f.encode(), a.ctypes.data_as(ctypes.c_void_p)); out[f] = a
+    names = sorted(os.listdir("Data"))
+    out["names"] = np.array(names)
+    for i, nm in enumerate(names):
+        with open(os.path.join("Data", nm), "rb") as f:
+            out[f"file{i}"] = np.frombuffer(f.read(), dtype=np.uint8)
 if "thist" in job:
     import os
     L.ref_simulate(h)
@@ -238,6 +250,39 @@ def csv_deck(name):
     return getattr(decks, name)()
 
 
+CUSTOM_DECKS = ("custom_snapshot", "custom_notrack")
+
+
+def custom_deck(name):
+    """The deck each custom_<name>.npz fixture (Domain: Custom File) was made from: seeded
+    points over the scanned area instead of a grid (the Domain's grid stays in the file and
+    only bounds the domain)."""
+    rng = np.random.default_rng(11)
+    if name == "custom_snapshot":
+        d = decks.small_snapshot()
+        lo, hi = (0.0, -0.05, -0.09), (0.59, 0.34, 0.0)
+        n = 300
+    else:                                          # Surface tracking in the file: the run goes without
+        d = decks.small_surface("Surface")
+        lo, hi = (-0.05, -0.1, -0.11), (0.44, 0.29, 0.0)
+        n = 200
+        d.outputs = {"T": 1, "tSol": 1, "G": 1, "V": 1, "dTdt": 1}
+    pts = rng.uniform(lo, hi, size=(n, 3))
+    pts[: n // 4, 2] = 0.0                         # a quarter on the top surface
+    d.points = [tuple(float(v) for v in p) for p in pts]
+    d.name = name
+    return d
+
+
+def custom_fixture(deck, scratch):
+    job = {"custom": np.asarray(deck.mode), "pts": np.arange(len(deck.points), dtype=np.int64)}
+    if deck.mode != "Snapshots":
+        del job["pts"]
+    r = run_ref(deck, job, scratch)
+    np.savez_compressed(os.path.join(HERE, f"{deck.name}.npz"), **r)
+    return r
+
+
 THIST_DECKS = ("thist_snapshot", "thist_notrack")
 
 
@@ -321,6 +366,12 @@ def main():
             for i, name in enumerate(RRDF_DECKS):
                 rrdf_fixture(rrdf_deck(name), scratch, i == 0)
         print("rrdf fixtures written to", HERE)
+        return
+    if sys.argv[1:] == ["custom"]:
+        with tempfile.TemporaryDirectory() as scratch:
+            for name in CUSTOM_DECKS:
+                custom_fixture(custom_deck(name), scratch)
+        print("custom fixtures written to", HERE)
         return
     if sys.argv[1:] == ["thist"]:
         with tempfile.TemporaryDirectory() as scratch:

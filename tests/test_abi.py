@@ -58,6 +58,30 @@ def test_bad_decks_are_rejected_before_any_launch(thesis, built_library, decks, 
     assert st != 0 and needle.lower() in msg.lower() and not ctx.value
 
 
+def test_custom_point_files_are_read_as_the_reference_reads_them(thesis, built_library, tmp_path):
+    """Domain: Custom File (Init::FileRead_Points, src/Init.cpp:816-857): the first line is
+    skipped, each point is three numbers in mm, and a custom deck goes without tracking.  The
+    point counts are the reference's (tests/golden/custom_*.npz); a file whose first line
+    already holds a point loses that point, as the reference's does."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import make_golden
+    import numpy as np
+    for name in make_golden.CUSTOM_DECKS:
+        d = make_golden.custom_deck(name)
+        g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", f"{name}.npz"))
+        info = thesis.deck_info(d.write(str(tmp_path / name)))
+        assert info["pnum"] == int(g["info"][3]) == len(d.points)
+        assert info["tracking"] == 0
+    path = d.write(str(tmp_path / "noheader"))
+    pts = os.path.join(os.path.dirname(path), "Points.txt")
+    with open(pts) as f:
+        lines = f.read().splitlines()
+    with open(pts, "w") as f:
+        f.write("\n".join(lines[1:]) + "\n")
+    assert thesis.deck_info(path)["pnum"] == len(d.points) - 1
+
+
 def test_T_hist_decks_without_tracking_parse(thesis, built_library, tmp_path):
     """Output T_hist 1 is taken without tracking (Snapshots and NoTracking solidification:
     every point shares the evaluation times); the host-only parse accepts both decks."""

@@ -181,3 +181,85 @@ def test_simulate_writes_the_reference_T_hist(built_library, thesis, tmp_path, n
     assert ["%f" % v for v in t] == ref_head[3:]
     assert T.shape == (len(t), len(ref_xyz))
     assert float(np.max(np.abs(T.T - T_txt))) <= 5e-7 + 1e-9
+
+
+def _close_text(a, b, tol):
+    """Two printed values: equal text, or within the tolerance and one printed unit."""
+    if a == b:
+        return True
+    va, vb = float(a), float(b)
+    unit = 10.0 ** (np.floor(np.log10(max(abs(va), abs(vb), 1e-300))) - 5)
+    return abs(va - vb) <= tol + unit * (1 + 1e-9)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_custom_points_snapshots_match_the_reference(built_library, thesis, tmp_path, prec):
+    """Domain: Custom File (src/Init.cpp:686-703, 816-857): the points file's points in place
+    of a grid, evaluated like the grid (src/Run.cpp:61, 80-124).  Every snapshot's T at every
+    point within 1e-7 K (FP64) / 0.01 K (FP32) of the reference's, and th_simulate writes the
+    reference's Snapshot files: the same header, the points' coordinates as the reference
+    prints them, each T within the tolerance and a printed unit."""
+    deck = make_golden.custom_deck("custom_snapshot")
+    path = deck.write(str(tmp_path / deck.name))
+    g = np.load(os.path.join(HERE, "golden", "custom_snapshot.npz"))
+    tol = 1e-7 if prec == "fp64" else 0.01
+    with thesis.Simulation(path, prec) as sim:
+        assert sim.pnum == len(deck.points)
+        for i in range(3):
+            T = sim.snapshot(i)
+            err = float(np.max(np.abs(T - g[f"T{i}"])))
+            assert err <= tol, (i, err)
+        sim.simulate()
+    data = os.path.join(os.path.dirname(path), "Data")
+    names = [str(n) for n in g["names"]]
+    assert sorted(os.listdir(data)) == names
+    for i, nm in enumerate(names):
+        ref = bytes(g[f"file{i}"]).decode().splitlines()
+        with open(os.path.join(data, nm)) as f:
+            got = f.read().splitlines()
+        assert got[0] == ref[0] and len(got) == len(ref)
+        for r, (a, b) in enumerate(zip(ref[1:], got[1:])):
+            ra, rb = a.split(","), b.split(",")
+            assert ra[:3] == rb[:3], (nm, r, a, b)
+            assert _close_text(ra[3], rb[3], tol), (nm, r, a, b)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_custom_points_solidify_without_tracking(built_library, thesis, tmp_path, prec):
+    """A Solidification deck with custom points runs without tracking whatever its Tracking
+    says (src/Run.cpp:391): every point every step (src/Run.cpp:409-467).  Its fields are the
+    reference's within the parity tolerances (T 1e-7 / 0.01 K, tSol 1e-15 / 1e-8 s, G and V
+    1e-9 / 1e-4 relative, the int-truncated dTdt within a unit beyond that), and the
+    Solidification.Final file has the reference's header, rows and coordinates.  A point's
+    G, V and dTdt may differ only where its two solidification times fall on different
+    quadrature schedules: the node lists at the two times (th_nodes, bit for bit the
+    reference's) differ, so the gradient sums run over different nodes (an ulp of t_sol
+    can flip the schedule)."""
+    deck = make_golden.custom_deck("custom_notrack")
+    path = deck.write(str(tmp_path / deck.name))
+    g = np.load(os.path.join(HERE, "golden", "custom_notrack.npz"))
+    fp64 = prec == "fp64"
+    rel = 1e-9 if fp64 else 1e-4
+    with thesis.Simulation(path, prec) as sim:
+        assert sim.info["tracking"] == 0                  # TH_TRACK_NONE
+        sim.simulate()
+        got = {f: sim.field(f) for f in ("T", "tSol", "G", "V", "dTdt")}
+        off = np.zeros(len(deck.points), dtype=bool)
+        for f in ("G", "V"):
+            off |= np.abs(got[f] - g[f]) > rel * np.abs(g[f]) + 1e-300
+        off |= np.abs(got["dTdt"] - g["dTdt"]) > rel * np.abs(g["dTdt"]) + 1.0
+        unexplained = []
+        for p in np.flatnonzero(off):
+            a, b = sim.integrate(got["tSol"][p], True), sim.integrate(g["tSol"][p], True)
+            if all(np.array_equal(a[k], b[k]) for k in a):
+                unexplained.append(int(p))
+    assert (g["tSol"] > 0).sum() > 30
+    assert np.array_equal(got["tSol"] > 0, g["tSol"] > 0)
+    assert float(np.max(np.abs(got["T"] - g["T"]))) <= (1e-7 if fp64 else 0.01)
+    assert float(np.max(np.abs(got["tSol"] - g["tSol"]))) <= (1e-15 if fp64 else 1e-8)
+    assert unexplained == [], (int(off.sum()), unexplained)
+    ref = bytes(g["file0"]).decode().splitlines()
+    with open(os.path.join(os.path.dirname(path), "Data", str(g["names"][0]))) as f:
+        out = f.read().splitlines()
+    assert out[0] == ref[0] and len(out) == len(ref)
+    assert [r.split(",")[:3] for r in out[1:]] == [r.split(",")[:3] for r in ref[1:]]
