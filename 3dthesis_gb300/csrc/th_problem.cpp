@@ -255,7 +255,8 @@ bool th_load_deck(const std::string& param_input, HostProblem& hp, std::string& 
         if (!times.empty()) { std::stringstream ss(times); while (std::getline(ss, item, ',')) hp.snaps.push_back(std::stod(item)); }
         if (!fracs.empty()) { std::stringstream ss(fracs); while (std::getline(ss, item, ',')) hp.snaps.push_back(std::stod(item) / 100.0 * hp.end_time); }
         hp.tracking = parse_tracking(m.str("Snapshots", "Tracking"), ok);
-        if (!ok || hp.tracking != TH_TRACK_NONE) { err = "snapshot tracking modes other than None are not supported"; return false; }
+        if (!ok) { err = "snapshot tracking modes other than None are not supported"; return false; }
+        // other modes are refused once the domain is read: custom points go without tracking
       } else {
         hp.mode = 1;
         hp.tracking = parse_tracking(m.str("Solidification", "Tracking"), ok);
@@ -333,6 +334,9 @@ bool th_load_deck(const std::string& param_input, HostProblem& hp, std::string& 
           err = "grid axis counts must be within 1..65535"; return false;
         }
         hp.pnum = (int64_t)hp.nx * hp.ny * hp.nz;
+        if (hp.mode == 0 && hp.tracking != TH_TRACK_NONE) {
+          err = "snapshot tracking modes other than None are not supported"; return false;
+        }
       }
     }
     // outputs (src/Init.cpp:709-771)

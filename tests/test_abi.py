@@ -73,6 +73,13 @@ def test_custom_point_files_are_read_as_the_reference_reads_them(thesis, built_l
         info = thesis.deck_info(d.write(str(tmp_path / name)))
         assert info["pnum"] == int(g["info"][3]) == len(d.points)
         assert info["tracking"] == 0
+    snap = make_golden.custom_deck("custom_snapshot")          # Snapshots with a tracking mode:
+    snap.tracking = "Volume"                                    # without tracking for custom points
+    assert thesis.deck_info(snap.write(str(tmp_path / "snapvol")))["tracking"] == 0
+    grid = make_golden.csv_deck("csv_snapshot")                 # and still refused on a grid
+    grid.tracking = "Volume"
+    with pytest.raises(thesis.ThesisError):
+        thesis.deck_info(grid.write(str(tmp_path / "gridvol")))
     path = d.write(str(tmp_path / "noheader"))
     pts = os.path.join(os.path.dirname(path), "Points.txt")
     with open(pts) as f:
