@@ -1,5 +1,5 @@
 // Issue-rate probe of the device: MUFU.EX2 and FP32 FMA results per SM per clock, measured
-// with a throughput-bound kernel, for the roofline the point x node kernels are judged
+// with a throughput-bound kernel, for the roofline the point x node kernels are measured
 // against (each FP32 pair costs about ten FP32 lane-operations and one ex2).
 #include <cuda_runtime.h>
 
