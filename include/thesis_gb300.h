@@ -217,7 +217,7 @@ th_status th_set_tile_shape(th_ctx* ctx, int32_t kp, int32_t kch);
 th_status th_last_kernel_ms(th_ctx* ctx, float* out);
 
 /* Issue rates of the current device, measured with throughput-bound probe kernels, for
- * the roofline the point x node kernels are judged against.  No counterpart in the
+ * the roofline the point x node kernels are measured against.  No counterpart in the
  * reference (it has no GPU code).  out[0] SM count, out[1] the device's maximum SM clock
  * (MHz), out[2] MUFU ex2 results per SM per clock, out[3] FP32 FMA lane-operations per SM
  * per clock. */
