@@ -96,6 +96,10 @@ struct Problem {
   bool use_bcs; int bc_refl; double bcx0, bcx1, bcy0, bcy1, bcz0;
   // grid copies of the axis counts are uint16_t in the reference (src/Grid.h:65-67)
   int gx, gy, gz;
+  // custom points in place of a grid (Domain: Custom File, src/Init.cpp:686-703): their
+  // coordinates, in the file's order
+  bool custom = false;
+  std::vector<double> cx, cy, cz;
   // mode
   int mode;  // 0 Snapshots, 1 Solidification
   std::vector<double> snaps;
@@ -300,8 +304,9 @@ bool load_problem(Problem& P, const std::string& param_input, std::string& err) 
       if (!m[0][0].empty()) { std::stringstream ss(m[0][0]); while (std::getline(ss, item, ',')) P.snaps.push_back(std::stod(item)); }
       if (!m[0][1].empty()) { std::stringstream ss(m[0][1]); while (std::getline(ss, item, ',')) P.snaps.push_back(std::stod(item) / 100.0 * P.end_time); }
       const std::string tr = m[0][2].empty() ? "None" : m[0][2];
-      if (tr != "None") { err = "snapshot tracking " + tr + " is not supported"; return false; }
-      P.tracking = TRACK_NONE;
+      // other modes are refused once the domain is read: custom points go without tracking
+      // (src/Run.cpp:61)
+      P.tracking = tr == "None" ? TRACK_NONE : -1;
       P.dt = 1e-5; P.out_freq = INT_MAX; P.rcheck = 1.0; P.secondary = false;
     } else {
       P.mode = 1;
@@ -328,7 +333,20 @@ bool load_problem(Problem& P, const std::string& param_input, std::string& err) 
     P.bcx0 = dval(d[3][0], DBL_MAX); P.bcx1 = dval(d[3][1], DBL_MAX); P.bcy0 = dval(d[3][2], DBL_MAX);
     P.bcy1 = dval(d[3][3], DBL_MAX); P.bcz0 = dval(d[3][4], DBL_MAX); P.bc_refl = ival(d[3][5], INT_MAX);
     P.use_bcs = P.bcx0 != DBL_MAX || P.bcx1 != DBL_MAX || P.bcy0 != DBL_MAX || P.bcy1 != DBL_MAX || P.bcz0 != DBL_MAX;
-    if (!d[4][0].empty()) { err = "custom point files are not supported"; return false; }
+    // custom points, read as Init::FileRead_Points does (src/Init.cpp:816-857): the first
+    // line is skipped; then, point by point, the rest of the current line is skipped and
+    // three numbers are read (mm), until a read fails
+    P.custom = !d[4][0].empty();
+    if (P.custom) {
+      std::ifstream in(resolve(P.dir, d[4][0]));
+      if (!in) { err = "cannot open the points file"; return false; }
+      std::string line;
+      double x = 0, y = 0, z = 0;
+      while (std::getline(in, line) && (in >> x >> y >> z)) {
+        P.cx.push_back(x / 1000.0); P.cy.push_back(y / 1000.0); P.cz.push_back(z / 1000.0);
+      }
+      if (P.cx.empty()) { err = "no points in the points file"; return false; }
+    }
 
     double sx0 = DBL_MAX, sx1 = -DBL_MAX, sy0 = DBL_MAX, sy1 = -DBL_MAX, sz0 = DBL_MAX, sz1 = -DBL_MAX;
     double px = 0, py = 0, pz = 0, pq = 0; bool first = true;
@@ -353,18 +371,26 @@ bool load_problem(Problem& P, const std::string& param_input, std::string& err) 
     if (P.zmin == -DBL_MAX) P.zmin = sz0 - 250e-6;
     if (P.zmax == DBL_MAX) P.zmax = sz1;
 
-    if (P.nx == INT_MAX) { P.nx = 1 + int(0.5 + (P.xmax - P.xmin) / P.xres); P.xmax = P.xmin + (P.nx - 1) * P.xres; }
-    else if (P.nx != 1) P.xres = (P.xmax - P.xmin) / (P.nx - 1);
-    else P.xres = DBL_MAX;
-    if (P.ny == INT_MAX) { P.ny = 1 + int(0.5 + (P.ymax - P.ymin) / P.yres); P.ymax = P.ymin + (P.ny - 1) * P.yres; }
-    else if (P.ny != 1) P.yres = (P.ymax - P.ymin) / (P.ny - 1);
-    else P.yres = DBL_MAX;
-    if (P.nz == INT_MAX) { P.nz = 1 + int(0.5 + (P.zmax - P.zmin) / P.zres); P.zmax = P.zmin + (P.nz - 1) * P.zres; }
-    else if (P.ny != 1) P.zres = (P.zmax - P.zmin) / (P.nz - 1);   // the reference tests ynum here
-    else P.zres = DBL_MAX;
-    if (P.nx <= 0 || P.ny <= 0 || P.nz <= 0 || P.nx > 65535 || P.ny > 65535 || P.nz > 65535) { err = "grid size out of range"; return false; }
-    P.pnum = (long)P.nx * P.ny * P.nz;
-    P.gx = (uint16_t)P.nx; P.gy = (uint16_t)P.ny; P.gz = (uint16_t)P.nz;
+    if (P.custom) {                   // no grid (src/Init.cpp:866-869), and no tracking (src/Run.cpp:61, 391)
+      P.nx = (int)P.cx.size(); P.ny = P.nz = 1;
+      P.pnum = (long)P.cx.size();
+      P.gx = P.gy = P.gz = 1;
+      P.tracking = TRACK_NONE;
+    } else {
+      if (P.tracking < 0) { err = "snapshot tracking modes other than None are not supported"; return false; }
+      if (P.nx == INT_MAX) { P.nx = 1 + int(0.5 + (P.xmax - P.xmin) / P.xres); P.xmax = P.xmin + (P.nx - 1) * P.xres; }
+      else if (P.nx != 1) P.xres = (P.xmax - P.xmin) / (P.nx - 1);
+      else P.xres = DBL_MAX;
+      if (P.ny == INT_MAX) { P.ny = 1 + int(0.5 + (P.ymax - P.ymin) / P.yres); P.ymax = P.ymin + (P.ny - 1) * P.yres; }
+      else if (P.ny != 1) P.yres = (P.ymax - P.ymin) / (P.ny - 1);
+      else P.yres = DBL_MAX;
+      if (P.nz == INT_MAX) { P.nz = 1 + int(0.5 + (P.zmax - P.zmin) / P.zres); P.zmax = P.zmin + (P.nz - 1) * P.zres; }
+      else if (P.ny != 1) P.zres = (P.zmax - P.zmin) / (P.nz - 1);   // the reference tests ynum here
+      else P.zres = DBL_MAX;
+      if (P.nx <= 0 || P.ny <= 0 || P.nz <= 0 || P.nx > 65535 || P.ny > 65535 || P.nz > 65535) { err = "grid size out of range"; return false; }
+      P.pnum = (long)P.nx * P.ny * P.nz;
+      P.gx = (uint16_t)P.nx; P.gy = (uint16_t)P.ny; P.gz = (uint16_t)P.nz;
+    }
   }
   // outputs (src/Init.cpp:709-771)
   {
@@ -719,9 +745,19 @@ inline int pk_(const Problem& P, long p) { return (int)(p % P.nz); }
 inline long pid(const Problem& P, int i, int j, int k) { return (long)i * ((long)P.nz * P.ny) + (long)j * P.nz + k; }
 
 // Point coordinates from indices (src/Grid.h:310-327); the grid keeps uint16_t counts.
-inline double px_(const Problem& P, long p) { return (P.gx - 1) ? P.xmin + (double(pi_(P, p)) * ((P.xmax - P.xmin) / (P.gx - 1))) : P.xmax; }
-inline double py_(const Problem& P, long p) { return (P.gy - 1) ? P.ymin + (double(pj_(P, p)) * ((P.ymax - P.ymin) / (P.gy - 1))) : P.ymax; }
-inline double pz_(const Problem& P, long p) { return (P.gz - 1) ? P.zmin + (double(pk_(P, p)) * ((P.zmax - P.zmin) / (P.gz - 1))) : P.zmax; }
+// Custom points keep their own coordinates.
+inline double px_(const Problem& P, long p) {
+  if (P.custom) return P.cx[p];
+  return (P.gx - 1) ? P.xmin + (double(pi_(P, p)) * ((P.xmax - P.xmin) / (P.gx - 1))) : P.xmax;
+}
+inline double py_(const Problem& P, long p) {
+  if (P.custom) return P.cy[p];
+  return (P.gy - 1) ? P.ymin + (double(pj_(P, p)) * ((P.ymax - P.ymin) / (P.gy - 1))) : P.ymax;
+}
+inline double pz_(const Problem& P, long p) {
+  if (P.custom) return P.cz[p];
+  return (P.gz - 1) ? P.zmin + (double(pk_(P, p)) * ((P.zmax - P.zmin) / (P.gz - 1))) : P.zmax;
+}
 
 double sum_T(Problem& P, const Nodes& N, long p) {                           // src/Grid.cpp:281-298
   const double xp = px_(P, p), yp = py_(P, p), zp = pz_(P, p);

@@ -126,3 +126,21 @@ def test_reference_rrdf_binary_layout():
     assert np.array_equal(b["geometry"][:3], [ax.vmin for ax in deck.axes])
     assert b["geometry"][4] == deck.material.TL
     assert make_golden.rrdf_digest(b["idx"], b["ts"], b["Ts"]) == str(g["digest"])
+
+
+@pytest.mark.parametrize("name", make_golden.CUSTOM_DECKS)
+def test_oracle_custom_points_match_reference(name, oracle, tmp_path):
+    """Custom point files (Domain: Custom File, src/Init.cpp:686-703, 816-857): the oracle
+    reads the same points and runs them without tracking as the reference does - every
+    snapshot's T, or the solidification run's T, tSol, G, V and dTdt, bit for bit."""
+    g = _load(f"{name}.npz")
+    deck = make_golden.custom_deck(name)
+    o = oracle(deck.write(str(tmp_path / name)))
+    assert o.pnum == int(g["info"][3]) == len(deck.points)
+    if deck.mode == "Snapshots":
+        for i in range(o.n_snapshots):
+            assert np.array_equal(o.snapshot(i, threads=2), g[f"T{i}"]), i
+    else:
+        o.solidify(threads=2)
+        for f in ("T", "tSol", "G", "V", "dTdt"):
+            assert np.array_equal(o.field(f), g[f]), f
